@@ -1,0 +1,246 @@
+/*
+ * mma_tdse.h -- C-ABI of the GB300 TDSE library (libmma_gb300.so).
+ *
+ * Two surfaces:
+ *
+ * 1. The legacy surface: exactly the symbols and record layouts that the
+ *    reference DLL exports and that its Python host binds
+ *    (1DTDSE/PythonTDSE.py:48-220, structures 1DTDSE/sources/structures.h:16-147).
+ *    A host that loads this library instead of libsingleTDSE.so runs the CUDA
+ *    kernels with no other change.  Arrays are host memory allocated with calloc,
+ *    as in the reference, and freed by the destructors below.  Unlike the
+ *    reference these calls never exit() or print-and-continue: a failure leaves
+ *    outputs untouched (or zeroed) and records a status, read back with
+ *    mma_last_error() / mma_last_error_message() (thread-local).
+ *
+ * 2. The batched device surface (mma_tdse_*): many instances, device pointers
+ *    (e.g. torch tensors' data_ptr), caller-allocated buffers, a CUDA stream.
+ *    Every call returns an mma_status.
+ */
+#ifndef MMA_TDSE_H
+#define MMA_TDSE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------- */
+/* Status codes                                                               */
+/* ------------------------------------------------------------------------- */
+typedef enum {
+    MMA_OK = 0,
+    MMA_ERR_ARG = 1,          /* invalid argument (sizes, NaN/inf inputs, null pointers) */
+    MMA_ERR_GS_NOCONV = 2,    /* ground state did not reach |dE| <= CV within max_iter (reference: exit) */
+    MMA_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+    MMA_ERR_CUFFT = 4,        /* a cuFFT call failed */
+    MMA_ERR_TOO_LARGE = 5,    /* grid does not fit the selected kernel's limits */
+    MMA_ERR_NO_DEVICE = 6,    /* no CUDA device: there is no CPU fallback */
+    MMA_ERR_UNSUPPORTED = 7   /* option the reference accepts but never implemented (velocity gauge) */
+} mma_status;
+
+/* ------------------------------------------------------------------------- */
+/* Legacy records (byte-identical to 1DTDSE/sources/structures.h:16-147)      */
+/* ------------------------------------------------------------------------- */
+typedef struct Efield_var {
+    double *tgrid;
+    double *Field;
+    double dt;
+    double omega;
+    double E0;
+    double phi;
+    double ton;
+    double toff;
+    int Nt;
+    int nc;
+} Efield_var;
+
+typedef struct trg_def {
+    double a;
+} trg_def;
+
+typedef struct analy_def {
+    double tprint;
+    int writewft;
+} analy_def;
+
+typedef struct output_print_def {
+    int Efield;
+    int FEfield;
+    int sourceterm;
+    int Fsourceterm;
+    int FEfieldM2;
+    int FsourceTermM2;
+    int PopTot;
+    int tgrid;
+    int omegagrid;
+    int PopInt;
+    int expval_x;
+} output_print_def;
+
+typedef struct inputs_def {
+    struct trg_def trg;
+    struct Efield_var Efield;
+    double Eguess;
+    double Einit;
+    double tmin;
+    int Nt;
+    int num_t;
+    double dt;
+    int num_r;
+    double dx;
+    double *psi0;
+    double *x;
+    int gauge;
+    double x_int;
+    struct analy_def analy;
+    int InterpByDTorNT;
+    int Ntinterp;
+    struct output_print_def Print;
+    double CV;
+    char precision[2];
+} inputs_def;
+
+typedef struct outputs_def {
+    double *tgrid;
+    double *Efield;
+    double *sourceterm;
+    double *omegagrid;
+    double *FEfield;
+    double *Fsourceterm;
+    double *FEfieldM2;
+    double *FsourcetermM2;
+    double *PopTot;
+    double *PopInt;
+    double *expval;
+    int Nt;
+    int Nomega;
+    double **psi;
+} outputs_def;
+
+/* ------------------------------------------------------------------------- */
+/* Legacy entry points                                                         */
+/* ------------------------------------------------------------------------- */
+
+/* Replaces Initialise_grid_and_ground_state (1DTDSE/sources/tools.c:31; bound at
+ * PythonTDSE.py:58-61).  Allocates in->x (num_r+1) and in->psi0 (2(num_r+1)),
+ * fills the grid and the ground state by inverse iteration on the GPU, sets
+ * in->Einit.  Non-convergence within 1000 iterations sets MMA_ERR_GS_NOCONV. */
+void Initialise_grid_and_ground_state(inputs_def *in);
+
+/* Replaces call1DTDSE (1DTDSE/sources/singleTDSE.c:28; bound at PythonTDSE.py:75-78).
+ * Reads in->Efield (set_time_and_field), in->psi0, in->x; allocates and fills every
+ * output array of *out like the reference (lengths Nt+2, Nomega, 2 Nomega), and
+ * out->psi when in->analy.writewft is set.  Updates in->Efield.dt, in->num_t and
+ * in->Ntinterp as the reference does. */
+void call1DTDSE(inputs_def *in, outputs_def *out);
+
+/* Replaces set_time_and_field (1DTDSE/sources/tools.c:423; PythonTDSE.py:216-220):
+ * copies N samples of time and field into calloc'ed in->Efield.tgrid / .Field. */
+void set_time_and_field(inputs_def *in, double *time, double *field, int N);
+
+/* Replace Set_all_prints / Initialise_Printing_struct (structures.c:92,116). */
+output_print_def Set_all_prints(void);
+output_print_def Initialise_Printing_struct(void);
+
+/* Replace outputs_destructor / inputs_destructor (structures.c:15,55), free_arr
+ * (tools.c:408) and free_mtrx (structures.c:76).  Same ownership rules. */
+void outputs_destructor(outputs_def *out);
+void inputs_destructor(inputs_def *in);
+void free_arr(double *buf);
+void free_mtrx(double **buf, int n_rows);
+
+/* Status of the last legacy call on this thread (no reference counterpart). */
+int mma_last_error(void);
+const char *mma_last_error_message(void);
+
+/* ------------------------------------------------------------------------- */
+/* Batched device surface                                                      */
+/* ------------------------------------------------------------------------- */
+
+/* Threads per CTA of the TDSE kernels; the per-grid tables are laid out for it. */
+#define MMA_TDSE_THREADS 256
+
+/* One spatial grid (soft-Coulomb target, spacing, time step).  All pointers are
+ * device pointers to caller-allocated memory; sizes follow from n and m:
+ *   n   = num_r + 1 sites,  m = ceil(n / MMA_TDSE_THREADS) sites per thread,
+ *   L   = m * MMA_TDSE_THREADS (padded length)
+ *   x        [n]           grid x_k = k dx - num_r dx / 2        (written by build)
+ *   gv       [n]           -dV/dx = x (a^2+x^2)^-3/2              (written by build)
+ *   psi0     [2n]          ground state, interleaved re/im       (written by build)
+ *   cn_tab   [14 L]        Crank-Nicolson solve tables (complex)  (written by build)
+ *   gs_tab   [5 L]         ground-state solve tables (real)       (written by build)
+ *   result   [4]           {Einit, iterations, status, |dE| at stop}
+ * The record has 8-byte fields only, so its layout is the same in every ABI. */
+typedef struct mma_tdse_grid {
+    int64_t n, m;
+    double dx, trg_a, dt, x_int, Eguess, CV;
+    int64_t max_iter;
+    double *x, *gv, *psi0, *cn_tab, *gs_tab, *result;
+} mma_tdse_grid;
+
+/* One TDSE instance of a batch (offsets are in doubles). */
+typedef struct mma_tdse_instance {
+    int64_t grid;        /* index into the grid array */
+    int64_t n_steps;     /* propagation steps S = k1 * n_field_raw + 2 (the reference's outputs.Nt) */
+    int64_t field_off;   /* this instance's refined field samples in buffers.fields */
+    int64_t n_field;     /* refined field samples (k1 * n_field_raw); later samples read as 0 */
+    int64_t out_off;     /* six series of S+1 doubles: tgrid|Efield|sourceterm|PopTot|PopInt|expval */
+    int64_t psi_off;     /* final wavefunction (2n doubles) in buffers.psi_final, or -1 */
+    int64_t snap_off;    /* wavefunction snapshots (n_snap x 2n) in buffers.snapshots, or -1 */
+    int64_t snap_every;  /* snapshot after step k when k % snap_every == 0 (prop.c:248-263) */
+    int64_t n_snap;      /* snapshots kept; the last slot always holds the final state */
+    double tmin;         /* start time (the reference's inputs.tmin) */
+    double gate_floor;   /* |f| <= gate_floor counts as 0 in the zero-gate test (0 = exact) */
+} mma_tdse_instance;
+
+typedef struct mma_tdse_buffers {
+    const double *fields;  /* device */
+    double *outputs;       /* device */
+    double *psi_final;     /* device or NULL */
+    double *snapshots;     /* device or NULL */
+    int *counter;          /* device int: work-queue head, zeroed by the call on its stream */
+    void *scratch;         /* device, mma_tdse_scratch_bytes() bytes */
+    size_t scratch_bytes;
+} mma_tdse_buffers;
+
+/* Build x, -V', ground state and the solve tables of n_grids grids (device array
+ * `grids_dev`, host copy `grids_host` for validation).  One CTA per grid.
+ * mode 0: everything; mode 1: CN tables only, from the x and psi0 already in the
+ * grid's buffers (a caller-supplied ground state). */
+int mma_tdse_build_grids(const mma_tdse_grid *grids_dev, const mma_tdse_grid *grids_host, int n_grids, int mode,
+                         void *stream);
+
+/* Propagate n_inst instances in one persistent launch (one CTA per instance at a
+ * time, instances pulled from a device work queue).
+ *   max_m      largest grid m in the batch (sizes shared memory and scratch)
+ *   grid_ctas  persistent CTAs to launch (0 = as many as are resident at once)
+ *   precision  0 = FP64, the reference's arithmetic */
+int mma_tdse_propagate(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
+                       const mma_tdse_buffers *bufs, int max_m, int grid_ctas, int precision, void *stream);
+
+/* Scratch bytes mma_tdse_propagate needs for these arguments. */
+size_t mma_tdse_scratch_bytes(int max_m, int grid_ctas, int precision);
+
+/* Persistent CTAs mma_tdse_propagate launches when grid_ctas is 0. */
+int mma_tdse_default_ctas(int max_m, int precision);
+
+/* Fourier interpolation (1DTDSE/sources/tools_fftw3.c:24-68) of n_batch fields of
+ * equal length n_raw (rows of `raw`, contiguous) by factor k1 into `interp`
+ * (k1*n_raw per row): real DFT, zero padding, inverse DFT, 1/n_raw (cuFFT).
+ * For k1 = 1 the interpolation is the identity and the samples are copied
+ * exactly (the reference's round trip only adds round-off). */
+int mma_tdse_prepare_fields(const double *raw, int n_batch, int n_raw, int k1, double *interp, void *stream);
+
+/* Spectra of the sourceterm and Efield series (tools_fftw3.c:84-143) for n_batch
+ * instances with equal n_out (= n_steps): omega [n_omega], F [2 n_omega] and
+ * M2 [n_omega] for each row; series are read at stride `series_stride`. */
+int mma_tdse_spectra(const double *series, int64_t series_stride, int n_batch, int n_out, double dt, double tmax,
+                     double *fsig, int64_t fsig_stride, double *fm2, int64_t fm2_stride, double *omega, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

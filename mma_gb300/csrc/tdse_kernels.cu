@@ -1,0 +1,586 @@
+// tdse_kernels.cu -- GB300 kernels for the 1D-TDSE single-atom response.
+//
+//   build_grids_kernel     grid, -V', ground state (inverse iteration) and the solve
+//                          tables of each grid; one CTA per grid.
+//   propagate_fp64_kernel  the Crank-Nicolson-Numerov propagation in FP64, one
+//                          persistent CTA per instance pulled from a device work
+//                          queue, wavefunction resident in shared memory for the
+//                          whole pulse, observables reduced in-kernel every step.
+//
+// Reference map (1DTDSE/sources):
+//   grid                 tools.c:62-79            x_k = k dx - num_r dx/2
+//   potential, gradient  tools.c:91-113           V = -(a^2+x^2)^-1/2, -V' = x (a^2+x^2)^-3/2
+//   ground state         tridiag.c:86-238,251-274 inverse iteration with (K - Eg M2), M2 psi rhs
+//   CN-Numerov step      prop.c:137-205           (M2 + i dt/2 K) psi' = (M2 - i dt/2 K) psi, phase e^{+iE dt x}
+//   observables          prop.c:293-347           |<psi0|psi>|^2, window population, <x>, -<V'> + E
+//   zero gate, time grid prop.c:118-134,241-242
+#include <cuda_runtime.h>
+
+#include "../../include/mma_tdse.h"
+#include "common.cuh"
+#include "tdse_solver.cuh"
+
+namespace mma {
+
+// Slots of the complex CN table (each L = m*kThreads complex entries, chunk-interleaved).
+enum { CN_IB6 = 0, CN_H, CN_F, CN_G, CN_GG, CN_PSI0, CN_GVX, CN_SLOTS };
+// Slots of the real ground-state table.
+enum { GS_IB12 = 0, GS_H, GS_F, GS_G, GS_GG, GS_SLOTS };
+
+__device__ __forceinline__ double soft_coulomb(double x, double a) { return -1.0 / sqrt(a * a + x * x); }
+__device__ __forceinline__ double minus_grad_v(double x, double a) { return x * pow(a * a + x * x, -1.5); }
+
+__device__ __forceinline__ int64_t qidx(int64_t j, int64_t m) { return (j % m) * kThreads + (j / m); }
+
+// ------------------------------------------------------------------------------------------
+// Sequential factorisation of one tridiagonal matrix (thread 0), results chunk-interleaved.
+// Row j: sub a_j (column j-1), diagonal b_j, super c_j (column j+1).
+// ------------------------------------------------------------------------------------------
+template <typename T, typename RowFn>
+__device__ void factorise(int64_t n, int64_t m, T* ib, T* h, T* g, double rhs_scale, RowFn row)
+{
+    T a, b, c, beta, ibeta;
+    row(0, a, b, c);
+    beta = b;
+    T one;
+    if constexpr (sizeof(T) == sizeof(double)) one = 1.0; else one = cd{1.0, 0.0};
+    for (int64_t j = 0; j < n; j++) {
+        T aj, bj, cj;
+        row(j, aj, bj, cj);
+        if (j > 0) {
+            // gamma_j = c_{j-1}/beta_{j-1} ; beta_j = b_j - a_j gamma_j
+            T gam;
+            if constexpr (sizeof(T) == sizeof(double)) gam = c / beta; else gam = cdiv(c, beta);
+            g[qidx(j - 1, m)] = gam;
+            if constexpr (sizeof(T) == sizeof(double)) beta = bj - aj * gam; else beta = bj - cmul(aj, gam);
+        }
+        if constexpr (sizeof(T) == sizeof(double)) {
+            ibeta = 1.0 / beta;
+            ib[qidx(j, m)] = ibeta * rhs_scale;
+            h[qidx(j, m)] = (j > 0) ? aj * ibeta : 0.0;
+        } else {
+            ibeta = cdiv(one, beta);
+            ib[qidx(j, m)] = cd{ibeta.re * rhs_scale, ibeta.im * rhs_scale};
+            h[qidx(j, m)] = (j > 0) ? cmul(aj, ibeta) : cd{0.0, 0.0};
+        }
+        c = cj;
+        a = aj;
+    }
+    g[qidx(n - 1, m)] = T{};
+}
+
+// Chunk products F (forward from the chunk start) and G (backward from the chunk end).
+template <typename T>
+__device__ void chunk_products(int64_t m, const T* h, const T* g, T* F, T* G)
+{
+    const int t = threadIdx.x;
+    T p;
+    if constexpr (sizeof(T) == sizeof(double)) p = 1.0; else p = cd{1.0, 0.0};
+    for (int64_t i = 0; i < m; i++) {
+        int64_t q = i * kThreads + t;
+        T mh;
+        if constexpr (sizeof(T) == sizeof(double)) mh = -h[q]; else mh = cd{-h[q].re, -h[q].im};
+        p = mul_(p, mh);
+        F[q] = p;
+    }
+    if constexpr (sizeof(T) == sizeof(double)) p = 1.0; else p = cd{1.0, 0.0};
+    for (int64_t i = m - 1; i >= 0; i--) {
+        int64_t q = i * kThreads + t;
+        T mg;
+        if constexpr (sizeof(T) == sizeof(double)) mg = -g[q]; else mg = cd{-g[q].re, -g[q].im};
+        p = mul_(p, mg);
+        G[q] = p;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Ground state by shifted inverse iteration (tridiag.c:86-159): psi <- (K - Eg M2)^-1 M2 psi,
+// normalise, Numerov energy quotient; stop when |E - E_old| <= CV.  Real arithmetic: the
+// matrix and the start vector psi = 1 are real, so the reference's imaginary parts stay 0.
+// ------------------------------------------------------------------------------------------
+__device__ void ground_state(const mma_tdse_grid& G, const double* tab, double* psi, double* yl, double* vq,
+                             double* red, double* sc, double* sb, double* out_psi0)
+{
+    const int t = threadIdx.x;
+    const int64_t n = G.n, m = G.m, L = m * kThreads;
+    const double* ib12 = tab + GS_IB12 * L;
+    const double* hh = tab + GS_H * L;
+    const double* FF = tab + GS_F * L;
+    const double* gg = tab + GS_G * L;
+    const double* GG = tab + GS_GG * L;
+    const double inv_dx2 = 1.0 / (G.dx * G.dx);
+    for (int64_t i = 0; i < m; i++) {
+        int64_t j = t * m + i, q = i * kThreads + t;
+        psi[q] = (j < n) ? 1.0 : 0.0;  // tools.c:39-42
+        vq[q] = (j < n) ? soft_coulomb(G.x[j], G.trg_a) : 0.0;
+    }
+    __syncthreads();
+    double e_old = G.Eguess, energy = G.Eguess, test = 0.0;
+    int64_t it = 0;
+    int status = MMA_OK;
+    for (;;) {
+        // ---- solve (K - Eg M2) res = M2 psi
+        double pm = (t == 0) ? 0.0 : psi[(m - 1) * kThreads + t - 1];
+        double pc = psi[t];
+        double yprev = 0.0;
+        for (int64_t i = 0; i < m; i++) {
+            int64_t q = i * kThreads + t;
+            double pn = (i + 1 < m) ? psi[q + kThreads] : ((t + 1 < kThreads) ? psi[t + 1] : 0.0);
+            double r = fma(10.0, pc, pm + pn);
+            double y = fma(-hh[q], yprev, ib12[q] * r);
+            yl[q] = y;
+            yprev = y;
+            pm = pc;
+            pc = pn;
+        }
+        double yin = scan_forward<double>(FF[(m - 1) * kThreads + t], yprev, sc, sb);
+        double unext = 0.0;
+        for (int64_t i = m - 1; i >= 0; i--) {
+            int64_t q = i * kThreads + t;
+            double y = fma(FF[q], yin, yl[q]);
+            double u = fma(-gg[q], unext, y);
+            yl[q] = u;
+            unext = u;
+        }
+        double uin = scan_backward<double>(GG[t], unext, sc + kWarps, sb + kWarps);
+        double s2[1] = {0.0};
+        for (int64_t i = 0; i < m; i++) {
+            int64_t q = i * kThreads + t;
+            double u = fma(GG[q], uin, yl[q]);
+            yl[q] = u;
+            s2[0] = fma(u, u, s2[0]);
+        }
+        block_sum<1>(s2, red);  // normalise (tools.c:137-145)
+        const double nrm = sqrt(s2[0]);
+        for (int64_t i = 0; i < m; i++) {
+            int64_t q = i * kThreads + t;
+            psi[q] = yl[q] / nrm;
+        }
+        __syncthreads();
+        // ---- energy quotient (tridiag.c:172-238)
+        double acc[2] = {0.0, 0.0};
+        pm = (t == 0) ? 0.0 : psi[(m - 1) * kThreads + t - 1];
+        double vm = (t == 0) ? 0.0 : vq[(m - 1) * kThreads + t - 1];
+        pc = psi[t];
+        double vc = vq[t];
+        for (int64_t i = 0; i < m; i++) {
+            int64_t q = i * kThreads + t;
+            double pn = (i + 1 < m) ? psi[q + kThreads] : ((t + 1 < kThreads) ? psi[t + 1] : 0.0);
+            double vn = (i + 1 < m) ? vq[q + kThreads] : ((t + 1 < kThreads) ? vq[t + 1] : 0.0);
+            double kpsi = inv_dx2 * pc - 0.5 * inv_dx2 * (pm + pn) + (10.0 / 12.0) * pc * vc + (pm * vm + pn * vn) / 12.0;
+            double mpsi = 10.0 * pc / 12.0 + (pm + pn) / 12.0;
+            acc[0] = fma(kpsi, mpsi, acc[0]);
+            acc[1] = fma(mpsi, mpsi, acc[1]);
+            pm = pc;
+            pc = pn;
+            vm = vc;
+            vc = vn;
+        }
+        block_sum<2>(acc, red);
+        energy = acc[0] / acc[1];
+        test = fabs(energy - e_old);
+        e_old = energy;
+        ++it;
+        if (it >= G.max_iter) {
+            status = MMA_ERR_GS_NOCONV;
+            break;
+        }
+        if (!(test > G.CV)) break;
+    }
+    // final normalisation (tridiag.c:150)
+    double s2[1] = {0.0};
+    for (int64_t i = 0; i < m; i++) {
+        int64_t q = i * kThreads + t;
+        s2[0] = fma(psi[q], psi[q], s2[0]);
+    }
+    block_sum<1>(s2, red);
+    const double nrm = sqrt(s2[0]);
+    for (int64_t i = 0; i < m; i++) {
+        int64_t j = t * m + i, q = i * kThreads + t;
+        if (j < n) {
+            out_psi0[2 * j] = psi[q] / nrm;
+            out_psi0[2 * j + 1] = 0.0;
+        }
+    }
+    if (t == 0) {
+        G.result[0] = energy;
+        G.result[1] = (double)it;
+        G.result[2] = (double)status;
+        G.result[3] = test;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Grid builder.  mode 0: x, ground state, CN tables.  mode 1: CN tables from the grid's
+// existing x and psi0 (a caller-supplied ground state, as the legacy call1DTDSE allows).
+// ------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) build_grids_kernel(const mma_tdse_grid* grids, int mode)
+{
+    __shared__ double red[kWarps * 4];
+    __shared__ double sc[2 * kWarps], sb[2 * kWarps];
+    const mma_tdse_grid G = grids[blockIdx.x];
+    const int t = threadIdx.x;
+    const int64_t n = G.n, m = G.m, L = m * kThreads, num_r = n - 1;
+    const double dx = G.dx, a = G.trg_a, dt = G.dt;
+
+    if (mode == 0) {
+        // separately rounded multiply and subtract, as the reference's x86 build evaluates
+        // (double)k dx - xmax (no fused multiply-add)
+        const double xmax = __dmul_rn(__dmul_rn(0.5, (double)num_r), dx);
+        for (int64_t j = t; j < n; j += kThreads) G.x[j] = __dsub_rn(__dmul_rn((double)j, dx), xmax);
+        __syncthreads();
+        // ground-state tables (tridiag.c:101-115)
+        double* gtab = G.gs_tab;
+        for (int64_t q = t; q < GS_SLOTS * L; q += kThreads) gtab[q] = 0.0;
+        __syncthreads();
+        if (t == 0) {
+            const double E = G.Eguess, k0 = -0.5 / (dx * dx), d0 = 1.0 / (dx * dx);
+            auto row = [&](int64_t j, double& aj, double& bj, double& cj) {
+                double vj = soft_coulomb(G.x[j], a);
+                aj = (j > 0) ? k0 - E / 12.0 + soft_coulomb(G.x[j - 1], a) / 12.0 : 0.0;
+                bj = 10.0 * vj / 12.0 + d0 - 10.0 * E / 12.0;
+                cj = (j + 1 < n) ? k0 - E / 12.0 + soft_coulomb(G.x[j + 1], a) / 12.0 : 0.0;
+            };
+            factorise<double>(n, m, gtab + GS_IB12 * L, gtab + GS_H * L, gtab + GS_G * L, 1.0 / 12.0, row);
+        }
+        __syncthreads();
+        chunk_products<double>(m, gtab + GS_H * L, gtab + GS_G * L, gtab + GS_F * L, gtab + GS_GG * L);
+        __syncthreads();
+        // the CN table area doubles as the ground-state work space (3 L of 2*CN_SLOTS*L)
+        double* work = G.cn_tab;
+        ground_state(G, gtab, work, work + L, work + 2 * L, red, sc, sb, G.psi0);
+        __syncthreads();
+    }
+    for (int64_t j = t; j < n; j += kThreads) G.gv[j] = minus_grad_v(G.x[j], a);
+    __syncthreads();
+    // Crank-Nicolson tables (prop.c:138-159): row j sub (1/12, w_{j-1}), diag (10/12, d_j),
+    // super (1/12, w_{j+1}); w_q = dt/2 (-1/(2dx^2) + V_q/12), d_q = dt/2 (1/dx^2 + 10 V_q/12).
+    // The right-hand side is 2 M2 psi = (psi_{j-1} + 10 psi_j + psi_{j+1})/6 and the new state
+    // is A^{-1}(2 M2 psi) - psi, which equals A^{-1} conj(A) psi because A + conj(A) = 2 M2.
+    cd* ctab = reinterpret_cast<cd*>(G.cn_tab);
+    for (int64_t q = t; q < CN_SLOTS * L; q += kThreads) ctab[q] = cd{0.0, 0.0};
+    __syncthreads();
+    if (t == 0) {
+        const double hdt = 0.5 * dt;
+        auto row = [&](int64_t j, cd& aj, cd& bj, cd& cj) {
+            double vj = soft_coulomb(G.x[j], a);
+            aj = (j > 0) ? cd{1.0 / 12.0, hdt * (-0.5 / (dx * dx)) + hdt * 1 / 12. * soft_coulomb(G.x[j - 1], a)}
+                         : cd{0.0, 0.0};
+            bj = cd{10.0 / 12.0, hdt * (1.0 / (dx * dx)) + hdt * 10 / 12. * vj};
+            cj = (j + 1 < n) ? cd{1.0 / 12.0, hdt * (-0.5 / (dx * dx)) + hdt * 1 / 12. * soft_coulomb(G.x[j + 1], a)}
+                             : cd{0.0, 0.0};
+        };
+        factorise<cd>(n, m, ctab + CN_IB6 * L, ctab + CN_H * L, ctab + CN_G * L, 1.0 / 6.0, row);
+    }
+    __syncthreads();
+    chunk_products<cd>(m, ctab + CN_H * L, ctab + CN_G * L, ctab + CN_F * L, ctab + CN_GG * L);
+    for (int64_t i = 0; i < m; i++) {
+        int64_t j = t * m + i, q = i * kThreads + t;
+        if (j < n) {
+            ctab[CN_PSI0 * L + q] = cd{G.psi0[2 * j], G.psi0[2 * j + 1]};
+            ctab[CN_GVX * L + q] = cd{G.gv[j], G.x[j]};
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// FP64 propagation.
+// ------------------------------------------------------------------------------------------
+struct PropArgs {
+    const mma_tdse_instance* insts;
+    int n_inst;
+    const mma_tdse_grid* grids;
+    const double* fields;
+    double* outputs;
+    double* psi_final;
+    double* snapshots;
+    int* counter;
+    double* scratch;  // per CTA: yl [L] complex, then (when psi is not in shared memory) psi [L] complex
+    int64_t max_L;
+};
+
+// First index where the reference's zero gate opens: the first k with f[k] f[k+1] <= 0
+// (prop.c:125-134); samples at and beyond n_field are zero, and samples with
+// |f| <= floor count as zero in this test (floor is 0 unless the field was
+// Fourier-interpolated, where it absorbs the transform's round-off).
+__device__ int64_t gate_index(const double* f, int64_t n_field, int64_t n_steps, double floor_)
+{
+    for (int64_t k = 0; k < n_steps; k++) {
+        double a = (k < n_field) ? f[k] : 0.0, b = (k + 1 < n_field) ? f[k + 1] : 0.0;
+        if (fabs(a) <= floor_) a = 0.0;
+        if (fabs(b) <= floor_) b = 0.0;
+        if (a * b <= 0.0) return k;
+    }
+    return n_steps;
+}
+
+template <bool PSI_SMEM>
+__global__ void __launch_bounds__(kThreads, 1) propagate_fp64_kernel(PropArgs P)
+{
+    extern __shared__ double2 smem_dyn[];
+    __shared__ cd sc[2 * kWarps], sb[2 * kWarps];
+    __shared__ double red[kWarps * 5];
+    __shared__ int64_t s_inst, s_gate, s_lo, s_hi;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    cd* yl = reinterpret_cast<cd*>(P.scratch) + blockIdx.x * P.max_L;
+    cd* psi = PSI_SMEM ? reinterpret_cast<cd*>(smem_dyn)
+                       : reinterpret_cast<cd*>(P.scratch) + (gridDim.x + blockIdx.x) * P.max_L;
+
+    for (;;) {
+        if (t == 0) s_inst = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int64_t inst = s_inst;
+        if (inst >= P.n_inst) break;
+        const mma_tdse_instance I = P.insts[inst];
+        const mma_tdse_grid G = P.grids[I.grid];
+        const int64_t n = G.n, m = G.m, L = m * kThreads, S = I.n_steps;
+        const cd* tab = reinterpret_cast<const cd*>(G.cn_tab);
+        const cd *ib6 = tab + CN_IB6 * L, *hh = tab + CN_H * L, *FF = tab + CN_F * L, *gg = tab + CN_G * L,
+                 *GG = tab + CN_GG * L, *P0 = tab + CN_PSI0 * L, *GVX = tab + CN_GVX * L;
+        const double* f = P.fields + I.field_off;
+        double* out = P.outputs + I.out_off;
+        double *o_t = out, *o_e = out + (S + 1), *o_src = out + 2 * (S + 1), *o_ptot = out + 3 * (S + 1),
+               *o_pint = out + 4 * (S + 1), *o_x = out + 5 * (S + 1);
+        const double dt = G.dt, dx = G.dx;
+
+        if (t == 0) {
+            s_gate = gate_index(f, I.n_field, S, I.gate_floor);
+            // PopInt window from the reference's findinterval (tools_algorithmic.c:19-43)
+            const int64_t num_r = n - 1;
+            int64_t lo = -1, hi;
+            if (!(-G.x_int < G.x[0])) {
+                int64_t i = 0;
+                while (i < num_r && !(-G.x_int <= G.x[i + 1])) i++;
+                lo = i;
+            }
+            if (G.x_int < G.x[0]) {
+                hi = 0;
+            } else {
+                int64_t i = 0;
+                while (i < num_r && !(G.x_int <= G.x[i + 1])) i++;
+                hi = (i < num_r) ? i + 1 : num_r + 1;
+            }
+            s_lo = lo < 0 ? 0 : lo;
+            s_hi = hi > num_r ? num_r : hi;
+        }
+        for (int64_t i = 0; i < m; i++) {
+            int64_t q = i * kThreads + t;
+            psi[q] = P0[q];
+        }
+        __syncthreads();
+        const int64_t lo = s_lo, hi = s_hi, gate = s_gate;
+        {   // initial window population (prop.c:87-93)
+            double v[1] = {0.0};
+            for (int64_t i = 0; i < m; i++) {
+                int64_t j = t * m + i, q = i * kThreads + t;
+                if (j >= lo && j <= hi) v[0] += psi[q].re * psi[q].re + psi[q].im * psi[q].im;
+            }
+            block_sum<1>(v, red);
+            if (t == 0) {
+                o_t[0] = I.tmin;
+                o_e[0] = 0.0;
+                o_src[0] = 0.0;
+                o_ptot[0] = 1.0;
+                o_pint[0] = v[0];
+                o_x[0] = 0.0;
+            }
+        }
+        double tt = I.tmin;
+        const int64_t s0 = t * m;
+        const double xs = (s0 < n) ? GVX[t].im : 0.0;
+
+        for (int64_t k = 0; k < S; k++) {
+            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : f[k];
+            if (t == 0) {
+                if (k > 0) {  // finish the previous step's observables
+                    double s[5];
+#pragma unroll
+                    for (int c = 0; c < 5; c++) {
+                        s[c] = 0.0;
+#pragma unroll
+                        for (int q = 0; q < kWarps; q++) s[c] += red[q * 5 + c];
+                    }
+                    o_src[k] = -s[0] + o_e[k];
+                    o_ptot[k] = s[2] * s[2] + s[3] * s[3];
+                    o_x[k] = s[1];
+                    o_pint[k] = s[4];
+                }
+                tt += dt;
+                o_t[k + 1] = tt;
+                o_e[k + 1] = Fk;
+            }
+            // ---- pass 1: local forward sweep of the right-hand side 2 M2 psi
+            cd pm = (t == 0) ? cd{0.0, 0.0} : psi[(m - 1) * kThreads + t - 1];
+            cd pc = psi[t];
+            cd yprev{0.0, 0.0};
+            for (int64_t i = 0; i < m; i++) {
+                int64_t q = i * kThreads + t;
+                cd pn = (i + 1 < m) ? psi[q + kThreads] : ((t + 1 < kThreads) ? psi[t + 1] : cd{0.0, 0.0});
+                cd r{fma(10.0, pc.re, pm.re + pn.re), fma(10.0, pc.im, pm.im + pn.im)};
+                cd y = cfms(hh[q], yprev, cmul(ib6[q], r));
+                yl[q] = y;
+                yprev = y;
+                pm = pc;
+                pc = pn;
+            }
+            const cd yin = scan_forward<cd>(FF[(m - 1) * kThreads + t], yprev, sc, sb);
+            // ---- pass 2: local backward sweep with the forward correction
+            cd unext{0.0, 0.0};
+            for (int64_t i = m - 1; i >= 0; i--) {
+                int64_t q = i * kThreads + t;
+                cd y = cfma(FF[q], yin, yl[q]);
+                cd u = cfms(gg[q], unext, y);
+                yl[q] = u;
+                unext = u;
+            }
+            const cd uin = scan_backward<cd>(GG[t], unext, sc + kWarps, sb + kWarps);
+            // ---- pass 3: backward correction, CN update, phase e^{+i F dt x}, observables
+            double sn, cs;
+            sincos(Fk * dt * xs, &sn, &cs);
+            cd ph{cs, sn};
+            sincos(Fk * dt * dx, &sn, &cs);
+            const cd z{cs, sn};
+            double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+            for (int64_t i = 0; i < m; i++) {
+                int64_t q = i * kThreads + t;
+                int64_t j = s0 + i;
+                cd u = cfma(GG[q], uin, yl[q]);
+                cd d = u - psi[q];
+                cd pn = cmul(ph, d);
+                psi[q] = pn;
+                ph = cmul(ph, z);
+                const double n2 = fma(pn.re, pn.re, pn.im * pn.im);
+                const cd gx = GVX[q];
+                const cd p0 = P0[q];
+                acc[0] = fma(n2, gx.re, acc[0]);
+                acc[1] = fma(n2, gx.im, acc[1]);
+                acc[2] = fma(pn.re, p0.re, fma(pn.im, p0.im, acc[2]));
+                acc[3] = fma(pn.re, p0.im, fma(-pn.im, p0.re, acc[3]));
+                if (j >= lo && j <= hi) acc[4] += n2;
+            }
+#pragma unroll
+            for (int c = 0; c < 5; c++)
+#pragma unroll
+                for (int d = 16; d >= 1; d >>= 1) acc[c] += shfl_xor(acc[c], d);
+            if (lane == 0)
+#pragma unroll
+                for (int c = 0; c < 5; c++) red[w * 5 + c] = acc[c];
+            if (I.snap_off >= 0 && P.snapshots) {  // prop.c:248-263
+                int64_t slot = -1;
+                if (k % I.snap_every == 0 && k / I.snap_every < I.n_snap - 1) slot = k / I.snap_every;
+                if (k == S - 1) slot = I.n_snap - 1;
+                if (slot >= 0) {
+                    double* sp = P.snapshots + I.snap_off + slot * 2 * n;
+                    for (int64_t i = 0; i < m; i++) {
+                        int64_t j = s0 + i;
+                        if (j < n) st2(sp + 2 * j, psi[i * kThreads + t]);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        if (t == 0) {
+            double s[5];
+#pragma unroll
+            for (int c = 0; c < 5; c++) {
+                s[c] = 0.0;
+#pragma unroll
+                for (int q = 0; q < kWarps; q++) s[c] += red[q * 5 + c];
+            }
+            o_src[S] = -s[0] + o_e[S];
+            o_ptot[S] = s[2] * s[2] + s[3] * s[3];
+            o_x[S] = s[1];
+            o_pint[S] = s[4];
+        }
+        if (P.psi_final && I.psi_off >= 0) {
+            double* pf = P.psi_final + I.psi_off;
+            for (int64_t i = 0; i < m; i++) {
+                int64_t j = s0 + i;
+                if (j < n) st2(pf + 2 * j, psi[i * kThreads + t]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace mma
+
+using namespace mma;
+
+// ------------------------------------------------------------------------------------------
+// Host entry points of the batched surface.
+// ------------------------------------------------------------------------------------------
+extern "C" int mma_tdse_build_grids(const mma_tdse_grid* grids_dev, const mma_tdse_grid* grids_host, int n_grids,
+                                    int mode, void* stream)
+{
+    if (n_grids <= 0 || !grids_dev || !grids_host || (mode != 0 && mode != 1)) return MMA_ERR_ARG;
+    for (int g = 0; g < n_grids; g++) {
+        const mma_tdse_grid& G = grids_host[g];
+        if (G.n < 3 || G.m < 1 || G.m * kThreads < G.n || !(G.dx > 0.0) || !(G.dt > 0.0) || !G.x || !G.gv ||
+            !G.psi0 || !G.cn_tab || !G.gs_tab || !G.result || !(G.trg_a == G.trg_a))
+            return MMA_ERR_ARG;
+        if (mode == 0 && G.max_iter < 1) return MMA_ERR_ARG;
+    }
+    build_grids_kernel<<<n_grids, kThreads, 0, (cudaStream_t)stream>>>(grids_dev, mode);
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
+
+static bool psi_fits_smem(int max_m) { return (size_t)max_m * kThreads * 16 <= 220 * 1024; }
+
+static int sm_count()
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+extern "C" int mma_tdse_default_ctas(int max_m, int precision)
+{
+    (void)precision;
+    const int sms = sm_count();
+    if (sms <= 0 || max_m < 1) return 0;
+    int per_sm = 1;
+    if (psi_fits_smem(max_m)) {
+        size_t smem = (size_t)max_m * kThreads * 16;
+        cudaFuncSetAttribute(propagate_fp64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, propagate_fp64_kernel<true>, kThreads, smem);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, propagate_fp64_kernel<false>, kThreads, 0);
+    }
+    return sms * (per_sm > 0 ? per_sm : 1);
+}
+
+extern "C" size_t mma_tdse_scratch_bytes(int max_m, int grid_ctas, int precision)
+{
+    if (grid_ctas <= 0) grid_ctas = mma_tdse_default_ctas(max_m, precision);
+    if (grid_ctas <= 0) grid_ctas = 1;
+    size_t per = (size_t)max_m * kThreads * 16;
+    return per * (size_t)grid_ctas * (psi_fits_smem(max_m) ? 1 : 2);
+}
+
+extern "C" int mma_tdse_propagate(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
+                                  const mma_tdse_buffers* bufs, int max_m, int grid_ctas, int precision, void* stream)
+{
+    if (n_inst <= 0) return MMA_OK;
+    if (!insts || !grids || !bufs || !bufs->fields || !bufs->outputs || !bufs->counter || !bufs->scratch ||
+        max_m < 1)
+        return MMA_ERR_ARG;
+    if (precision != 0) return MMA_ERR_UNSUPPORTED;
+    if (sm_count() <= 0) return MMA_ERR_NO_DEVICE;
+    if (grid_ctas <= 0) grid_ctas = mma_tdse_default_ctas(max_m, precision);
+    if (grid_ctas > n_inst) grid_ctas = n_inst;
+    if (bufs->scratch_bytes < mma_tdse_scratch_bytes(max_m, grid_ctas, precision)) return MMA_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(bufs->counter, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+    PropArgs A{insts, n_inst, grids, bufs->fields, bufs->outputs, bufs->psi_final, bufs->snapshots, bufs->counter,
+               (double*)bufs->scratch, (int64_t)max_m * kThreads};
+    if (psi_fits_smem(max_m)) {
+        size_t smem = (size_t)max_m * kThreads * 16;
+        cudaFuncSetAttribute(propagate_fp64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        propagate_fp64_kernel<true><<<grid_ctas, kThreads, smem, st>>>(A);
+    } else {
+        propagate_fp64_kernel<false><<<grid_ctas, kThreads, 0, st>>>(A);
+    }
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}

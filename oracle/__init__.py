@@ -1,0 +1,35 @@
+"""The oracle: CPU restatements of the reference algorithms on the 1D-TDSE -> Hankel path.
+
+TEST INFRASTRUCTURE ONLY -- imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, and never by the product package ``mma_gb300``.
+
+* ``tdse``   -- ctypes binding of ``_build/libmma_oracle.so`` (tdse_oracle.c), the C
+  restatement of 1DTDSE/sources.  ``ref_dll_path()`` points at the reference
+  DLL built unchanged from its sources (``make ref``) where those exist.
+* ``hankel`` -- numpy restatement of Hankel/Hankel_transform.py.
+"""
+import os
+import subprocess
+
+ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
+
+
+def build(ref=None):
+    """Compile the C restatement (always) and the reference DLL (when its sources
+    are present, or when ``ref`` is True)."""
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+    src = os.environ.get("MMA_REF_SRC", "/root/reference/1DTDSE/sources")
+    if ref is None:
+        ref = os.path.isdir(src)
+    if ref:
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref", "REF_SRC=" + src], check=True)
+
+
+def oracle_lib_path():
+    return os.path.join(ORACLE_DIR, "_build", "libmma_oracle.so")
+
+
+def ref_dll_path():
+    """Path of the reference DLL built from its own sources, or None."""
+    p = os.path.join(ORACLE_DIR, "_ref", "libsingleTDSE.so")
+    return p if os.path.exists(p) else None

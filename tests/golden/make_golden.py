@@ -1,0 +1,139 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+TDSE fixtures: the reference DLL compiled unchanged from its sources
+(1DTDSE/sources, see oracle/Makefile `ref`) driven through its own C-ABI by
+mma_gb300.tdse.TDSE_DLL -- the same host class that drives the GPU library.
+
+Hankel fixtures: the reference's Hankel/Hankel_transform.py imported from the
+reference checkout, with two modules it imports but this path does not use
+replaced in sys.modules: h5py (file I/O only) and XUV_refractive_index, whose
+dispersion_function/beta_factor_ref return the constant complex index of the
+synthetic medium (n = 1 - 1e-5 + 1e-7 i by default), and `gases`.
+
+Run from the repository root where the reference checkout exists:
+    python tests/golden/make_golden.py [--ref /root/reference]
+"""
+import argparse
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+from tdse_cases import A_CONFIG, sin2_pulse  # noqa: E402
+
+# Cases: name -> (run_single kwargs, pulse kwargs).  All pulses start one sample after
+# t = 0 so the reference's zero gate is decided by the field, not by FFT round-off.
+TDSE_CASES = {
+    "tdse_small": (dict(num_r=600, dx=0.4, trg_a=A_CONFIG), dict(n_cycles=2)),
+    "tdse_medium": (dict(num_r=2000, dx=0.2, trg_a=A_CONFIG), dict(n_cycles=3)),
+    # the parameters of the reference's own regression test (1DTDSE/tests.py:13-39)
+    "tdse_reftest": (dict(num_r=8000, dx=0.4, trg_a=1.0), dict(n_cycles=4, E0=0.14, omega=0.07)),
+    # field sampled at 0.5 a.u. > dt = 0.25: Fourier interpolation with k1 = 3
+    "tdse_interp": (dict(num_r=600, dx=0.4, trg_a=A_CONFIG), dict(n_cycles=2, dt=0.5)),
+    "tdse_snapshots": (dict(num_r=600, dx=0.4, trg_a=1.0, writewft=1, tprint=10.0), dict(n_cycles=1.5)),
+    # config 0 of the benchmark: a^2 = 1.68, x in [-400, 400], dx = 0.1, 10-cycle 800 nm pulse
+    "tdse_config0": (dict(num_r=8000, dx=0.1, trg_a=A_CONFIG), dict(n_cycles=10)),
+}
+
+
+def make_tdse(ref_src):
+    import oracle
+    from mma_gb300.tdse import TDSE_DLL, run_single
+
+    os.environ["MMA_REF_SRC"] = ref_src
+    oracle.build(ref=True)
+    dll = TDSE_DLL(oracle.ref_dll_path())
+    for name, (kw, pk) in TDSE_CASES.items():
+        t, E = sin2_pulse(skip_first=True, **pk)
+        r = run_single(dll, t, E, CV=1e-15, **kw)
+        out = dict(t=t, E=E, Einit=r["Einit"], psi0_re=np.real(r["psi0"]), x=r["x"],
+                   sourceterm=r["sourceterm"], PopTot=r["PopTot"], PopInt=r["PopInt"], expval=r["expval"],
+                   Efield=r["Efield"], tgrid=r["tgrid"], omegagrid=r["omegagrid"],
+                   Fsourceterm=r["Fsourceterm"], FsourcetermM2=r["FsourcetermM2"], FEfield=r["FEfield"],
+                   Nt=r["Nt"], Nomega=r["Nomega"], dt=r["dt"],
+                   params=np.array([kw["num_r"], kw["dx"], kw["trg_a"]]))
+        if "snapshots" in r and r["snapshots"] is not None:
+            out["snapshots"] = r["snapshots"]
+            out["tprint"] = kw["tprint"]
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, "Nt", r["Nt"], "Einit", r["Einit"])
+
+
+def import_reference_hankel(ref_root, n_xuv=complex(1 - 1e-5, 1e-7)):
+    """Import Hankel_transform.py from the reference with the two stubs described above."""
+    sys.modules["h5py"] = types.ModuleType("h5py")
+    xuv = types.ModuleType("XUV_refractive_index")
+    sys.path.insert(0, os.path.join(ref_root, "shared_python"))
+    import units  # the reference's own unit module
+
+    xuv.gases = ["Ar_Henke", "Ar_NIST"]
+    # n = n0 + i beta (XUV_refractive_index.py:164-167): 1/v_IR - 1/v_XUV = (n_IR - n0)/c
+    xuv.dispersion_function = lambda omega, pressure, gas, n_IR=1.0, **kw: \
+        pressure * (n_IR - n_xuv.real) / units.c_light * np.ones_like(np.asarray(omega, dtype=float))
+    xuv.beta_factor_ref = lambda omega, gas, **kw: n_xuv.imag * np.ones_like(np.asarray(omega, dtype=float))
+    sys.modules["XUV_refractive_index"] = xuv
+    sys.path.insert(0, os.path.join(ref_root, "Hankel"))
+    import Hankel_transform as HT
+
+    return HT, units
+
+
+HANKEL_CASES = {
+    # name: (No, Nr, Nz_planes, Nrho, gas, near_field, cumulative)
+    "hankel_small": (6, 24, 5, 12, "Ar", True, True),
+    "hankel_vacuum": (5, 20, 4, 10, "vacuum", True, False),
+    "hankel_far_only": (4, 16, 4, 8, "Ar", False, True),
+}
+
+
+def hankel_inputs(No, Nr, Nz, Nrho, seed=0):
+    """Seeded synthetic source with config-3 structure at small size: Gaussian radial
+    profile (50 um) times a comb of odd harmonics (11..41 of 800 nm, Lorentzian width
+    0.3 omega0) with random phases, complex64 like the production source."""
+    rng = np.random.default_rng(seed)
+    omega0 = 0.057 / 2.4188843265857e-17
+    zgrid = np.linspace(-5e-3, 5e-3, Nz + 1)  # +1: FSources_provider drops the last plane
+    rgrid = np.linspace(0.0, 200e-6, Nr)
+    ogrid = np.linspace(10 * omega0, 42 * omega0, No)
+    rho = np.linspace(0.0, 5e-3, Nrho)
+    q = np.arange(11, 42, 2)
+    phases = rng.uniform(0, 2 * np.pi, size=(Nz + 1, len(q)))
+    lor = 1.0 / (1.0 + ((ogrid[None, :] - q[:, None] * omega0) / (0.3 * omega0)) ** 2)
+    comb = np.einsum("zq,qo->zo", np.exp(1j * phases), lor)
+    prof = np.exp(-(rgrid / 50e-6) ** 2)
+    S = (comb[:, :, None] * prof[None, None, :]).astype(np.complex64)
+    S = S * (1.0 + 0.3 * rng.standard_normal(S.shape)).astype(np.float32)
+    return zgrid, rgrid, ogrid, rho, S
+
+
+def make_hankel(ref_root):
+    HT, units = import_reference_hankel(ref_root)
+    for name, (No, Nr, Nz, Nrho, gas, nff, cum) in HANKEL_CASES.items():
+        zgrid, rgrid, ogrid, rho, S = hankel_inputs(No, Nr, Nz, Nrho)
+        target = HT.FSources_provider(zgrid, rgrid, ogrid, data_source="static", FSource=S)
+        res = HT.Hankel_long(target, 1.0, rho, preset_gas=gas, pressure=1.0, near_field_factor=nff,
+                             store_cumulative_result=cum)
+        out = dict(zgrid=zgrid, rgrid=rgrid, ogrid=ogrid, rho=rho, S=S, FF_integrated=res.FF_integrated,
+                   entry=res.entry_plane_transform, exit=res.exit_plane_transform, distance=1.0,
+                   gas=np.bytes_(gas), near_field=nff, n_xuv=np.array([1 - 1e-5, 1e-7]))
+        if cum:
+            out["cumulative"] = res.cumulative_field
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, res.FF_integrated.shape)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", choices=["tdse", "hankel"], default=None)
+    a = ap.parse_args()
+    if a.only in (None, "tdse"):
+        make_tdse(os.path.join(a.ref, "1DTDSE", "sources"))
+    if a.only in (None, "hankel"):
+        make_hankel(a.ref)

@@ -1,0 +1,33 @@
+"""Shared TDSE test inputs (seeded, synthetic): sin^2-envelope 800 nm pulses on soft-Coulomb grids."""
+import numpy as np
+
+A_CONFIG = np.sqrt(1.68)  # soft-Coulomb a of the benchmark configurations (a^2 = 1.68)
+OMEGA0 = 0.057            # 800 nm in atomic units
+
+
+def sin2_pulse(n_cycles, E0=0.0534, omega=OMEGA0, dt=0.25, cep=0.0, even=True, skip_first=False):
+    """Field sampled at ~dt on t in [0, T], T = n_cycles 2 pi/omega; an even sample count
+    keeps the reference's last-step field read inside its interpolation buffer.
+
+    skip_first drops the t = 0 sample (where the field is exactly 0).  The reference's
+    zero gate tests f[0] f[1] <= 0 on its Fourier-interpolated field, so on a field that
+    starts at exactly 0 its decision follows the sign of FFT round-off; starting one
+    sample later makes the decision unambiguous for every implementation."""
+    T = n_cycles * 2 * np.pi / omega
+    n = int(T / dt) + 1
+    if skip_first:
+        n += 1
+    if even and (n - (1 if skip_first else 0)) % 2:
+        n += 1
+    t = np.linspace(0.0, T, n)
+    if skip_first:
+        t = t[1:]
+    E = E0 * np.sin(np.pi * t / T) ** 2 * np.cos(omega * t + cep)
+    return t, E
+
+
+def rel_l2(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
