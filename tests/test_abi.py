@@ -1,0 +1,136 @@
+"""The C-ABI boundary without a GPU: the library loads, exports every entry point
+declared in include/*.h, its records have the reference's byte layout, and the
+legacy calls report (rather than crash on) a missing device or bad arguments."""
+import ctypes
+import glob
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = sorted(glob.glob(os.path.join(ROOT, "include", "*.h")))
+
+
+def declared_functions():
+    names = []
+    for h in HEADERS:
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        src = "\n".join(l for l in src.split("\n") if not l.strip().startswith("#"))
+        src = src.replace('extern "C" {', "")
+        depth = 0
+        stmt = ""
+        for ch in src:
+            if ch == "{":
+                depth += 1
+            elif ch == "}":
+                depth = max(depth - 1, 0)
+                stmt = ""
+                continue
+            if depth:
+                continue
+            if ch == ";":
+                s = " ".join(stmt.split())
+                stmt = ""
+                if s.startswith("typedef") or s.startswith("#") or "(" not in s:
+                    continue
+                m = re.match(r"^(?:extern\s+\"C\"\s+)?[\w\s\*]+?\**\s*(\w+)\s*\(", s)
+                if m:
+                    names.append(m.group(1))
+            else:
+                stmt += ch
+    return sorted(set(names))
+
+
+def test_headers_declare_entry_points():
+    names = declared_functions()
+    assert "call1DTDSE" in names and "mma_tdse_propagate" in names
+    assert len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol():
+    from mma_gb300 import load
+
+    lib = load()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+STRUCTS = ["Efield_var", "trg_def", "analy_def", "output_print_def", "inputs_def", "outputs_def"]
+
+
+def test_record_layout_matches_header():
+    """Compile a probe against include/mma_tdse.h and compare sizeof/offsetof with the
+    ctypes mirrors (which follow 1DTDSE/sources/structures.h)."""
+    from mma_gb300 import structures as S
+
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "mma_tdse.h"', "int main(void){"]
+    for name in STRUCTS:
+        cls = getattr(S, name)
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (name, name))
+        for f, _ in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (name, f, name, f))
+    lines.append("return 0;}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "probe.c")
+        open(c, "w").write("\n".join(lines))
+        exe = os.path.join(d, "probe")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = dict(l.split() for l in out if l.strip())
+    for name in STRUCTS:
+        cls = getattr(S, name)
+        assert int(got[name]) == ctypes.sizeof(cls), name
+        for f, _ in cls._fields_:
+            assert int(got[name + "." + f]) == getattr(cls, f).offset, (name, f)
+
+
+def test_batched_records_are_8_byte_fields():
+    src = open(os.path.join(ROOT, "include", "mma_tdse.h")).read()
+    for rec in ("mma_tdse_grid", "mma_tdse_instance"):
+        body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (rec, rec), src, re.S).group(1)
+        body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+        for decl in body.split(";"):
+            decl = decl.strip()
+            if decl:
+                assert decl.split()[0] in ("int64_t", "double", "double", "const"), decl
+
+
+def test_legacy_calls_report_errors_without_crashing():
+    """Bad arguments (or, on a machine without a GPU, the missing device) come back as a
+    status, never as exit() or a crash; no kernel runs on these paths."""
+    from mma_gb300.structures import inputs_def, outputs_def
+    from mma_gb300.tdse import MMAError, TDSE_DLL
+
+    dll = TDSE_DLL()
+    inp = inputs_def()
+    inp.init_default_inputs(num_r=1)  # too small: rejected before any device work
+    with pytest.raises(MMAError):
+        dll.init_GS(inp)
+    out = outputs_def()
+    with pytest.raises(MMAError):
+        dll.call1DTDSE(inp, out)  # no field, no ground state
+    t = np.linspace(0, 10, 41)
+    E = np.zeros_like(t)
+    E[3] = np.nan
+    inp2 = inputs_def()
+    inp2.init_default_inputs(num_r=100, dx=0.4)
+    from mma_gb300.tdse import init_time_and_field
+
+    init_time_and_field(dll, inp2, t, E)
+    import ctypes as C
+
+    n = 101
+    xs = (C.c_double * n)(*np.linspace(-20, 20, n))
+    ps = (C.c_double * (2 * n))()
+    inp2.x = C.cast(xs, C.POINTER(C.c_double))
+    inp2.psi0 = C.cast(ps, C.POINTER(C.c_double))
+    with pytest.raises(MMAError, match="non-finite"):
+        dll.call1DTDSE(inp2, out)
+    inp2.gauge = 1
+    E[3] = 0.0
