@@ -227,6 +227,27 @@ size_t mma_tdse_scratch_bytes(int max_m, int grid_ctas, int precision);
 /* Persistent CTAs mma_tdse_propagate launches when grid_ctas is 0. */
 int mma_tdse_default_ctas(int max_m, int precision);
 
+/* No counterpart in the reference.  The same FP64 propagation as mma_tdse_propagate
+ * for callers that cannot allocate device memory (their process's device memory is
+ * owned by another runtime's allocator, or they must not allocate while recording a
+ * graph): the work space comes from a fixed 8 MiB array compiled into this library
+ * (mma_tdse_noalloc_capacity_bytes()), which every GPU that loads the library holds
+ * until the process exits.  The caller still passes inputs and outputs.
+ *   - The first call on each device looks up that device's address of the array;
+ *     make it before any stream capture on that device.
+ *   - Limits: the wavefunction must fit in shared memory and one CTA's sweep buffer
+ *     (max_m * 4096 bytes) must fit in the array; larger grids return
+ *     MMA_ERR_TOO_LARGE without launching.  Fewer CTAs run when the array is the limit.
+ *   - Every call shares the array: calls whose kernels overlap on the GPU (different
+ *     streams without ordering) race on it and give wrong results.  Issue them in order.
+ *   - Allocates nothing: no cudaMalloc/cudaFree and no allocating library call. */
+int mma_tdse_propagate_noalloc(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
+                               const double *fields, double *outputs, double *psi_final, double *snapshots,
+                               int max_m, void *stream);
+
+/* Size in bytes of the fixed work-space array behind mma_tdse_propagate_noalloc. */
+size_t mma_tdse_noalloc_capacity_bytes(void);
+
 /* Fourier interpolation (1DTDSE/sources/tools_fftw3.c:24-68) of n_batch fields of
  * equal length n_raw (rows of `raw`, contiguous) by factor k1 into `interp`
  * (k1*n_raw per row): real DFT, zero padding, inverse DFT, 1/n_raw (cuFFT).

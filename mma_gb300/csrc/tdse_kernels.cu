@@ -584,3 +584,78 @@ extern "C" int mma_tdse_propagate(const mma_tdse_instance* insts, int n_inst, co
     }
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free propagation.
+//
+// For callers that cannot allocate device memory themselves -- a host embedded in a
+// process whose device memory belongs to another runtime's pool (a framework caching
+// allocator with a hard cap, a plugin host that hands out only the buffers it owns),
+// or code that must not allocate while a graph is being recorded -- this entry point
+// runs the same FP64 propagation kernel with its work space (the work-queue counter and
+// the per-CTA sweep buffer) taken from a fixed array compiled into this library instead
+// of a caller-provided scratch buffer.  The caller still passes inputs and outputs.
+// ------------------------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr size_t kNoAllocBytes = (size_t)8 << 20;  // 8 MiB on every device that loads the library
+constexpr size_t kNoAllocHeader = 256;            // work-queue counter lives in the first 256 bytes
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {};
+
+// Device address of g_noalloc_scratch on the current device.  The symbol's host-side name
+// is only a stand-in, so the address is looked up once per device, with that device current.
+int noalloc_address(void** out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MMA_ERR_NO_DEVICE;
+    if (dev < 0 || dev >= 64) return MMA_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return MMA_ERR_CUDA;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return MMA_OK;
+}
+
+}  // namespace
+
+extern "C" size_t mma_tdse_noalloc_capacity_bytes(void) { return kNoAllocBytes; }
+
+extern "C" int mma_tdse_propagate_noalloc(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
+                                          const double* fields, double* outputs, double* psi_final,
+                                          double* snapshots, int max_m, void* stream)
+{
+    if (n_inst <= 0) return MMA_OK;
+    if (!insts || !grids || !fields || !outputs || max_m < 1) return MMA_ERR_ARG;
+    // one CTA needs max_m * 256 * 16 bytes of sweep buffer, and the wavefunction must fit
+    // in shared memory (the fixed array does not also hold it)
+    const size_t per_cta = (size_t)max_m * kThreads * 16;
+    if (!psi_fits_smem(max_m) || per_cta > kNoAllocBytes - kNoAllocHeader) return MMA_ERR_TOO_LARGE;
+    if (sm_count() <= 0) return MMA_ERR_NO_DEVICE;
+    void* base = nullptr;
+    int rc = noalloc_address(&base);
+    if (rc != MMA_OK) return rc;
+    int ctas = mma_tdse_default_ctas(max_m, 0);
+    const int cap = (int)((kNoAllocBytes - kNoAllocHeader) / per_cta);
+    if (ctas > cap) ctas = cap;
+    if (ctas > n_inst) ctas = n_inst;
+    if (ctas < 1) return MMA_ERR_TOO_LARGE;
+    cudaStream_t st = (cudaStream_t)stream;
+    int* counter = reinterpret_cast<int*>(base);
+    // the array keeps the previous call's contents: the work-queue head must restart at 0
+    if (cudaMemsetAsync(counter, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+    PropArgs A{insts, n_inst, grids, fields, outputs, psi_final, snapshots, counter,
+               reinterpret_cast<double*>(static_cast<unsigned char*>(base) + kNoAllocHeader),
+               (int64_t)max_m * kThreads};
+    const size_t smem = per_cta;
+    cudaFuncSetAttribute(propagate_fp64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    propagate_fp64_kernel<true><<<ctas, kThreads, smem, st>>>(A);
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
