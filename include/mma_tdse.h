@@ -173,12 +173,17 @@ const char *mma_last_error_message(void);
  *   cn_tab   [14 L]        Crank-Nicolson solve tables (complex)  (written by build)
  *   gs_tab   [5 L]         ground-state solve tables (real)       (written by build)
  *   result   [4]           {Einit, iterations, status, |dE| at stop}
+ *   c64_tab  [5 * 256 * m32] floats, tables of the complex64 form (precision 1), laid
+ *            out for m32 = ceil(m/8)*8 <= 32 sites per thread; NULL when unused
+ *            (written by mma_tdse_build_c64_tables)
  * The record has 8-byte fields only, so its layout is the same in every ABI. */
 typedef struct mma_tdse_grid {
     int64_t n, m;
     double dx, trg_a, dt, x_int, Eguess, CV;
     int64_t max_iter;
     double *x, *gv, *psi0, *cn_tab, *gs_tab, *result;
+    int64_t m32;
+    float *c64_tab;
 } mma_tdse_grid;
 
 /* One TDSE instance of a batch (offsets are in doubles). */
@@ -213,11 +218,21 @@ typedef struct mma_tdse_buffers {
 int mma_tdse_build_grids(const mma_tdse_grid *grids_dev, const mma_tdse_grid *grids_host, int n_grids, int mode,
                          void *stream);
 
+/* Build the complex64-form tables of n_grids grids from their FP64 data (after
+ * mma_tdse_build_grids): 1/beta of the FP64 factorisation, the off-diagonal factor
+ * w_j = dt/2 (-1/(2dx^2) + V_j/12), -V' and the (real) ground state, rounded once to
+ * FP32 and laid out for m32 sites per thread.  Needs m32 <= 32 (n <= 8192). */
+int mma_tdse_build_c64_tables(const mma_tdse_grid *grids_dev, const mma_tdse_grid *grids_host, int n_grids,
+                              void *stream);
+
 /* Propagate n_inst instances in one persistent launch (one CTA per instance at a
  * time, instances pulled from a device work queue).
  *   max_m      largest grid m in the batch (sizes shared memory and scratch)
  *   grid_ctas  persistent CTAs to launch (0 = as many as are resident at once)
- *   precision  0 = FP64, the reference's arithmetic */
+ *   precision  0 = FP64, the reference's arithmetic;
+ *              1 = complex64 propagation (FP32 wavefunction and sweeps) with the
+ *                  factorisation computed in FP64 and the observables summed with
+ *                  compensation and finished in FP64; needs c64 tables (n <= 8192) */
 int mma_tdse_propagate(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
                        const mma_tdse_buffers *bufs, int max_m, int grid_ctas, int precision, void *stream);
 

@@ -1,0 +1,491 @@
+// tdse_c64.cu -- complex64 form of the TDSE propagation (the precision-chosen form).
+//
+// Same Crank-Nicolson-Numerov step and the same partitioned solve as the FP64 kernel
+// (tdse_kernels.cu, tdse_solver.cuh), with:
+//   * the factorisation computed in FP64 (build_grids_kernel) and rounded once to FP32;
+//   * the wavefunction, the sweeps and the chunk products in FP32 registers: each of the
+//     256 threads keeps its M <= 32 sites of psi, of the local sweep and of the running
+//     chunk products (F forward, then G backward) in registers for the whole pulse;
+//   * the per-site tables in shared memory, 20 bytes per site: 1/beta (complex), the
+//     off-diagonal factor w_j = dt/2 (-1/(2dx^2) + V_j/12) from which h_j = 6 a_j /beta_j and
+//     g_j = 6 c_j /beta_j are re-derived (a_j = 1/12 + i w_{j-1}, c_j = 1/12 + i w_{j+1}), -V'
+//     and the (real) ground state -- nothing per step goes to L2 but the four observables;
+//   * the phase e^{+i E dt x}: the chunk-start angle is formed and reduced mod 2 pi in
+//     float-float arithmetic, then e^{i E dt dx i} per site from a 32-entry table;
+//   * the observables summed per thread with Kahan compensation, across the warp with
+//     two-sum pairs, and across warps in FP64 by thread 0.
+// Reference: 1DTDSE/sources/prop.c:115-347 (step and observables), tridiag.c:26-70 (solve).
+#include <cuda_runtime.h>
+
+#include "../../include/mma_tdse.h"
+#include "common.cuh"
+
+namespace mma {
+namespace c64 {
+
+struct cf {
+    float re, im;
+};
+__device__ __forceinline__ cf operator+(cf a, cf b) { return cf{a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ cf operator-(cf a, cf b) { return cf{a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ cf cmul(cf a, cf b) { return cf{fmaf(a.re, b.re, -a.im * b.im), fmaf(a.re, b.im, a.im * b.re)}; }
+// a + b*c
+__device__ __forceinline__ cf cfma(cf b, cf c, cf a)
+{
+    return cf{fmaf(b.re, c.re, fmaf(-b.im, c.im, a.re)), fmaf(b.re, c.im, fmaf(b.im, c.re, a.im))};
+}
+// a - b*c
+__device__ __forceinline__ cf cfms(cf b, cf c, cf a)
+{
+    return cf{fmaf(-b.re, c.re, fmaf(b.im, c.im, a.re)), fmaf(-b.re, c.im, fmaf(-b.im, c.re, a.im))};
+}
+__device__ __forceinline__ cf shup(cf v, int d)
+{
+    return cf{__shfl_up_sync(0xffffffffu, v.re, d), __shfl_up_sync(0xffffffffu, v.im, d)};
+}
+__device__ __forceinline__ cf shdn(cf v, int d)
+{
+    return cf{__shfl_down_sync(0xffffffffu, v.re, d), __shfl_down_sync(0xffffffffu, v.im, d)};
+}
+
+// Table slots (floats), each L = 256*M long, site j = t*M + i at q = i*256 + t.
+enum { T_IBRE = 0, T_IBIM, T_W, T_GV, T_PSI0, T_SLOTS };
+
+// forward scan of Y_t = b_t + c_t Y_{t-1} over the CTA, exclusive (see tdse_solver.cuh)
+__device__ __forceinline__ cf scan_fwd(cf c, cf b, cf* sc, cf* sb)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        cf cp = shup(c, d), bp = shup(b, d);
+        if (lane >= d) {
+            b = cfma(c, bp, b);
+            c = cmul(c, cp);
+        }
+    }
+    if (lane == 31) {
+        sc[w] = c;
+        sb[w] = b;
+    }
+    __syncthreads();
+    cf yw{0.f, 0.f};
+    for (int q = 0; q < kWarps; q++)
+        if (q < w) yw = cfma(sc[q], yw, sb[q]);
+    cf cp = shup(c, 1), bp = shup(b, 1);
+    return lane == 0 ? yw : cfma(cp, yw, bp);
+}
+
+__device__ __forceinline__ cf scan_bwd(cf c, cf b, cf* sc, cf* sb)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        cf cp = shdn(c, d), bp = shdn(b, d);
+        if (lane + d < 32) {
+            b = cfma(c, bp, b);
+            c = cmul(c, cp);
+        }
+    }
+    if (lane == 0) {
+        sc[w] = c;
+        sb[w] = b;
+    }
+    __syncthreads();
+    cf uw{0.f, 0.f};
+    for (int q = kWarps - 1; q >= 0; q--)
+        if (q > w) uw = cfma(sc[q], uw, sb[q]);
+    cf cp = shdn(c, 1), bp = shdn(b, 1);
+    return lane == 31 ? uw : cfma(cp, uw, bp);
+}
+
+// error-free sum (Knuth two-sum)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+struct Args {
+    const mma_tdse_instance* insts;
+    int n_inst;
+    const mma_tdse_grid* grids;
+    const double* fields;
+    double* outputs;
+    double* psi_final;
+    double* snapshots;
+    int* counter;
+};
+
+// First index where the zero gate opens (prop.c:125-134), as in the FP64 kernel.
+__device__ int64_t gate_index32(const double* f, int64_t n_field, int64_t n_steps, double floor_)
+{
+    for (int64_t k = 0; k < n_steps; k++) {
+        double a = (k < n_field) ? f[k] : 0.0, b = (k + 1 < n_field) ? f[k + 1] : 0.0;
+        if (fabs(a) <= floor_) a = 0.0;
+        if (fabs(b) <= floor_) b = 0.0;
+        if (a * b <= 0.0) return k;
+    }
+    return n_steps;
+}
+
+constexpr double kInvTwoPi = 0.15915494309189533576888376337251;
+
+template <int M>
+__global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
+{
+    extern __shared__ float tab[];  // T_SLOTS * 256 * M floats
+    __shared__ cf sc[2 * kWarps], sb[2 * kWarps];
+    __shared__ float red_hi[kWarps * 4], red_lo[kWarps * 4];
+    __shared__ cf bfirst[kWarps], blast[kWarps];
+    __shared__ cf wtab[M];
+    __shared__ float s_ahi, s_alo;  // F_k dt as a float-float pair (phase angle of pass 3)
+    __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    constexpr int L = kThreads * M;
+    if (t == 0) s_grid = -1;
+
+    for (;;) {
+        if (t == 0) s_inst = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int64_t inst = s_inst;
+        if (inst >= P.n_inst) break;
+        const mma_tdse_instance I = P.insts[inst];
+        const mma_tdse_grid G = P.grids[I.grid];
+        const int64_t n = G.n, S = I.n_steps;
+        // ---- tables into shared memory when the grid changes
+        if (s_grid != I.grid) {
+            for (int q = t; q < T_SLOTS * L; q += kThreads) tab[q] = G.c64_tab[q];
+        }
+        __syncthreads();
+        if (t == 0) {
+            s_grid = I.grid;
+            s_gate = gate_index32(P.fields + I.field_off, I.n_field, S, I.gate_floor);
+            const int64_t num_r = n - 1;
+            int64_t lo = -1, hi;
+            if (!(-G.x_int < G.x[0])) {
+                int64_t i = 0;
+                while (i < num_r && !(-G.x_int <= G.x[i + 1])) i++;
+                lo = i;
+            }
+            if (G.x_int < G.x[0]) {
+                hi = 0;
+            } else {
+                int64_t i = 0;
+                while (i < num_r && !(G.x_int <= G.x[i + 1])) i++;
+                hi = (i < num_r) ? i + 1 : num_r + 1;
+            }
+            s_lo = lo < 0 ? 0 : lo;
+            s_hi = hi > num_r ? num_r : hi;
+        }
+        const float* ibre = tab + T_IBRE * L;
+        const float* ibim = tab + T_IBIM * L;
+        const float* ww = tab + T_W * L;
+        const float* gv = tab + T_GV * L;
+        const float* p0 = tab + T_PSI0 * L;
+        // ---- state: psi in registers, initialised from the ground state
+        cf psi[M], yl[M], fg[M];
+        const int64_t s0 = (int64_t)t * M;
+#pragma unroll
+        for (int i = 0; i < M; i++) psi[i] = cf{p0[i * kThreads + t], 0.f};
+        // chunk start x as a float-float pair (phase angle) and as a float (<x>)
+        const double xs_d = (s0 < n) ? G.x[s0] : 0.0;
+        const float xs_hi = (float)xs_d, xs_lo = (float)(xs_d - (double)xs_hi);
+        const float dxf = (float)G.dx;
+        const double dt = G.dt;
+        const float w6 = 6.0f;
+        if (lane == 0) bfirst[w] = psi[0];
+        if (lane == 31) blast[w] = psi[M - 1];
+        __syncthreads();
+        const int64_t lo = s_lo, hi = s_hi, gate = s_gate;
+        const double* f = P.fields + I.field_off;
+        double* out = P.outputs + I.out_off;
+        double *o_t = out, *o_e = out + (S + 1), *o_src = out + 2 * (S + 1), *o_ptot = out + 3 * (S + 1),
+               *o_pint = out + 4 * (S + 1), *o_x = out + 5 * (S + 1);
+        {   // initial window population (prop.c:87-93), FP64 from the FP64 ground state
+            double v[1] = {0.0};
+            for (int64_t j = t; j < n; j += kThreads)
+                if (j >= lo && j <= hi) v[0] += G.psi0[2 * j] * G.psi0[2 * j] + G.psi0[2 * j + 1] * G.psi0[2 * j + 1];
+            block_sum<1>(v, reinterpret_cast<double*>(red_hi));
+            if (t == 0) {
+                o_t[0] = I.tmin;
+                o_e[0] = 0.0;
+                o_src[0] = 0.0;
+                o_ptot[0] = 1.0;
+                o_pint[0] = v[0];
+                o_x[0] = 0.0;
+            }
+        }
+        double tt = I.tmin;
+
+        for (int64_t k = 0; k < S; k++) {
+            // FP64 work of a step is spread over three warps so that no single warp holds the
+            // (1/64-rate) FP64 pipe for long: warp 0 finishes the previous step's observables,
+            // warp 1 lane 0 advances the time grid and the field, the last warp's lanes build
+            // the step's phase constants.
+            if (w == 0 && k > 0) {
+                // lanes 8c+q hold warp q's two-sum pair of observable c; reduce over q
+                const int c = lane >> 3, q = lane & 7;
+                float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
+#pragma unroll
+                for (int d = 4; d >= 1; d >>= 1) {
+                    const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
+                    const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
+                    float s2, e2;
+                    two_sum(hs, oh, s2, e2);
+                    hs = s2;
+                    ls += ol + e2;
+                }
+                const double v = (double)hs + (double)ls;  // FP64 finish
+                const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
+                if (lane == 0) o_src[k] = -v + o_e[k];
+                if (lane == 8) o_x[k] = v;
+                if (lane == 16) o_ptot[k] = fma(pr, pr, pim * pim);
+            }
+            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : f[k];
+            if (w == 1 && lane == 0) {
+                tt += dt;
+                o_t[k + 1] = tt;
+                o_e[k + 1] = Fk;
+            }
+            if (w == kWarps - 1) {
+                if (lane < M) {  // per-site phase factors e^{i F dt dx i}, i < M
+                    float sn, cs;
+                    sincosf((float)(Fk * dt * G.dx) * (float)lane, &sn, &cs);
+                    wtab[lane] = cf{cs, sn};
+                }
+                if (lane == 31) {
+                    const double fdt = Fk * dt;
+                    const float a_hi = (float)fdt;
+                    s_ahi = a_hi;
+                    s_alo = (float)(fdt - (double)a_hi);
+                }
+            }
+            // ---- pass 1: right-hand side 2 M2 psi, local forward sweep, forward products F
+            cf left = shup(psi[M - 1], 1), right = shdn(psi[0], 1);
+            if (lane == 0) left = (w == 0) ? cf{0.f, 0.f} : blast[w - 1];
+            if (lane == 31) right = (w == kWarps - 1) ? cf{0.f, 0.f} : bfirst[w + 1];
+            cf yprev{0.f, 0.f}, Fp{1.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < M; i++) {
+                const int q = i * kThreads + t;
+                const cf pm = (i == 0) ? left : psi[i - 1];
+                const cf pn = (i == M - 1) ? right : psi[i + 1];
+                const cf r{fmaf(10.f, psi[i].re, pm.re + pn.re), fmaf(10.f, psi[i].im, pm.im + pn.im)};
+                const cf ib{ibre[q], ibim[q]};
+                // a_j = 1/12 + i w_{j-1}; h_j = a_j / beta_j = (6 a_j) (ib/6)
+                const float wl = (i == 0) ? ((t == 0) ? 0.f : ww[(M - 1) * kThreads + t - 1]) : ww[q - kThreads];
+                cf h = cmul(cf{0.5f, w6 * wl}, ib);
+                if (s0 + i == 0) h = cf{0.f, 0.f};
+                const cf y = cfms(h, yprev, cmul(ib, r));
+                yl[i] = y;
+                yprev = y;
+                Fp = cmul(Fp, cf{-h.re, -h.im});
+                fg[i] = Fp;
+            }
+            const cf yin = scan_fwd(fg[M - 1], yprev, sc, sb);
+            // ---- pass 2: forward correction, local backward sweep, backward products G
+            cf unext{0.f, 0.f}, Gp{1.f, 0.f};
+#pragma unroll
+            for (int i = M - 1; i >= 0; i--) {
+                const int q = i * kThreads + t;
+                const cf y = cfma(fg[i], yin, yl[i]);
+                const cf ib{ibre[q], ibim[q]};
+                const float wr = (i == M - 1) ? ((t == kThreads - 1) ? 0.f : ww[t + 1]) : ww[q + kThreads];
+                cf g = cmul(cf{0.5f, w6 * wr}, ib);
+                if (s0 + i >= n - 1) g = cf{0.f, 0.f};
+                const cf u = cfms(g, unext, y);
+                yl[i] = u;
+                unext = u;
+                Gp = cmul(Gp, cf{-g.re, -g.im});
+                fg[i] = Gp;
+            }
+            const cf uin = scan_bwd(fg[0], unext, sc + kWarps, sb + kWarps);
+            // ---- pass 3: backward correction, CN update, phase, observables
+            // chunk-start angle F dt x_s in float-float, reduced mod 2 pi
+            const float a_hi = s_ahi, a_lo = s_alo;
+            float th_hi = a_hi * xs_hi;
+            float th_lo = fmaf(a_hi, xs_hi, -th_hi) + fmaf(a_hi, xs_lo, a_lo * xs_hi);
+            const float kk = rintf(th_hi * (float)kInvTwoPi);
+            // 2 pi = C1 + C2 + C3 (C1, C2 exact in float)
+            const float C1 = 6.28125f, C2 = 1.93500518798828125e-3f, C3 = 3.0199159819370158e-07f;
+            float red = fmaf(-kk, C1, th_hi);
+            red = fmaf(-kk, C2, red);
+            red = fmaf(-kk, C3, red) + th_lo;
+            float sn, cs;
+            sincosf(red, &sn, &cs);
+            const cf phs{cs, sn};
+            float acc_hi[4] = {0.f, 0.f, 0.f, 0.f}, acc_c[4] = {0.f, 0.f, 0.f, 0.f};
+            float pint = 0.f;
+#pragma unroll
+            for (int i = 0; i < M; i++) {
+                const int q = i * kThreads + t;
+                const int64_t j = s0 + i;
+                const cf u = cfma(fg[i], uin, yl[i]);
+                const cf d = u - psi[i];
+                const cf ph = cmul(phs, wtab[i]);
+                const cf pn = cmul(ph, d);
+                psi[i] = pn;
+                const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
+                const float xj = xs_hi + dxf * (float)i;
+                const float terms[4] = {n2 * gv[q], n2 * xj, pn.re * p0[q], -pn.im * p0[q]};
+#pragma unroll
+                for (int c = 0; c < 4; c++) {  // Kahan
+                    const float y = terms[c] - acc_c[c];
+                    const float s = acc_hi[c] + y;
+                    acc_c[c] = (s - acc_hi[c]) - y;
+                    acc_hi[c] = s;
+                }
+                if (j >= lo && j <= hi) pint += n2;
+            }
+            if (lane == 0) bfirst[w] = psi[0];
+            if (lane == 31) blast[w] = psi[M - 1];
+            // warp reduction in two-sum pairs
+            float hs[4], ls[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                hs[c] = acc_hi[c];
+                ls[c] = -acc_c[c];
+            }
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1)
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float oh = __shfl_xor_sync(0xffffffffu, hs[c], d);
+                    const float ol = __shfl_xor_sync(0xffffffffu, ls[c], d);
+                    float s, e;
+                    two_sum(hs[c], oh, s, e);
+                    hs[c] = s;
+                    ls[c] += ol + e;
+                }
+            // the window population covers a handful of sites: plain float, FP64 across warps
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) pint += __shfl_xor_sync(0xffffffffu, pint, d);
+            if (lane == 0) {
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    red_hi[w * 4 + c] = hs[c];
+                    red_lo[w * 4 + c] = ls[c];
+                }
+                sc[2 * kWarps - 1 - w].re = pint;  // parked in an idle scan slot until step end
+            }
+            if (I.snap_off >= 0 && P.snapshots) {  // prop.c:248-263
+                int64_t slot = -1;
+                if (k % I.snap_every == 0 && k / I.snap_every < I.n_snap - 1) slot = k / I.snap_every;
+                if (k == S - 1) slot = I.n_snap - 1;
+                if (slot >= 0) {
+                    double* sp = P.snapshots + I.snap_off + slot * 2 * n;
+#pragma unroll
+                    for (int i = 0; i < M; i++)
+                        if (s0 + i < n) {
+                            sp[2 * (s0 + i)] = psi[i].re;
+                            sp[2 * (s0 + i) + 1] = psi[i].im;
+                        }
+                }
+            }
+            __syncthreads();
+            if (w == 2 && lane == 0) {
+                float pi_sum = 0.f;
+                for (int q = 0; q < kWarps; q++) pi_sum += sc[2 * kWarps - 1 - q].re;
+                o_pint[k + 1] = (double)pi_sum;
+            }
+        }
+        if (w == 0) {  // observables of the last step, as at the top of the step loop
+            const int c = lane >> 3, q = lane & 7;
+            float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
+#pragma unroll
+            for (int d = 4; d >= 1; d >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
+                const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
+                float s2, e2;
+                two_sum(hs, oh, s2, e2);
+                hs = s2;
+                ls += ol + e2;
+            }
+            const double v = (double)hs + (double)ls;
+            const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
+            if (lane == 0) o_src[S] = -v + o_e[S];
+            if (lane == 8) o_x[S] = v;
+            if (lane == 16) o_ptot[S] = fma(pr, pr, pim * pim);
+        }
+        if (P.psi_final && I.psi_off >= 0) {
+            double* pf = P.psi_final + I.psi_off;
+#pragma unroll
+            for (int i = 0; i < M; i++)
+                if (s0 + i < n) {
+                    pf[2 * (s0 + i)] = psi[i].re;
+                    pf[2 * (s0 + i) + 1] = psi[i].im;
+                }
+        }
+        __syncthreads();
+    }
+}
+
+// Complex64 tables from the FP64 grid data, laid out for M32 sites per thread.
+__global__ void __launch_bounds__(kThreads) build_c64_kernel(const mma_tdse_grid* grids)
+{
+    const mma_tdse_grid G = grids[blockIdx.x];
+    const int64_t n = G.n, m = G.m, Lm = m * kThreads, M = G.m32, L = M * kThreads;
+    const cd* ctab = reinterpret_cast<const cd*>(G.cn_tab);
+    const double hdt = 0.5 * G.dt;
+    for (int64_t q = threadIdx.x; q < L; q += kThreads) {
+        const int64_t i = q / kThreads, t = q % kThreads, j = t * M + i;
+        float v[T_SLOTS] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        if (j < n) {
+            const int64_t q64 = (j % m) * kThreads + j / m;  // FP64 table layout
+            const cd ib6 = ctab[0 * Lm + q64];
+            const double vj = -1.0 / sqrt(G.trg_a * G.trg_a + G.x[j] * G.x[j]);
+            v[T_IBRE] = (float)ib6.re;
+            v[T_IBIM] = (float)ib6.im;
+            v[T_W] = (float)(hdt * (-0.5 / (G.dx * G.dx)) + hdt * 1 / 12. * vj);
+            v[T_GV] = (float)G.gv[j];
+            v[T_PSI0] = (float)G.psi0[2 * j];
+        }
+#pragma unroll
+        for (int s = 0; s < T_SLOTS; s++) G.c64_tab[s * L + q] = v[s];
+    }
+}
+
+}  // namespace c64
+}  // namespace mma
+
+using namespace mma;
+
+extern "C" int mma_tdse_build_c64_tables(const mma_tdse_grid* grids_dev, const mma_tdse_grid* grids_host, int n_grids,
+                                         void* stream)
+{
+    if (n_grids <= 0 || !grids_dev || !grids_host) return MMA_ERR_ARG;
+    for (int g = 0; g < n_grids; g++) {
+        const mma_tdse_grid& G = grids_host[g];
+        if (!G.c64_tab || G.m32 < G.m || G.m32 > 32 || G.m32 % 8 != 0 || G.m32 * kThreads < G.n) return MMA_ERR_ARG;
+    }
+    c64::build_c64_kernel<<<n_grids, kThreads, 0, (cudaStream_t)stream>>>(grids_dev);
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
+
+namespace {
+template <int M>
+int launch_c64(const c64::Args& A, int ctas, cudaStream_t st)
+{
+    const size_t smem = (size_t)c64::T_SLOTS * kThreads * M * sizeof(float);
+    cudaFuncSetAttribute(c64::propagate_c64_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    c64::propagate_c64_kernel<M><<<ctas, kThreads, smem, st>>>(A);
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
+}  // namespace
+
+// Launch of the complex64 form (called by mma_tdse_propagate for precision 1).
+extern "C" int mma_tdse_propagate_c64_impl(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
+                                           const mma_tdse_buffers* bufs, int m32, int grid_ctas, void* stream)
+{
+    c64::Args A{insts, n_inst, grids, bufs->fields, bufs->outputs, bufs->psi_final, bufs->snapshots, bufs->counter};
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(bufs->counter, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+    switch (m32) {
+        case 8: return launch_c64<8>(A, grid_ctas, st);
+        case 16: return launch_c64<16>(A, grid_ctas, st);
+        case 24: return launch_c64<24>(A, grid_ctas, st);
+        case 32: return launch_c64<32>(A, grid_ctas, st);
+        default: return MMA_ERR_TOO_LARGE;
+    }
+}

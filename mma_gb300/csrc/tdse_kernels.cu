@@ -535,11 +535,14 @@ static int sm_count()
     return sms;
 }
 
+extern "C" int mma_tdse_propagate_c64_impl(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
+                                           const mma_tdse_buffers* bufs, int m32, int grid_ctas, void* stream);
+
 extern "C" int mma_tdse_default_ctas(int max_m, int precision)
 {
-    (void)precision;
     const int sms = sm_count();
     if (sms <= 0 || max_m < 1) return 0;
+    if (precision == 1) return sms;  // complex64 form: one register-resident instance per SM
     int per_sm = 1;
     if (psi_fits_smem(max_m)) {
         size_t smem = (size_t)max_m * kThreads * 16;
@@ -553,6 +556,7 @@ extern "C" int mma_tdse_default_ctas(int max_m, int precision)
 
 extern "C" size_t mma_tdse_scratch_bytes(int max_m, int grid_ctas, int precision)
 {
+    if (precision == 1) return 8;  // complex64 form keeps its sweep in registers
     if (grid_ctas <= 0) grid_ctas = mma_tdse_default_ctas(max_m, precision);
     if (grid_ctas <= 0) grid_ctas = 1;
     size_t per = (size_t)max_m * kThreads * 16;
@@ -566,10 +570,14 @@ extern "C" int mma_tdse_propagate(const mma_tdse_instance* insts, int n_inst, co
     if (!insts || !grids || !bufs || !bufs->fields || !bufs->outputs || !bufs->counter || !bufs->scratch ||
         max_m < 1)
         return MMA_ERR_ARG;
-    if (precision != 0) return MMA_ERR_UNSUPPORTED;
+    if (precision != 0 && precision != 1) return MMA_ERR_UNSUPPORTED;
     if (sm_count() <= 0) return MMA_ERR_NO_DEVICE;
     if (grid_ctas <= 0) grid_ctas = mma_tdse_default_ctas(max_m, precision);
     if (grid_ctas > n_inst) grid_ctas = n_inst;
+    if (precision == 1) {
+        // max_m is the common m32 of the batch's complex64 tables (8, 16, 24 or 32)
+        return mma_tdse_propagate_c64_impl(insts, n_inst, grids, bufs, max_m, grid_ctas, stream);
+    }
     if (bufs->scratch_bytes < mma_tdse_scratch_bytes(max_m, grid_ctas, precision)) return MMA_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(bufs->counter, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;

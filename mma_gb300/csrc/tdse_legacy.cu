@@ -99,6 +99,8 @@ int alloc_grid(DevGrid& g, int num_r, double dx, double a, double dt, double x_i
     g.h.gs_tab = p;
     p += 5 * L;
     g.h.result = p;
+    g.h.m32 = 0;
+    g.h.c64_tab = nullptr;
     if (cudaMemcpy(g.d, &g.h, sizeof(mma_tdse_grid), cudaMemcpyHostToDevice) != cudaSuccess) return MMA_ERR_CUDA;
     return MMA_OK;
 }

@@ -28,14 +28,15 @@ THREADS = 256
 CN_SLOTS = 14  # doubles per padded site in the CN tables
 GS_SLOTS = 5
 
-PRECISIONS = {"fp64": 0}
+PRECISIONS = {"fp64": 0, "c64": 1}
+C64_SLOTS = 5  # floats per padded site in the complex64 tables
 
 
 class GridRec(Structure):
     _fields_ = [("n", c_int64), ("m", c_int64), ("dx", c_double), ("trg_a", c_double), ("dt", c_double),
                 ("x_int", c_double), ("Eguess", c_double), ("CV", c_double), ("max_iter", c_int64),
                 ("x", c_void_p), ("gv", c_void_p), ("psi0", c_void_p), ("cn_tab", c_void_p), ("gs_tab", c_void_p),
-                ("result", c_void_p)]
+                ("result", c_void_p), ("m32", c_int64), ("c64_tab", c_void_p)]
 
 
 class InstRec(Structure):
@@ -114,7 +115,7 @@ class TDSEGrids:
     (already refined).  The ground states are computed on construction.
     """
 
-    def __init__(self, params, dt, device="cuda", stream=None):
+    def __init__(self, params, dt, device="cuda", stream=None, c64=False):
         lib = _sig()
         self.device = torch.device(device)
         self.dt = float(dt)
@@ -152,6 +153,17 @@ class TDSEGrids:
         self.n = np.array([s[0] for s in sizes])
         self.m = np.array([s[1] for s in sizes])
         self.max_m = int(self.m.max())
+        self.m32 = np.array([((m + 7) // 8) * 8 for m in self.m])
+        self.c64 = bool(c64)
+        if self.c64:
+            if self.m32.max() > 32:
+                raise ValueError("the complex64 form takes grids of at most 8192 sites")
+            c_sizes = C64_SLOTS * THREADS * self.m32
+            self.c64_buf = torch.zeros(int(c_sizes.sum()), dtype=torch.float32, device=self.device)
+            c_off = np.concatenate([[0], np.cumsum(c_sizes)])[:-1]
+            for r, m32, o in zip(recs, self.m32, c_off):
+                r.m32 = int(m32)
+                r.c64_tab = self.c64_buf.data_ptr() + 4 * int(o)
         arr = (GridRec * len(recs))(*recs)
         self.host_recs = arr
         self.dev_recs = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
@@ -159,6 +171,12 @@ class TDSEGrids:
         _check(lib.mma_tdse_build_grids(ctypes.c_void_p(self.dev_recs.data_ptr()), ctypes.addressof(arr), len(recs),
                                         0, st), "mma_tdse_build_grids")
         torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
+        if self.c64:
+            lib.mma_tdse_build_c64_tables.argtypes = [c_void_p, c_void_p, c_int, c_void_p]
+            lib.mma_tdse_build_c64_tables.restype = c_int
+            _check(lib.mma_tdse_build_c64_tables(ctypes.c_void_p(self.dev_recs.data_ptr()), ctypes.addressof(arr),
+                                                 len(recs), st), "mma_tdse_build_c64_tables")
+            torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
         res = np.stack([self._view(g, "result").cpu().numpy() for g in range(len(recs))])
         self.Einit = res[:, 0].copy()
         self.iterations = res[:, 1].astype(int)
@@ -265,6 +283,13 @@ def run_batch(grids, fields, dt_field, grid_ids=None, dt_req=None, tmin=0.0, spe
     d_insts = torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(dev)
     max_m = int(grids.m[np.unique(gid)].max())
     prec = PRECISIONS[precision]
+    if prec == 1:
+        if not grids.c64:
+            raise ValueError("build the grids with c64=True for the complex64 form")
+        m32s = np.unique(grids.m32[np.unique(gid)])
+        if len(m32s) != 1:
+            raise ValueError("one complex64 launch needs grids of one m32; split the batch by grids.m32")
+        max_m = int(m32s[0])
     ctas = grid_ctas or lib.mma_tdse_default_ctas(max_m, prec)
     ctas = min(ctas, n_inst)
     sbytes = lib.mma_tdse_scratch_bytes(max_m, ctas, prec)

@@ -31,3 +31,11 @@ def rel_l2(a, b):
     b = np.asarray(b)
     nb = np.linalg.norm(b)
     return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def plateau_error(F_test, F_ref, omega, omega0=OMEGA0, q_lo=11, q_hi=41):
+    """Relative L2 error of |F|^2 over the harmonic window [q_lo, q_hi] omega0."""
+    sel = (omega >= q_lo * omega0) & (omega <= q_hi * omega0)
+    a = np.abs(np.asarray(F_test)[sel]) ** 2
+    b = np.abs(np.asarray(F_ref)[sel]) ** 2
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))

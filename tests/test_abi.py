@@ -97,8 +97,8 @@ def test_batched_records_are_8_byte_fields():
         body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
         for decl in body.split(";"):
             decl = decl.strip()
-            if decl:
-                assert decl.split()[0] in ("int64_t", "double", "double", "const"), decl
+            if decl:  # pointers, int64_t and double only: 8-byte fields, no padding
+                assert "*" in decl or decl.split()[0] in ("int64_t", "double"), decl
 
 
 def test_legacy_calls_report_errors_without_crashing():
