@@ -1,0 +1,77 @@
+/*
+ * mma_hankel.h -- C-ABI of the GB300 far-field (Hankel) kernels in libmma_gb300.so.
+ *
+ * Replaces the computational core of Hankel/Hankel_transform.py:
+ *   HankelTransform (:452-519)  per-plane transform
+ *       P_k[w, rho] = trapz_r( pre_k(w) e^{-i k r^2/(2 D_k)} r S_k[w, r] J0(k r rho / D_k) ),
+ *       k = w/c, D_k = distance - z_k (the near-field factor optional)
+ *   Hankel_long (:523-686)      z-trapezoid of the planes, entry/exit planes
+ * Grids are SI; all pointers are device pointers; complex arrays are interleaved
+ * (re, im).  Outputs use the reference's layout after its transposes: [rho][omega].
+ */
+#ifndef MMA_HANKEL_H
+#define MMA_HANKEL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* 8-byte fields only (same layout in every ABI). */
+typedef struct mma_hankel_problem {
+    int64_t n_omega, n_r, n_z, n_rho; /* n_z = planes used (the reference drops the last plane, :62) */
+    double distance;                  /* screen distance from the first medium point (Hankel_long `distance`) */
+    int64_t near_field;               /* 1 = apply e^{-i k r^2/(2 D_k)} (the reference default) */
+    int64_t source_c128;              /* 0 = complex64 source, 1 = complex128 */
+    int64_t plane_stride;             /* source elements between planes k */
+    int64_t omega_stride;             /* source elements between frequencies; r is contiguous */
+} mma_hankel_problem;
+
+/* Inputs common to both forms:
+ *   ogrid [n_omega], rgrid [n_r], zgrid [n_z], rho [n_rho]    float64 grids
+ *   source                                                    S[k][w][r] with the strides above
+ *   pre     [n_z][n_omega] complex128 pre-factor, or NULL for 1 (get_propagation_pre_factor_function)
+ * Outputs:
+ *   ff      [n_rho][n_omega] complex128                        FF_integrated
+ *   plane_slot [n_z] int64 (or NULL): slot of plane k in `planes`, -1 = not stored;
+ *           n_planes = number of slots in use (0..n_planes-1, each used once)
+ *   planes  [n_planes][n_rho][n_omega] complex128 (or NULL)    per-plane transforms */
+
+/* Plain form: the reference's arithmetic in FP64, one J0 (CUDA j0) per (w, k, rho, r)
+ * term.  One CTA per frequency. */
+int mma_hankel_plain(const mma_hankel_problem *p, const double *ogrid, const double *rgrid, const double *zgrid,
+                     const double *rho, const void *source, const double *pre, double *ff,
+                     const int64_t *plane_slot, int n_planes, double *planes, void *stream);
+
+/* Parameters of the fast form, chosen on the host from the grids by mma_hankel_fast_plan. */
+typedef struct mma_hankel_fast_plan_t {
+    double d_ref;     /* reference distance: lambda_k = d_ref / D_k */
+    double sigma;     /* max_k |1 - lambda_k^2| */
+    int64_t n_terms;  /* terms of the multiplication-theorem series */
+    double y_max;     /* largest k r rho / d_ref */
+    double trunc_bound; /* bound on the truncation error relative to the largest |J0| term */
+} mma_hankel_fast_plan_t;
+
+/* Fast form (the chosen form): J0(lambda y) = sum_m ((1 - lambda^2) y / 2)^m / m! J_m(y)
+ * (Bessel multiplication theorem) separates the plane distance from the (r, rho) kernel,
+ * so the z-trapezoid is contracted first:
+ *   B_m[w, r]   = sum_k tau_k v_k^m A_k[w, r],  v_k = (1 - lambda_k^2)/sigma     (HBM-bound)
+ *   FF[rho, w]  = sum_{r, m} K_m(k r rho / d_ref) B_m[w, r],
+ *   K_m(y) = (sigma y / 2)^m J_m(y) / m!, by a division-free recurrence from J0, J1. (FP32)
+ * FP32 arithmetic, float-float phases, compensated sums; planes requested through
+ * plane_slot are evaluated directly (FP32, one J0 per term).
+ * The host fills `plan` with mma_hankel_fast_plan (zgrid on the host). */
+int mma_hankel_fast_plan(const double *zgrid_host, int64_t n_z, double distance, double omega_max, double r_max,
+                         double rho_max, double tol, mma_hankel_fast_plan_t *plan);
+size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan);
+int mma_hankel_fast(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan, const double *ogrid,
+                    const double *rgrid, const double *zgrid, const double *rho, const void *source, const double *pre,
+                    double *ff, const int64_t *plane_slot, int n_planes, double *planes, void *scratch,
+                    size_t scratch_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,526 @@
+// hankel.cu -- far-field (Hankel) kernels: the plain FP64 form and the fast form.
+//
+// Reference: Hankel/Hankel_transform.py:452-519 (HankelTransform), :523-686 (Hankel_long).
+// Per plane k and frequency w (k_w = w/c, D_k = distance - z_k):
+//   A_k[w, r]   = pre_k(w) e^{-i k_w r^2/(2 D_k)} r S_k[w, r] wr_r      (wr = r trapezoid weights)
+//   P_k[w, rho] = sum_r A_k[w, r] J0(k_w r rho / D_k)
+//   FF[rho, w]  = sum_k tau_k P_k[w, rho]                               (tau = z trapezoid weights)
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "../../include/mma_hankel.h"
+#include "../../include/mma_tdse.h"
+
+namespace mma {
+namespace hk {
+
+constexpr double kC = 299792458.0;  // shared_python/units.py:3
+constexpr int kThreads = 256;
+constexpr int kMaxRhoPerThread = 8;  // plain form: n_rho <= 2048
+
+__device__ __forceinline__ double trap_w(const double* x, int64_t i, int64_t n)
+{
+    double w = 0.0;
+    if (i + 1 < n) w += 0.5 * (x[i + 1] - x[i]);
+    if (i > 0) w += 0.5 * (x[i] - x[i - 1]);
+    return w;
+}
+
+__device__ __forceinline__ double2 load_src_d(const void* src, int64_t idx, int64_t c128)
+{
+    if (c128) return reinterpret_cast<const double2*>(src)[idx];
+    const float2 v = reinterpret_cast<const float2*>(src)[idx];
+    return make_double2(v.x, v.y);
+}
+
+__device__ __forceinline__ float2 load_src_f(const void* src, int64_t idx, int64_t c128)
+{
+    if (c128) {
+        const double2 v = reinterpret_cast<const double2*>(src)[idx];
+        return make_float2((float)v.x, (float)v.y);
+    }
+    return reinterpret_cast<const float2*>(src)[idx];
+}
+
+// ------------------------------------------------------------------------ plain FP64 form
+// One CTA per frequency; per plane the CTA builds A_k[r] in shared memory, then each thread
+// accumulates its rho values with CUDA's FP64 j0, in the reference's argument order
+// k * r * rho / D.  The z-trapezoid is accumulated in registers (deterministic order).
+__global__ void __launch_bounds__(kThreads) plain_kernel(mma_hankel_problem P, const double* og, const double* rg,
+                                                         const double* zg, const double* rho, const void* src,
+                                                         const double2* pre, double2* ff, const int64_t* slot,
+                                                         double2* planes)
+{
+    extern __shared__ double2 A[];  // n_r
+    const int64_t o = blockIdx.x;
+    const int64_t Nr = P.n_r, Nz = P.n_z, Nrho = P.n_rho, No = P.n_omega;
+    const double k = og[o] / kC;
+    double2 acc[kMaxRhoPerThread];
+#pragma unroll
+    for (int q = 0; q < kMaxRhoPerThread; q++) acc[q] = make_double2(0.0, 0.0);
+    for (int64_t kz = 0; kz < Nz; kz++) {
+        const double D = P.distance - zg[kz];
+        const double tau = trap_w(zg, kz, Nz);
+        const double2 pf = pre ? pre[kz * No + o] : make_double2(1.0, 0.0);
+        __syncthreads();
+        for (int64_t r = threadIdx.x; r < Nr; r += blockDim.x) {
+            const double rr = rg[r];
+            const double2 s = load_src_d(src, kz * P.plane_stride + o * P.omega_stride + r, P.source_c128);
+            double2 a = pf;
+            if (P.near_field) {  // exp(-1j k r^2 / (2 D)), Hankel_transform.py:506
+                double sn, cs;
+                sincos(-((k * (rr * rr)) / (2.0 * D)), &sn, &cs);
+                a = make_double2(a.x * cs - a.y * sn, a.x * sn + a.y * cs);
+            }
+            a = make_double2(a.x * rr, a.y * rr);
+            a = make_double2(a.x * s.x - a.y * s.y, a.x * s.y + a.y * s.x);
+            const double w = trap_w(rg, r, Nr);
+            A[r] = make_double2(a.x * w, a.y * w);
+        }
+        __syncthreads();
+        const int64_t sl = slot ? slot[kz] : -1;
+#pragma unroll
+        for (int q = 0; q < kMaxRhoPerThread; q++) {
+            const int64_t j = threadIdx.x + (int64_t)q * blockDim.x;
+            if (j < Nrho) {
+                const double rj = rho[j];
+                double re = 0.0, im = 0.0;
+                for (int64_t r = 0; r < Nr; r++) {
+                    const double J = j0(k * rg[r] * rj / D);
+                    re = fma(A[r].x, J, re);
+                    im = fma(A[r].y, J, im);
+                }
+                if (sl >= 0 && planes) planes[(sl * Nrho + j) * No + o] = make_double2(re, im);
+                acc[q].x = fma(tau, re, acc[q].x);
+                acc[q].y = fma(tau, im, acc[q].y);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kMaxRhoPerThread; q++) {
+        const int64_t j = threadIdx.x + (int64_t)q * blockDim.x;
+        if (j < Nrho) ff[j * No + o] = acc[q];
+    }
+}
+
+// ------------------------------------------------------------------------ fast form helpers
+__device__ __forceinline__ void split_d(double v, float& hi, float& lo)
+{
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// (yh + yl) reduced mod 2 pi with 2 pi = C1 + C2 + C3 (C1, C2 short enough that k*C is exact)
+__device__ __forceinline__ float reduce_2pi(float yh, float yl)
+{
+    const float kk = rintf(yh * 0.159154943f);
+    float r = fmaf(-kk, 6.28125f, yh);
+    r = fmaf(-kk, 1.93500518798828125e-3f, r);
+    r = fmaf(-kk, 3.0199159819370158e-07f, r);
+    return r + yl;
+}
+
+// J0 and J1 in FP32 from the rational/asymptotic approximations of Abramowitz & Stegun
+// 9.4.1, 9.4.4 (x < 3) and 9.4.3, 9.4.6 (x >= 3; modulus and phase, |error| < 1e-7 absolute),
+// with the phase argument x reduced mod 2 pi in float-float (x = yh + yl).
+template <bool WANT_J1>
+__device__ __forceinline__ void bessel01(float yh, float yl, float& J0, float& J1)
+{
+    if (yh < 3.0f) {
+        const float y = yh + yl;
+        const float u = (y * 0.333333343f) * (y * 0.333333343f);
+        J0 = fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, 0.0002100f, -0.0039444f), 0.0444479f), -0.3163866f),
+                                      1.2656208f), -2.2499997f), 1.0f);
+        if (WANT_J1)
+            J1 = y * fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, 0.00001109f, -0.00031761f), 0.00443319f),
+                                               -0.03954289f), 0.21093573f), -0.56249985f), 0.5f);
+    } else {
+        const float t = 3.0f / yh;
+        const float red = reduce_2pi(yh, yl);
+        const float sq = rsqrtf(yh);
+        const float f0 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.00014476f, -0.00072805f), 0.00137237f),
+                                                   -0.00009512f), -0.00552740f), -0.00000077f), 0.79788456f);
+        const float p0 = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.00013558f, -0.00029333f), -0.00054125f),
+                                               0.00262573f), -0.00003954f), -0.04166397f);
+        J0 = f0 * sq * cosf(red - 0.785398163f + p0);
+        if (WANT_J1) {
+            const float f1 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, -0.00020033f, 0.00113653f), -0.00249511f),
+                                                       0.00017105f), 0.01659667f), 0.00000156f), 0.79788456f);
+            const float p1 = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, -0.00029166f, 0.00079824f), 0.00074348f),
+                                                   -0.00637879f), 0.00005650f), 0.12499612f);
+            J1 = f1 * sq * cosf(red - 2.35619449f + p1);
+        }
+    }
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// add a partial sum into a float-float accumulator (hi, lo)
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float part)
+{
+    float s, e;
+    two_sum(hi, part, s, e);
+    hi = s;
+    lo += e;
+}
+
+// ------------------------------------------------------------------------ fast form, stage 1
+// z-contraction B_m[w, r] = sum_k tau_k v_k^m A_k[w, r]: one thread per (w, r), source read once.
+template <int MM>
+__global__ void __launch_bounds__(kThreads) fast_stage1(mma_hankel_problem P, mma_hankel_fast_plan_t F,
+                                                        const double* og, const double* rg, const double* zg,
+                                                        const void* src, const double2* pre, float2* Bp)
+{
+    extern __shared__ float smem[];
+    const int64_t o = blockIdx.y, Nz = P.n_z, Nr = P.n_r, No = P.n_omega;
+    float* coef = smem;                                           // Nz * MM
+    float2* k2 = reinterpret_cast<float2*>(smem + ((Nz * MM + 1) / 2) * 2);  // Nz: k/(2 D_k) (hi, lo)
+    float2* pr = k2 + Nz;                                         // Nz: pre-factor
+    const double k = og[o] / kC;
+    for (int64_t q = threadIdx.x; q < Nz; q += blockDim.x) {
+        const double D = P.distance - zg[q];
+        const double lam = F.d_ref / D;
+        const double v = (1.0 - lam * lam) / F.sigma;
+        double c = trap_w(zg, q, Nz);
+        for (int m = 0; m < MM; m++) {
+            coef[q * MM + m] = (float)c;
+            c *= v;
+        }
+        float hi, lo;
+        split_d(k / (2.0 * D), hi, lo);
+        k2[q] = make_float2(hi, lo);
+        const double2 pf = pre ? pre[q * No + o] : make_double2(1.0, 0.0);
+        pr[q] = make_float2((float)pf.x, (float)pf.y);
+    }
+    __syncthreads();
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= Nr) return;  // no barrier below
+    const double rr = rg[r];
+    float r2h, r2l;
+    split_d(rr * rr, r2h, r2l);
+    const float wr = (float)(trap_w(rg, r, Nr) * rr);
+    float2 part[MM], hi[MM], lo[MM];
+#pragma unroll
+    for (int m = 0; m < MM; m++) part[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
+    for (int64_t kz = 0; kz < Nz; kz++) {
+        const float2 s = load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r, P.source_c128);
+        const float2 pf = pr[kz];
+        float2 a = make_float2(fmaf(pf.x, s.x, -pf.y * s.y), fmaf(pf.x, s.y, pf.y * s.x));
+        if (P.near_field) {
+            const float2 kk = k2[kz];
+            const float th = kk.x * r2h;
+            const float te = fmaf(kk.x, r2h, -th) + fmaf(kk.x, r2l, kk.y * r2h);
+            float sn, cs;
+            sincosf(reduce_2pi(th, te), &sn, &cs);  // e^{-i theta} = (cs, -sn)
+            a = make_float2(fmaf(a.x, cs, a.y * sn), fmaf(a.y, cs, -a.x * sn));
+        }
+        a.x *= wr;
+        a.y *= wr;
+        const float* cz = coef + kz * MM;
+#pragma unroll
+        for (int m = 0; m < MM; m++) {
+            part[m].x = fmaf(cz[m], a.x, part[m].x);
+            part[m].y = fmaf(cz[m], a.y, part[m].y);
+        }
+        if ((kz & 15) == 15 || kz == Nz - 1) {
+#pragma unroll
+            for (int m = 0; m < MM; m++) {
+                ff_acc(hi[m].x, lo[m].x, part[m].x);
+                ff_acc(hi[m].y, lo[m].y, part[m].y);
+                part[m] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < MM; m++) Bp[(o * MM + m) * Nr + r] = make_float2(hi[m].x + lo[m].x, hi[m].y + lo[m].y);
+}
+
+// ------------------------------------------------------------------------ fast form, stage 2
+// FF[rho, w] = sum_r sum_m K_m(y) B_m[w, r], y = k_w r rho / d_ref, with
+//   K_0 = J0(y), K_1 = (sigma y/2) J1(y),
+//   K_{m+1} = sigma m/(m+1) K_m - (sigma y/2)^2 / (m (m+1)) K_{m-1}
+// (J_{m+1} = (2m/y) J_m - J_{m-1} rescaled by (sigma y/2)^m/m!: no division by y).
+// One thread per (w, rho); B and k r / d_ref staged in shared memory in tiles of r.
+template <int MM>
+__global__ void __launch_bounds__(kThreads) fast_stage2(mma_hankel_problem P, mma_hankel_fast_plan_t F,
+                                                        const double* og, const double* rg, const double* rho,
+                                                        const float2* Bp, double2* ff, int rtile)
+{
+    extern __shared__ float smem[];
+    const int64_t o = blockIdx.y, Nr = P.n_r, Nrho = P.n_rho, No = P.n_omega;
+    float2* B = reinterpret_cast<float2*>(smem);  // MM * rtile
+    float2* kr = B + MM * rtile;                  // rtile
+    const double kap = (og[o] / kC) / F.d_ref;
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float rh = 0.f, rl = 0.f;
+    if (j < Nrho) split_d(rho[j], rh, rl);
+    const float s = (float)F.sigma;
+    float2 part = make_float2(0.f, 0.f), hi = part, lo = part;
+    int cnt = 0;
+    for (int64_t r0 = 0; r0 < Nr; r0 += rtile) {
+        const int64_t nt = (Nr - r0 < rtile) ? (Nr - r0) : rtile;
+        __syncthreads();
+        for (int64_t q = threadIdx.x; q < MM * nt; q += blockDim.x) {
+            const int64_t m = q / nt, rr = q % nt;
+            B[m * rtile + rr] = Bp[(o * MM + m) * Nr + r0 + rr];
+        }
+        for (int64_t q = threadIdx.x; q < nt; q += blockDim.x) {
+            float h, l;
+            split_d(kap * rg[r0 + q], h, l);
+            kr[q] = make_float2(h, l);
+        }
+        __syncthreads();
+        if (j < Nrho) {
+            for (int64_t q = 0; q < nt; q++) {
+                const float2 kk = kr[q];
+                const float yh = kk.x * rh;
+                const float yl = fmaf(kk.x, rh, -yh) + fmaf(kk.x, rl, kk.y * rh);
+                float J0, J1;
+                bessel01<true>(yh, yl, J0, J1);
+                const float y = yh + yl;
+                float K0 = J0, K1 = 0.5f * s * y * J1;
+                const float q2 = 0.25f * s * s * y * y;
+                float2 b0 = B[q], b1 = B[rtile + q];
+                float2 in = make_float2(fmaf(b0.x, K0, b1.x * K1), fmaf(b0.y, K0, b1.y * K1));
+#pragma unroll
+                for (int m = 1; m + 1 < MM; m++) {
+                    const float K2 = fmaf(s * ((float)m / (float)(m + 1)), K1, -(q2 * (1.0f / (float)(m * (m + 1)))) * K0);
+                    const float2 b = B[(m + 1) * rtile + q];
+                    in.x = fmaf(b.x, K2, in.x);
+                    in.y = fmaf(b.y, K2, in.y);
+                    K0 = K1;
+                    K1 = K2;
+                }
+                part.x += in.x;
+                part.y += in.y;
+                if (++cnt == 16) {
+                    ff_acc(hi.x, lo.x, part.x);
+                    ff_acc(hi.y, lo.y, part.y);
+                    part = make_float2(0.f, 0.f);
+                    cnt = 0;
+                }
+            }
+        }
+    }
+    if (j < Nrho) {
+        ff_acc(hi.x, lo.x, part.x);
+        ff_acc(hi.y, lo.y, part.y);
+        ff[j * No + o] = make_double2((double)hi.x + (double)lo.x, (double)hi.y + (double)lo.y);
+    }
+}
+
+// ------------------------------------------------------------------------ fast form, single planes
+// P_k[w, rho] evaluated directly in FP32 (one J0 per term): grid (rho blocks, w, requested plane).
+__global__ void __launch_bounds__(kThreads) fast_planes(mma_hankel_problem P, const double* og, const double* rg,
+                                                        const double* zg, const double* rho, const void* src,
+                                                        const double2* pre, const int64_t* slot, double2* planes,
+                                                        int rtile)
+{
+    extern __shared__ float smem[];
+    float2* A = reinterpret_cast<float2*>(smem);  // rtile
+    float2* kd = A + rtile;                       // rtile: k r / D_k (hi, lo)
+    const int64_t o = blockIdx.y, Nr = P.n_r, Nrho = P.n_rho, No = P.n_omega, Nz = P.n_z;
+    const int64_t want = blockIdx.z;
+    int64_t kz = -1;
+    for (int64_t q = 0; q < Nz; q++)
+        if (slot[q] == want) kz = q;
+    if (kz < 0) return;  // uniform over the CTA
+    const double k = og[o] / kC, D = P.distance - zg[kz];
+    const double2 pf = pre ? pre[kz * No + o] : make_double2(1.0, 0.0);
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float rh = 0.f, rl = 0.f;
+    if (j < Nrho) split_d(rho[j], rh, rl);
+    float2 part = make_float2(0.f, 0.f), hi = part, lo = part;
+    int cnt = 0;
+    for (int64_t r0 = 0; r0 < Nr; r0 += rtile) {
+        const int64_t nt = (Nr - r0 < rtile) ? (Nr - r0) : rtile;
+        __syncthreads();
+        for (int64_t q = threadIdx.x; q < nt; q += blockDim.x) {
+            const int64_t r = r0 + q;
+            const double rr = rg[r];
+            const double2 sd = load_src_d(src, kz * P.plane_stride + o * P.omega_stride + r, P.source_c128);
+            double2 a = pf;
+            if (P.near_field) {
+                double sn, cs;
+                sincos(-((k * (rr * rr)) / (2.0 * D)), &sn, &cs);
+                a = make_double2(a.x * cs - a.y * sn, a.x * sn + a.y * cs);
+            }
+            const double w = trap_w(rg, r, Nr) * rr;
+            a = make_double2(a.x * w, a.y * w);
+            A[q] = make_float2((float)(a.x * sd.x - a.y * sd.y), (float)(a.x * sd.y + a.y * sd.x));
+            float h, l;
+            split_d(k * rr / D, h, l);
+            kd[q] = make_float2(h, l);
+        }
+        __syncthreads();
+        if (j < Nrho) {
+            for (int64_t q = 0; q < nt; q++) {
+                const float2 kk = kd[q];
+                const float yh = kk.x * rh;
+                const float yl = fmaf(kk.x, rh, -yh) + fmaf(kk.x, rl, kk.y * rh);
+                float J0, J1;
+                bessel01<false>(yh, yl, J0, J1);
+                part.x = fmaf(A[q].x, J0, part.x);
+                part.y = fmaf(A[q].y, J0, part.y);
+                if (++cnt == 16) {
+                    ff_acc(hi.x, lo.x, part.x);
+                    ff_acc(hi.y, lo.y, part.y);
+                    part = make_float2(0.f, 0.f);
+                    cnt = 0;
+                }
+            }
+        }
+    }
+    if (j < Nrho) {
+        ff_acc(hi.x, lo.x, part.x);
+        ff_acc(hi.y, lo.y, part.y);
+        planes[(want * Nrho + j) * No + o] = make_double2((double)hi.x + (double)lo.x, (double)hi.y + (double)lo.y);
+    }
+}
+
+bool valid(const mma_hankel_problem* p)
+{
+    return p && p->n_omega > 0 && p->n_r > 1 && p->n_z > 0 && p->n_rho > 0 && p->distance == p->distance &&
+           p->plane_stride >= 0 && p->omega_stride >= p->n_r;
+}
+
+constexpr int kTerms[] = {8, 12, 16, 20, 24, 32, 40, 48};
+
+}  // namespace hk
+}  // namespace mma
+
+using namespace mma::hk;
+
+extern "C" int mma_hankel_plain(const mma_hankel_problem* p, const double* ogrid, const double* rgrid,
+                                const double* zgrid, const double* rho, const void* source, const double* pre,
+                                double* ff, const int64_t* plane_slot, int n_planes, double* planes, void* stream)
+{
+    if (!valid(p) || !ogrid || !rgrid || !zgrid || !rho || !source || !ff) return MMA_ERR_ARG;
+    if (p->n_rho > (int64_t)kThreads * kMaxRhoPerThread) return MMA_ERR_TOO_LARGE;
+    if ((n_planes > 0) != (plane_slot != nullptr && planes != nullptr)) return MMA_ERR_ARG;
+    const size_t smem = sizeof(double2) * (size_t)p->n_r;
+    if (smem > 220 * 1024) return MMA_ERR_TOO_LARGE;
+    cudaFuncSetAttribute(plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    plain_kernel<<<(unsigned)p->n_omega, kThreads, smem, (cudaStream_t)stream>>>(
+        *p, ogrid, rgrid, zgrid, rho, source, reinterpret_cast<const double2*>(pre), reinterpret_cast<double2*>(ff),
+        n_planes > 0 ? plane_slot : nullptr, reinterpret_cast<double2*>(planes));
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
+
+extern "C" int mma_hankel_fast_plan(const double* zg, int64_t nz, double distance, double omega_max, double r_max,
+                                    double rho_max, double tol, mma_hankel_fast_plan_t* plan)
+{
+    if (!zg || nz < 1 || !plan || !(tol > 0.0)) return MMA_ERR_ARG;
+    double dmin = 1e300, dmax = -1e300;
+    for (int64_t k = 0; k < nz; k++) {
+        const double D = distance - zg[k];
+        if (!(D > 0.0)) return MMA_ERR_ARG;
+        dmin = D < dmin ? D : dmin;
+        dmax = D > dmax ? D : dmax;
+    }
+    const double d_ref = std::sqrt(2.0 / (1.0 / (dmin * dmin) + 1.0 / (dmax * dmax)));
+    double sigma = 0.0;
+    for (int64_t k = 0; k < nz; k++) {
+        const double l = d_ref / (distance - zg[k]);
+        sigma = std::fabs(1.0 - l * l) > sigma ? std::fabs(1.0 - l * l) : sigma;
+    }
+    if (!(sigma > 1e-300)) sigma = 1.0;  // one distance only: v_k = 0, the m = 0 term is exact
+    const double y_max = std::fabs(omega_max) / kC * std::fabs(r_max) * std::fabs(rho_max) / d_ref;
+    const double x = 0.5 * sigma * y_max;
+    // smallest M with x^M / M! e^x < tol (|J_m| <= 1 bounds the dropped tail)
+    int need = -1;
+    double term = 1.0;
+    for (int m = 1; m <= 64; m++) {
+        term *= x / m;
+        if (term * std::exp(x) < tol) {
+            need = m;
+            break;
+        }
+    }
+    if (need < 0) return MMA_ERR_UNSUPPORTED;
+    int M = -1;
+    for (int c : kTerms)
+        if (c >= need && c >= 2) {
+            M = c;
+            break;
+        }
+    if (M < 0) return MMA_ERR_UNSUPPORTED;
+    double t = 1.0;
+    for (int m = 1; m <= M; m++) t *= x / m;
+    plan->d_ref = d_ref;
+    plan->sigma = sigma;
+    plan->n_terms = M;
+    plan->y_max = y_max;
+    plan->trunc_bound = t * std::exp(x);
+    return MMA_OK;
+}
+
+extern "C" size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
+{
+    if (!p || !plan) return 0;
+    return sizeof(float2) * (size_t)p->n_omega * (size_t)plan->n_terms * (size_t)p->n_r;
+}
+
+namespace {
+template <int MM>
+int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, const double* og, const double* rg,
+                const double* zg, const double* rho, const void* src, const double2* pre, double2* ff,
+                float2* Bp, cudaStream_t st)
+{
+    const size_t s1 = sizeof(float) * (((size_t)p->n_z * MM + 1) / 2 * 2) + sizeof(float2) * 2 * (size_t)p->n_z;
+    if (s1 > 200 * 1024) return MMA_ERR_TOO_LARGE;
+    cudaFuncSetAttribute(fast_stage1<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
+    dim3 g1((unsigned)((p->n_r + kThreads - 1) / kThreads), (unsigned)p->n_omega);
+    fast_stage1<MM><<<g1, kThreads, s1, st>>>(*p, *plan, og, rg, zg, src, pre, Bp);
+    int rtile = (int)(p->n_r < 512 ? p->n_r : 512);
+    while ((size_t)(MM + 1) * rtile * sizeof(float2) > 96 * 1024 && rtile > 32) rtile /= 2;
+    const size_t s2 = (size_t)(MM + 1) * rtile * sizeof(float2);
+    cudaFuncSetAttribute(fast_stage2<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
+    dim3 g2((unsigned)((p->n_rho + kThreads - 1) / kThreads), (unsigned)p->n_omega);
+    fast_stage2<MM><<<g2, kThreads, s2, st>>>(*p, *plan, og, rg, rho, Bp, ff, rtile);
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
+}  // namespace
+
+extern "C" int mma_hankel_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, const double* ogrid,
+                               const double* rgrid, const double* zgrid, const double* rho, const void* source,
+                               const double* pre, double* ff, const int64_t* plane_slot, int n_planes,
+                               double* planes, void* scratch, size_t scratch_bytes, void* stream)
+{
+    if (!valid(p) || !plan || !ogrid || !rgrid || !zgrid || !rho || !source || !ff) return MMA_ERR_ARG;
+    if ((n_planes > 0) != (plane_slot != nullptr && planes != nullptr)) return MMA_ERR_ARG;
+    if (!scratch || scratch_bytes < mma_hankel_fast_scratch_bytes(p, plan)) return MMA_ERR_ARG;
+    if (!(plan->sigma > 0.0) || !(plan->d_ref > 0.0)) return MMA_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const double2* pre2 = reinterpret_cast<const double2*>(pre);
+    double2* ff2 = reinterpret_cast<double2*>(ff);
+    float2* Bp = reinterpret_cast<float2*>(scratch);
+    int rc;
+    switch (plan->n_terms) {
+        case 8: rc = launch_fast<8>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
+        case 12: rc = launch_fast<12>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
+        case 16: rc = launch_fast<16>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
+        case 20: rc = launch_fast<20>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
+        case 24: rc = launch_fast<24>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
+        case 32: rc = launch_fast<32>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
+        case 40: rc = launch_fast<40>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
+        case 48: rc = launch_fast<48>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
+        default: return MMA_ERR_ARG;
+    }
+    if (rc != MMA_OK) return rc;
+    if (n_planes > 0) {
+        const int rtile = (int)(p->n_r < 1024 ? p->n_r : 1024);
+        const size_t sp = 2 * sizeof(float2) * (size_t)rtile;
+        dim3 gp((unsigned)((p->n_rho + kThreads - 1) / kThreads), (unsigned)p->n_omega, (unsigned)n_planes);
+        fast_planes<<<gp, kThreads, sp, st>>>(*p, ogrid, rgrid, zgrid, rho, source, pre2, plane_slot,
+                                              reinterpret_cast<double2*>(planes), rtile);
+        if (cudaGetLastError() != cudaSuccess) return MMA_ERR_CUDA;
+    }
+    return MMA_OK;
+}

@@ -1,0 +1,365 @@
+"""The far-field integral on the GPU, mirroring Hankel/Hankel_transform.py.
+
+Same names, arguments and results as the reference module:
+
+* ``trapezoidal_integrator`` (:22) -- the only radial integrator; it is a marker
+  here (the kernels apply trapezoid weights), other integrators raise.
+* ``FSources_provider`` (:29-80) -- planes zgrid[0:-1:kz_step] (the last plane is
+  dropped, as in the reference), source slices FSource[kz, omega, r]; the static
+  source is moved to the GPU once.  'dynamic' (HDF5) sources raise: no h5py here.
+* ``get_propagation_pre_factor_function`` (:85-448) -- the no-modulation branch
+  (scalar pressure) and the z-modulation branch (dict with 'zgrid', 'value'),
+  returning (pre_factor(kz) -> [Nr, No], exp_renorm(kz) -> [No]) like the reference.
+* ``HankelTransform`` (:452-519) -> [No, Nrho] complex128.
+* ``Hankel_long`` (:523-686) -- FF_integrated [Nrho, No], entry/exit planes,
+  cumulative results.  ``form="plain"`` runs the reference's arithmetic in FP64
+  (CUDA kernels in mma_gb300/csrc/hankel.cu); ``form="fast"`` runs the chosen
+  form (Bessel multiplication theorem, z-first contraction, FP32 with float-float
+  phases) and records its truncation bound in ``self.fast_plan``.
+
+Refractive index: the reference reads f1/f2 tables through XUV_refractive_index
+(HDF5).  Here ``XUV_index`` is a provider with the same two functions; by default it
+models a constant complex XUV index (``XUV_index.set_constant_index``).
+"""
+import ctypes
+from ctypes import POINTER, Structure, c_double, c_int, c_int64, c_size_t, c_void_p
+
+import numpy as np
+import torch
+
+from ._lib import load
+
+C_LIGHT = 299792458.0  # shared_python/units.py:3
+
+
+# ------------------------------------------------------------------------------ C-ABI records
+class HankelProblem(Structure):
+    _fields_ = [("n_omega", c_int64), ("n_r", c_int64), ("n_z", c_int64), ("n_rho", c_int64), ("distance", c_double),
+                ("near_field", c_int64), ("source_c128", c_int64), ("plane_stride", c_int64),
+                ("omega_stride", c_int64)]
+
+
+class FastPlan(Structure):
+    _fields_ = [("d_ref", c_double), ("sigma", c_double), ("n_terms", c_int64), ("y_max", c_double),
+                ("trunc_bound", c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class HankelError(RuntimeError):
+    pass
+
+
+def _sig():
+    lib = load()
+    if getattr(lib, "_mma_hankel_sig", False):
+        return lib
+    P = POINTER(HankelProblem)
+    lib.mma_hankel_plain.argtypes = [P, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                     c_void_p, c_int, c_void_p, c_void_p]
+    lib.mma_hankel_plain.restype = c_int
+    lib.mma_hankel_fast_plan.argtypes = [POINTER(c_double), c_int64, c_double, c_double, c_double, c_double,
+                                         c_double, POINTER(FastPlan)]
+    lib.mma_hankel_fast_plan.restype = c_int
+    lib.mma_hankel_fast_scratch_bytes.argtypes = [P, POINTER(FastPlan)]
+    lib.mma_hankel_fast_scratch_bytes.restype = c_size_t
+    lib.mma_hankel_fast.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p]
+    lib.mma_hankel_fast.restype = c_int
+    lib._mma_hankel_sig = True
+    return lib
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise HankelError("%s failed with status %d" % (what, rc))
+
+
+# ------------------------------------------------------------------------------ refractive index
+class _XUVIndex:
+    """Stand-in for XUV_refractive_index (dispersion_function :125, beta_factor_ref :164) with
+    a constant complex index n = n0 + i beta per reference density; the dispersion term
+    scales with pressure like the tabulated one."""
+
+    def __init__(self):
+        self.set_constant_index(complex(1 - 1e-5, 1e-7))
+
+    def set_constant_index(self, n, gases=("Ar_Henke", "Ar_NIST", "Ne_Henke", "He_Henke", "Kr_Henke", "Xe_Henke")):
+        self.n = complex(n)
+        self.gases = list(gases)
+
+    def dispersion_function(self, omega, pressure, gas, n_IR=1.0):
+        return pressure * (n_IR - self.n.real) / C_LIGHT * np.ones_like(np.asarray(omega, dtype=float))
+
+    def beta_factor_ref(self, omega, gas):
+        return self.n.imag * np.ones_like(np.asarray(omega, dtype=float))
+
+
+XUV_index = _XUVIndex()
+
+
+def trapezoidal_integrator(y, x):
+    """Marker for the reference's default radial integrator (scipy trapezoid, :22-27)."""
+    from scipy import integrate
+
+    return integrate.trapezoid(y, x=x)
+
+
+# ------------------------------------------------------------------------------ sources
+class FSources_provider:
+    """Planes and source of a long medium (Hankel_transform.py:29-80)."""
+
+    def __init__(self, zgrid, rgrid, ogrid, data_source="static", FSource=None, h5_handle=None, h5_path=None,
+                 ko_min=0, ko_step=1, ko_max="end", kr_step=1, kr_max="end", kz_step=1, device="cuda"):
+        if ko_max == "end":
+            ko_max = len(ogrid)
+        if kr_max == "end":
+            kr_max = len(rgrid)
+        self.zgrid = np.asarray(zgrid)[0:-1:kz_step]
+        self.rgrid = np.asarray(rgrid)[0:kr_max:kr_step]
+        self.ogrid = np.asarray(ogrid)[ko_min:ko_max:ko_step]
+        if data_source == "static":
+            nz = len(self.zgrid)
+            if torch.is_tensor(FSource):
+                S = FSource[0:nz * kz_step:kz_step, ko_min:ko_max:ko_step, 0:kr_max:kr_step]
+            else:
+                S = torch.from_numpy(np.ascontiguousarray(
+                    np.asarray(FSource)[0:nz * kz_step:kz_step, ko_min:ko_max:ko_step, 0:kr_max:kr_step]))
+            if S.dtype not in (torch.complex64, torch.complex128):
+                S = S.to(torch.complex128)
+            self.source = S.to(device).contiguous()
+        elif data_source == "dynamic":
+            raise NotImplementedError("HDF5 ('dynamic') sources need h5py, which this build does not use")
+        else:
+            raise ValueError("Wrongly specified input of the class.")
+
+        def _planes():
+            for k in range(self.source.shape[0]):
+                yield self.source[k]
+
+        self.Fsource_plane = _planes()
+
+
+# ------------------------------------------------------------------------------ pre-factor
+def get_propagation_pre_factor_function(zgrid, rgrid, ogrid, preset_gas="vacuum", pressure=1.0,
+                                        absorption_tables="Henke", include_absorption=True, dispersion_tables="Henke",
+                                        include_dispersion=True, effective_IR_refrective_index=1.0):
+    """(pre_factor, exp_renorm) as in Hankel_transform.py:85-448 (no-modulation :405-448,
+    z-modulation :146-239).  Returns numpy closures; ``pre_table`` gives [Nz, No]."""
+    pre_tab, renorm_tab = pre_factor_table(zgrid, ogrid, preset_gas, pressure, absorption_tables, include_absorption,
+                                           dispersion_tables, include_dispersion, effective_IR_refrective_index)
+    Nr = len(rgrid)
+
+    def pre_factor(kz):
+        return np.outer(np.ones(Nr), pre_tab[kz])
+
+    def exp_renorm(kz):
+        return renorm_tab[kz]
+
+    pre_factor.pre_table = pre_tab
+    exp_renorm.table = renorm_tab
+    return pre_factor, exp_renorm
+
+
+def pre_factor_table(zgrid, ogrid, preset_gas="vacuum", pressure=1.0, absorption_tables="Henke",
+                     include_absorption=True, dispersion_tables="Henke", include_dispersion=True,
+                     effective_IR_refrective_index=1.0):
+    """[Nz, No] pre-factor and renormalisation tables (the reference's closures evaluated)."""
+    z = np.asarray(zgrid, dtype=np.float64)
+    w = np.asarray(ogrid, dtype=np.float64)
+    n_ir = effective_IR_refrective_index
+    if isinstance(pressure, dict):
+        if "rgrid" in pressure:
+            raise NotImplementedError("radially modulated density (r and zr branches) is not implemented")
+        from scipy import integrate, interpolate
+
+        pz, pv = np.asarray(pressure["zgrid"]), np.asarray(pressure["value"])
+        p_loc = interpolate.interp1d(pz, pv, bounds_error=False, fill_value=(pv[0], pv[-1]), copy=False)(z)
+        pre = np.empty((len(z), len(w)), dtype=np.complex128)
+        absw = np.empty((len(z), len(w)))
+        for k1 in range(len(w)):
+            if include_dispersion:
+                integrand = XUV_index.dispersion_function(w[k1], pv, preset_gas + "_" + dispersion_tables, n_IR=n_ir)
+                ph = integrate.cumulative_trapezoid(integrand, x=pz, initial=0.0)
+                disp = 1j * interpolate.interp1d(pz, ph, bounds_error=False, fill_value=(ph[0], ph[-1]), copy=False)(z)
+            else:
+                disp = 1j * (n_ir - 1.0) / C_LIGHT
+            if include_absorption:
+                ib = XUV_index.beta_factor_ref(w[k1], preset_gas + "_" + absorption_tables) * \
+                    integrate.cumulative_trapezoid(pv, x=pz, initial=0.0)
+                absf = (1.0 / C_LIGHT) * interpolate.interp1d(pz, ib, bounds_error=False, fill_value=(ib[0], ib[-1]),
+                                                              copy=False)(z)
+                absw[:, k1] = w[k1] * absf
+                absf = absf - absf[-1]
+            else:
+                absf = 0.0
+                absw[:, k1] = 0.0
+            pre[:, k1] = p_loc * np.exp(w[k1] * (disp + absf))
+        renorm = np.exp(absw[-1][None, :] - absw)
+        return pre, renorm
+    if include_dispersion:
+        disp = 1j * XUV_index.dispersion_function(w, pressure, preset_gas + "_" + dispersion_tables, n_IR=n_ir)
+    else:
+        disp = 1j * (n_ir - 1.0) / C_LIGHT * np.ones_like(w)
+    if include_absorption:
+        absorb = (pressure / C_LIGHT) * XUV_index.beta_factor_ref(w, preset_gas + "_" + absorption_tables)
+    else:
+        absorb = np.zeros_like(w)
+    pre = pressure * np.exp(w[None, :] * (z[:, None] * disp[None, :] + (z[:, None] - z[-1]) * absorb[None, :]))
+    renorm = np.exp((z[-1] - z[:, None]) * (w * absorb)[None, :])
+    return pre, renorm
+
+
+# ------------------------------------------------------------------------------ kernels
+def _dev(a, device):
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=device)
+
+
+def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_field=True, planes=(), form="plain",
+              tol=1e-9, stream=None):
+    """Run the far-field kernels.  source: torch complex tensor [Nz, No, Nr] on the GPU.
+    Returns (FF [Nrho, No] complex128 tensor, {plane: [Nrho, No] tensor}, fast plan dict or None)."""
+    lib = _sig()
+    dev = source.device
+    Nz, No, Nr = source.shape
+    if len(zgrid) != Nz or len(ogrid) != No or len(rgrid) != Nr:
+        raise ValueError("source shape does not match the grids")
+    S = source.contiguous()
+    prob = HankelProblem(No, Nr, Nz, len(rho), float(distance), int(bool(near_field)),
+                         int(S.dtype == torch.complex128), No * Nr, Nr)
+    og, rg, zg, rh = (_dev(a, dev) for a in (ogrid, rgrid, zgrid, rho))
+    pre = None
+    if pre_table is not None:
+        pre = torch.as_tensor(np.ascontiguousarray(pre_table, dtype=np.complex128), device=dev)
+    ff = torch.zeros(len(rho), No, dtype=torch.complex128, device=dev)
+    planes = sorted(set(int(p) % Nz for p in planes))
+    slot = None
+    pl = None
+    if planes:
+        s = np.full(Nz, -1, dtype=np.int64)
+        for i, p in enumerate(planes):
+            s[p] = i
+        slot = torch.as_tensor(s, device=dev)
+        pl = torch.zeros(len(planes), len(rho), No, dtype=torch.complex128, device=dev)
+    st = ctypes.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
+    ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+    plan_d = None
+    if form == "plain":
+        _check(lib.mma_hankel_plain(ctypes.byref(prob), og.data_ptr(), rg.data_ptr(), zg.data_ptr(), rh.data_ptr(),
+                                    S.data_ptr(), ptr(pre), ff.data_ptr(), ptr(slot), len(planes), ptr(pl), st),
+               "mma_hankel_plain")
+    elif form == "fast":
+        zh = np.ascontiguousarray(zgrid, dtype=np.float64)
+        plan = FastPlan()
+        _check(lib.mma_hankel_fast_plan(zh.ctypes.data_as(POINTER(c_double)), Nz, float(distance),
+                                        float(np.max(np.abs(ogrid))), float(np.max(np.abs(rgrid))),
+                                        float(np.max(np.abs(rho))), float(tol), ctypes.byref(plan)),
+               "mma_hankel_fast_plan")
+        nb = lib.mma_hankel_fast_scratch_bytes(ctypes.byref(prob), ctypes.byref(plan))
+        scratch = torch.empty(int(nb), dtype=torch.uint8, device=dev)
+        _check(lib.mma_hankel_fast(ctypes.byref(prob), ctypes.byref(plan), og.data_ptr(), rg.data_ptr(), zg.data_ptr(),
+                                   rh.data_ptr(), S.data_ptr(), ptr(pre), ff.data_ptr(), ptr(slot), len(planes),
+                                   ptr(pl), scratch.data_ptr(), int(nb), st), "mma_hankel_fast")
+        plan_d = plan.as_dict()
+    else:
+        raise ValueError("form must be 'plain' or 'fast'")
+    out_planes = {p: pl[i] for i, p in enumerate(planes)} if planes else {}
+    return ff, out_planes, plan_d
+
+
+def HankelTransform(ogrid, rgrid, FField, distance, rgrid_FF, integrator=trapezoidal_integrator,
+                    near_field_factor=True, pre_factor=1.0, form="plain"):
+    """One plane (Hankel_transform.py:452-519): FField[omega, r] -> [omega, rho] complex128."""
+    if integrator is not trapezoidal_integrator:
+        raise NotImplementedError("only the trapezoidal radial integrator is implemented")
+    pre = None
+    pf = np.asarray(pre_factor)
+    if pf.ndim == 2:
+        if not np.allclose(pf, pf[:1, :]):
+            raise NotImplementedError("radially varying pre-factors are not implemented")
+        pre = pf[0][None, :]
+    elif pf.ndim == 0 and pf != 1.0:
+        pre = np.full((1, len(ogrid)), complex(pf))
+    src = FField if torch.is_tensor(FField) else torch.from_numpy(np.ascontiguousarray(FField))
+    if src.dtype not in (torch.complex64, torch.complex128):
+        src = src.to(torch.complex128)
+    src = src.to("cuda")[None]
+    # a single plane at z = 0 with the plane's own distance
+    _, planes, _ = far_field(ogrid, rgrid, np.zeros(1), rgrid_FF, src, distance, pre, near_field_factor, planes=(0,),
+                             form=form)
+    return planes[0].T.cpu().numpy()
+
+
+class Hankel_long:
+    """Longitudinally integrated far field (Hankel_transform.py:523-686)."""
+
+    def __init__(self, target, distance, rgrid_FF, preset_gas="vacuum", pressure=1.0, absorption_tables="Henke",
+                 include_absorption=True, dispersion_tables="Henke", include_dispersion=True,
+                 effective_IR_refrective_index=1.0, integrator_Hankel=trapezoidal_integrator,
+                 integrator_longitudinal="trapezoidal", near_field_factor=True, store_cumulative_result=False,
+                 store_non_normalised_cumulative_result=False, store_entry_and_exit_plane_transform=True,
+                 form="plain", tol=1e-9, as_numpy=True):
+        if not (integrator_longitudinal == "trapezoidal"):
+            raise NotImplementedError("only logitudinal trapezoidal integrator implemented so far")
+        if integrator_Hankel is not trapezoidal_integrator:
+            raise NotImplementedError("only the trapezoidal radial integrator is implemented")
+        self.include_dispersion = include_dispersion
+        if include_dispersion:
+            self.dispersion_tables = dispersion_tables
+        self.include_absorption = include_absorption
+        if include_absorption:
+            self.absorption_tables = absorption_tables
+        self.effective_IR_refrective_index = effective_IR_refrective_index
+        self.integrator_Hankel = integrator_Hankel
+        self.integrator_longitudinal = integrator_longitudinal
+        self.near_field_factor = near_field_factor
+        self.rgrid = rgrid_FF
+        self.ogrid = np.copy(target.ogrid)
+        cum = store_cumulative_result or store_non_normalised_cumulative_result
+        if cum:
+            self.zgrid = np.copy(target.zgrid)
+        if not (((preset_gas + "_" + absorption_tables in XUV_index.gases) and
+                 (preset_gas + "_" + dispersion_tables in XUV_index.gases)) or (preset_gas == "vacuum")):
+            raise ValueError("Wrongly specified preset gas (or tables).")
+        if store_cumulative_result and isinstance(pressure, dict) and "rgrid" in pressure:
+            raise NotImplementedError("Renormalisation of the signal is not implemented for radially modulated density.")
+        pre, renorm = pre_factor_table(target.zgrid, target.ogrid, preset_gas, pressure, absorption_tables,
+                                       include_absorption, dispersion_tables, include_dispersion,
+                                       effective_IR_refrective_index)
+        z = np.asarray(target.zgrid, dtype=np.float64)
+        Nz = len(z)
+        if Nz < 2:
+            raise ValueError("Hankel_long needs at least two source planes")
+        want = set()
+        if store_entry_and_exit_plane_transform:
+            want |= {0, Nz - 1}
+        if cum:
+            want |= set(range(Nz))
+        ff, planes, plan = far_field(target.ogrid, target.rgrid, z, rgrid_FF, target.source, distance, pre,
+                                     near_field_factor, planes=sorted(want), form=form, tol=tol)
+        self.fast_plan = plan
+        conv = (lambda t: t.cpu().numpy()) if as_numpy else (lambda t: t)
+        self.FF_integrated = conv(ff)
+        if store_entry_and_exit_plane_transform:
+            self.entry_plane_transform = conv(planes[0])
+            self.exit_plane_transform = conv(planes[Nz - 1])
+        if cum:
+            P = torch.stack([planes[k] for k in range(Nz)])  # [Nz, Nrho, No]
+            dz = torch.as_tensor(np.diff(z), device=P.device, dtype=torch.float64)
+            contrib = 0.5 * dz[:, None, None] * (P[:-1] + P[1:])
+            run = torch.cumsum(contrib, dim=0)  # running z-trapezoid after planes 1..Nz-1
+            if store_cumulative_result:
+                rn = torch.as_tensor(renorm[:Nz - 1], device=P.device)
+                self.cumulative_field = conv(rn[:, None, :] * run)  # renorm_factor(k1), :668
+            if store_non_normalised_cumulative_result:
+                self.cumulative_field_no_norm = conv(run)
+
+
+def Signal_cum_integrator(ogrid, zgrid, FSourceTerm, integrator=None):
+    """Cumulative trapezoid of FSourceTerm[omega, z] along z (Hankel_transform.py:691-698)."""
+    z = torch.as_tensor(np.asarray(zgrid, dtype=np.float64), device="cuda")
+    F = torch.as_tensor(np.asarray(FSourceTerm), device="cuda").to(torch.complex128)
+    out = torch.zeros_like(F)
+    out[:, 1:] = torch.cumsum(0.5 * (z[1:] - z[:-1])[None, :] * (F[:, 1:] + F[:, :-1]), dim=1)
+    return out.cpu().numpy()

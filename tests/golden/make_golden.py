@@ -89,6 +89,8 @@ HANKEL_CASES = {
     "hankel_small": (6, 24, 5, 12, "Ar", True, True),
     "hankel_vacuum": (5, 20, 4, 10, "vacuum", True, False),
     "hankel_far_only": (4, 16, 4, 8, "Ar", False, True),
+    # config-3 geometry at reduced size: 512 -> 64 radii, 256 -> 17 planes, 2048 -> 12 frequencies
+    "hankel_config3_slice": (12, 64, 16, 32, "Ar", True, True),
 }
 
 
@@ -117,8 +119,9 @@ def make_hankel(ref_root):
     for name, (No, Nr, Nz, Nrho, gas, nff, cum) in HANKEL_CASES.items():
         zgrid, rgrid, ogrid, rho, S = hankel_inputs(No, Nr, Nz, Nrho)
         target = HT.FSources_provider(zgrid, rgrid, ogrid, data_source="static", FSource=S)
+        vac = gas == "vacuum"  # the reference has no tables for vacuum: both factors off
         res = HT.Hankel_long(target, 1.0, rho, preset_gas=gas, pressure=1.0, near_field_factor=nff,
-                             store_cumulative_result=cum)
+                             store_cumulative_result=cum, include_dispersion=not vac, include_absorption=not vac)
         out = dict(zgrid=zgrid, rgrid=rgrid, ogrid=ogrid, rho=rho, S=S, FF_integrated=res.FF_integrated,
                    entry=res.entry_plane_transform, exit=res.exit_plane_transform, distance=1.0,
                    gas=np.bytes_(gas), near_field=nff, n_xuv=np.array([1 - 1e-5, 1e-7]))

@@ -1,0 +1,93 @@
+"""Far field on the GPU against the reference (golden fixtures from Hankel_transform.py)
+and the oracle.
+
+Plain form (FP64, the reference's arithmetic): relative error <= 1e-10 of the largest
+value, per output.  Fast form (multiplication theorem, FP32): per-harmonic relative L2
+error over rho <= 2e-5 (the stated bound of the chosen form), planes <= 2e-5."""
+import glob
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FIX = sorted(glob.glob(os.path.join(GOLDEN, "hankel_*.npz")))
+FAST_TOL = 2e-5
+
+
+def per_harmonic(a, b):
+    """max over omega of ||a[:, w] - b[:, w]|| / ||b[:, w]|| (arrays [rho, omega])."""
+    return float(np.max(np.linalg.norm(a - b, axis=0) / np.linalg.norm(b, axis=0)))
+
+
+def _run(g, form):
+    from mma_gb300 import hankel as H
+
+    gas = g["gas"].item().decode() if isinstance(g["gas"].item(), bytes) else str(g["gas"])
+    H.XUV_index.set_constant_index(complex(g["n_xuv"][0], g["n_xuv"][1]))
+    target = H.FSources_provider(g["zgrid"], g["rgrid"], g["ogrid"], data_source="static", FSource=g["S"])
+    vac = gas == "vacuum"
+    return H.Hankel_long(target, float(g["distance"]), g["rho"], preset_gas=gas, pressure=1.0,
+                         near_field_factor=bool(g["near_field"]), store_cumulative_result="cumulative" in g,
+                         include_dispersion=not vac, include_absorption=not vac, form=form)
+
+
+@pytest.mark.parametrize("path", FIX, ids=[os.path.basename(p)[:-4] for p in FIX])
+def test_plain_matches_reference(gpu_lib, path):
+    g = np.load(path)
+    h = _run(g, "plain")
+    for key, attr in (("FF_integrated", "FF_integrated"), ("entry", "entry_plane_transform"),
+                      ("exit", "exit_plane_transform")):
+        ref = g[key]
+        assert np.abs(getattr(h, attr) - ref).max() < 1e-10 * np.abs(ref).max(), key
+    if "cumulative" in g:
+        assert np.abs(h.cumulative_field - g["cumulative"]).max() < 1e-10 * np.abs(g["cumulative"]).max()
+
+
+@pytest.mark.parametrize("path", FIX, ids=[os.path.basename(p)[:-4] for p in FIX])
+def test_fast_matches_reference(gpu_lib, path):
+    g = np.load(path)
+    h = _run(g, "fast")
+    err = per_harmonic(h.FF_integrated, g["FF_integrated"])
+    print(os.path.basename(path), "fast per-harmonic error %.2e, plan %s" % (err, h.fast_plan))
+    assert err < FAST_TOL
+    assert per_harmonic(h.entry_plane_transform, g["entry"]) < FAST_TOL
+    assert per_harmonic(h.exit_plane_transform, g["exit"]) < FAST_TOL
+
+
+def test_fast_vs_plain_config3_geometry(gpu_lib):
+    """Config-3 geometry (D = 1 m, z in [-5, 5] mm, r <= 200 um, rho <= 5 mm, harmonics
+    10-42 of 800 nm) at reduced sizes, many planes: fast against plain per harmonic."""
+    import sys
+
+    sys.path.insert(0, GOLDEN)
+    from make_golden import hankel_inputs
+    from mma_gb300 import hankel as H
+
+    H.XUV_index.set_constant_index(complex(1 - 1e-5, 1e-7))
+    zgrid, rgrid, ogrid, rho, S = hankel_inputs(24, 256, 64, 96, seed=3)
+    res = {}
+    for form in ("plain", "fast"):
+        t = H.FSources_provider(zgrid, rgrid, ogrid, FSource=S)
+        res[form] = H.Hankel_long(t, 1.0, rho, preset_gas="Ar", form=form)
+    err = per_harmonic(res["fast"].FF_integrated, res["plain"].FF_integrated)
+    print("config-3 geometry fast vs plain per-harmonic error %.2e plan %s" % (err, res["fast"].fast_plan))
+    assert err < FAST_TOL
+    assert res["fast"].fast_plan["trunc_bound"] < 1e-9
+
+
+def test_hankel_transform_single_plane(gpu_lib):
+    import oracle.hankel as oh
+    from mma_gb300 import hankel as H
+
+    rng = np.random.default_rng(5)
+    og = np.linspace(1e16, 8e16, 7)
+    rg = np.linspace(0, 150e-6, 40)
+    rho = np.linspace(0, 4e-3, 21)
+    F = (rng.standard_normal((7, 40)) + 1j * rng.standard_normal((7, 40))) * np.exp(-(rg / 60e-6) ** 2)
+    pre = np.outer(np.ones(40), np.exp(1j * np.linspace(0, 1, 7)))
+    got = H.HankelTransform(og, rg, F, 0.9, rho, pre_factor=pre)
+    ref = oh.hankel_plane(og, rg, F, 0.9, rho, pre_row=pre[0])
+    assert np.abs(got - ref).max() < 1e-11 * np.abs(ref).max()
