@@ -53,6 +53,207 @@ def focus_fields(n_r=64, n_z=32, n_cycles=10, E0=0.0534, dt=0.25, w0=100e-6, lam
     return t, fields
 
 
+def config3_inputs(device, n_r=512, n_z=256, n_omega=2048, n_rho=256, seed=0):
+    """Config-3 far-field inputs: r in [0, 200 um], z in [-5, 5] mm (the last plane is
+    dropped by the source provider, 255 planes integrate), omega in [10, 42] omega0 (800 nm),
+    rho in [0, 5 mm], D = 1 m; complex64 source exp(-r^2/(50 um)^2) x a comb of odd
+    harmonics 11..41 (Lorentzian width 0.3 omega0) with seeded random phases per plane,
+    built on the device (2.15 GB)."""
+    import torch
+
+    omega0 = OMEGA0 / 2.4188843265857e-17
+    rgrid = np.linspace(0.0, 200e-6, n_r)
+    zgrid = np.linspace(-5e-3, 5e-3, n_z)
+    ogrid = np.linspace(10 * omega0, 42 * omega0, n_omega)
+    rho = np.linspace(0.0, 5e-3, n_rho)
+    q = np.arange(11, 42, 2)
+    rng = np.random.default_rng(seed)
+    ph = rng.uniform(0, 2 * np.pi, size=(n_z, len(q)))
+    lor = 1.0 / (1.0 + ((ogrid[None, :] - q[:, None] * omega0) / (0.3 * omega0)) ** 2)
+    comb = torch.tensor(np.exp(1j * ph) @ lor, dtype=torch.complex64, device=device)  # [z, omega]
+    prof = torch.tensor(np.exp(-(rgrid / 50e-6) ** 2), dtype=torch.float32, device=device)
+    S = comb[:, :, None] * prof[None, None, :]
+    return zgrid, rgrid, ogrid, rho, S
+
+
+def config2_instances(n_inst=4096, seed=0, dt=0.25, dx=0.1):
+    """Uneven batch: x half-width ~ U[200, 600] a.u. (dx = 0.1), 6..20-cycle sin^2 pulses,
+    peak field log-uniform in [0.02, 0.075] a.u., CEP ~ U[0, 2 pi), seeded.  Each instance has
+    its own grid.  Fields start one sample after t = 0."""
+    rng = np.random.default_rng(seed)
+    half = rng.uniform(200.0, 600.0, n_inst)
+    cycles = rng.integers(6, 21, n_inst)
+    E0 = np.exp(rng.uniform(np.log(0.02), np.log(0.075), n_inst))
+    cep = rng.uniform(0.0, 2 * np.pi, n_inst)
+    params, fields = [], []
+    for i in range(n_inst):
+        params.append(dict(num_r=int(round(2 * half[i] / dx)), dx=dx, trg_a=A_CONFIG))
+        T = cycles[i] * 2 * np.pi / OMEGA0
+        n = int(T / dt)
+        n += n % 2
+        t = dt * np.arange(1, n + 1)
+        fields.append(E0[i] * np.sin(np.pi * t / T) ** 2 * np.cos(OMEGA0 * t + cep[i]))
+    return params, fields, E0
+
+
+def run_config2(args, device):
+    """The uneven batch in the complex64 form (one plan, five table widths) and in FP64;
+    throughput of both and the plateau (H11-H41) error of complex64 against FP64."""
+    import torch
+
+    from mma_gb300.tdse_batch import TDSEBatchPlan, TDSEGrids
+
+    n_inst = 4096 if args.workload == "config2" else 256
+    params, fields, E0 = config2_instances(n_inst)
+    t0 = time.perf_counter()
+    g64 = TDSEGrids(params, dt=0.25, c64=True)
+    torch.cuda.synchronize()
+    t_grids = time.perf_counter() - t0
+    tf = [torch.tensor(f, device=device) for f in fields]
+    out = {"instances": n_inst, "grid_build_s": t_grids, "site_steps": float(sum(
+        (p["num_r"] + 1) * (len(f) + 2) for p, f in zip(params, fields)))}
+    res = {}
+    for prec in ("c64", "fp64"):
+        plan = TDSEBatchPlan(g64, [len(f) for f in fields], 0.25, grid_ids=np.arange(n_inst), precision=prec)
+        plan.load_fields(tf)
+        plan.capture()
+        plan.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        plan.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) * 1e-3
+        out[prec] = {"seconds": sec, "site_steps_per_s": out["site_steps"] / sec,
+                     "launches": len(plan.launches)}
+        res[prec] = plan
+    # plateau error per instance (FP64 form = the oracle's arithmetic, checked by the tests)
+    errs = []
+    for i in range(n_inst):
+        a = res["c64"].result().spectrum(i)
+        b = res["fp64"].result().spectrum(i)
+        om = res["fp64"].result().omegagrid(i)
+        sel = (om >= 11 * OMEGA0) & (om <= 41 * OMEGA0)
+        pa, pb = a[sel].abs() ** 2, b[sel].abs() ** 2
+        errs.append(float(torch.linalg.norm(pa - pb) / torch.linalg.norm(pb)))
+    errs = np.array(errs)
+    out["c64_speedup_vs_fp64"] = out["fp64"]["seconds"] / out["c64"]["seconds"]
+    out["c64_plateau_rel_err"] = {"median": float(np.median(errs)), "p90": float(np.percentile(errs, 90)),
+                                  "max": float(errs.max()),
+                                  "median_E0_ge_0.04": float(np.median(errs[E0 >= 0.04]))}
+    return out
+
+
+HANKEL_FLOP_PER_TERM = 8.0  # one complex multiply-accumulate per (omega, plane, rho, r) term
+
+
+def run_hankel(args, device):
+    import torch
+
+    from mma_gb300 import hankel as H
+
+    H.XUV_index.set_constant_index(complex(1 - 1e-5, 1e-7))
+    zgrid, rgrid, ogrid, rho, S = config3_inputs(device, n_omega=WORKLOADS[args.workload][3])
+    target = H.FSources_provider(zgrid, rgrid, ogrid, FSource=S, device=device)
+    del S
+    z = target.zgrid
+    pre, _ = H.pre_factor_table(z, target.ogrid, "Ar", 1.0)
+    Nz, No, Nr = target.source.shape
+    terms = float(No) * Nz * len(rho) * Nr
+    stream = torch.cuda.current_stream()
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=device)
+
+    def run(form, planes=(0, -1)):
+        return H.far_field(target.ogrid, target.rgrid, z, rho, target.source, 1.0, pre, True, planes=planes,
+                           form=form)
+
+    out = {}
+    for _ in range(max(args.warmup, 3)):
+        run("fast")
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.add_(1.0)
+        ev[i][0].record(stream)
+        ff_fast, _, plan = run("fast")
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    t_fast = float(np.mean([a.elapsed_time(b) for a, b in ev])) * 1e-3
+    # plain FP64: one warm-up on a 32-frequency slice, then one timed full far field
+    sl = H.FSources_provider(np.append(z, z[-1] + (z[-1] - z[-2])), target.rgrid, target.ogrid[:32],
+                             FSource=target.source[:, :32].clone(), device=device)
+    H.far_field(sl.ogrid, sl.rgrid, sl.zgrid, rho, sl.source, 1.0, pre[:, :32], True, form="plain")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.add_(1.0)
+    e0.record(stream)
+    ff_plain, _, _ = run("plain")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = e0.elapsed_time(e1) * 1e-3
+    a = ff_fast.cpu().numpy()
+    b = ff_plain.cpu().numpy()
+    ph = np.linalg.norm(a - b, axis=0) / np.linalg.norm(b, axis=0)
+    # end to end through the public API: pinned host source in, host far field out
+    host_src = target.source.cpu().pin_memory()
+    host_ff = torch.empty(len(rho), No, dtype=torch.complex128).pin_memory()
+    e0.record(stream)
+    dsrc = host_src.to(device, non_blocking=True)
+    ffe, _, _ = H.far_field(target.ogrid, target.rgrid, z, rho, dsrc, 1.0, pre, True, planes=(0, -1), form="fast")
+    host_ff.copy_(ffe, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = e0.elapsed_time(e1) * 1e-3
+    out = {"workload": "config3: N_r=512, N_z=256 (255 planes integrated), N_omega=2048, N_rho=256, D=1 m, "
+                       "complex64 source, constant XUV index n=1-1e-5+1e-7i, near-field factor on",
+           "terms": terms, "flop_per_term": HANKEL_FLOP_PER_TERM,
+           "plain_fp64": {"seconds": t_plain, "tflops_algorithmic": HANKEL_FLOP_PER_TERM * terms / t_plain / 1e12},
+           "chosen_fast": {"seconds": t_fast, "tflops_algorithmic": HANKEL_FLOP_PER_TERM * terms / t_fast / 1e12,
+                           "speedup_vs_plain": t_plain / t_fast, "series_terms": plan["n_terms"],
+                           "truncation_bound": plan["trunc_bound"],
+                           "per_harmonic_rel_err_vs_plain": {"max": float(ph.max()), "median": float(np.median(ph))},
+                           "includes": "FF_integrated plus entry and exit plane transforms"},
+           "e2e_fast": {"seconds": t_e2e, "h2d_bytes": host_src.numel() * 8, "d2h_bytes": host_ff.numel() * 16,
+                        "tflops_algorithmic": HANKEL_FLOP_PER_TERM * terms / t_e2e / 1e12}}
+    return out
+
+
+def hankel_cpu_baseline(cores=None):
+    """The numpy restatement (oracle) on a slice of config 3 -- 16 frequencies x 9 source
+    planes (8 integrated) x 256 rho x 512 r -- split over frequencies on `cores` spawned
+    processes, extrapolated linearly in terms to the full far field."""
+    import multiprocessing as mp
+
+    cores = cores or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_hankel_slice, [(i, cores) for i in range(cores)])
+        wall = time.perf_counter() - t0
+    terms = sum(res)
+    full = 2048.0 * 255 * 256 * 512
+    rate = terms / wall
+    return {"value": HANKEL_FLOP_PER_TERM * rate / 1e12, "unit": "TFLOP/s (algorithmic)", "cores": cores,
+            "kind": "port", "seconds_full_extrapolated": full / rate,
+            "sample": "numpy restatement, %d frequencies x 8 planes x 256 rho x 512 r on %d processes, %.1f s; "
+                      "extrapolated linearly in terms to config 3" % (8 * cores, cores, wall)}
+
+
+def _hankel_slice(args):
+    i, n = args
+    import oracle.hankel as oh
+
+    omega0 = OMEGA0 / 2.4188843265857e-17
+    og = np.linspace(10 * omega0, 42 * omega0, 2048)[i::n][:8]
+    rg = np.linspace(0.0, 200e-6, 512)
+    rho = np.linspace(0.0, 5e-3, 256)
+    z = np.linspace(-5e-3, 5e-3, 256)[:10]
+    S = np.exp(-(rg / 50e-6) ** 2)[None, None, :] * np.ones((len(z), len(og), 1), dtype=np.complex64)
+    oh.hankel_long(z, rg, og, S, 1.0, rho)
+    return len(og) * (len(z) - 1) * 256 * 512
+
+
 # ---------------------------------------------------------------------------------- clocks
 class ClockSampler:
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -148,16 +349,25 @@ def l2_flush(buf):
     buf.add_(1.0)
 
 
+WORKLOADS = {
+    # name: (n_r, n_z, n_cycles, hankel n_omega)
+    "config1": (64, 32, 10, 2048),
+    "config2": (64, 32, 10, 2048),  # uneven batch (run_config2), reported on its own line
+    "small": (8, 19, 2, 128),  # profiling case: same grids, fewer instances, shorter pulses
+}
+
+
 def run_ours(args, rank, world, precision):
     import torch
 
     from mma_gb300 import load
-    from mma_gb300.tdse_batch import TDSEGrids, run_batch
+    from mma_gb300.tdse_batch import TDSEBatchPlan, TDSEGrids, run_batch
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     lib = load()
-    t, fields_np = focus_fields()
+    wr, wz, wc, _ = WORKLOADS[args.workload]
+    t, fields_np = focus_fields(n_r=wr, n_z=wz, n_cycles=wc)
     dtf = t[1] - t[0]
     tmax = t[-1] - t[0]
     n_inst = fields_np.shape[0]
@@ -165,14 +375,19 @@ def run_ours(args, rank, world, precision):
     grids = TDSEGrids([dict(num_r=8000, dx=0.1, trg_a=A_CONFIG)], dt=dtf, c64=(precision == "c64"))
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
     stream = torch.cuda.current_stream()
+    plan = TDSEBatchPlan(grids, [fields.shape[1]] * n_inst, dtf, tmax=tmax, precision=precision)
+    plan.load_fields(fields)
+    plan.check_fields()
+    plan.capture()  # the whole batch (interpolation, propagation, spectra) as one CUDA graph
 
     def step():
-        return run_batch(grids, fields, dt_field=dtf, tmax=tmax, precision=precision)
+        plan.replay()
+        return plan.result()
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    S = int(step()["S"][0])
+    S = int(plan.S[0])
     sites = 8001
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if world > 1:
@@ -201,7 +416,7 @@ def run_ours(args, rank, world, precision):
     kms = []
     for _ in range(2):
         l2_flush(flush)
-        r = run_batch(grids, fields, dt_field=dtf, tmax=tmax, spectra=False, _events=kev, precision=precision)
+        plan.launch(_events=kev)
         torch.cuda.synchronize()
         kms.append(kev[0].elapsed_time(kev[1]))
     k_ms = float(np.mean(kms))
@@ -215,9 +430,9 @@ def run_ours(args, rank, world, precision):
     for _ in range(max(1, min(args.steps, 2))):
         l2_flush(flush)
         e2e_ev[0].record(stream)
-        f_dev = host_fields.to(dev, non_blocking=True)
-        rr = run_batch(grids, f_dev, dt_field=dtf, tmax=tmax, precision=precision)
-        host_out.copy_(rr["Fsourceterm"], non_blocking=True)
+        plan.load_fields(host_fields)  # host -> device copy of this step's fields
+        plan.replay()
+        host_out.copy_(plan.result()["Fsourceterm"], non_blocking=True)
         e2e_ev[1].record(stream)
         torch.cuda.synchronize()
         e_ms.append(e2e_ev[0].elapsed_time(e2e_ev[1]))
@@ -273,6 +488,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-hankel", action="store_true")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config1")
+    ap.add_argument("--forms", choices=["both", "fp64", "c64"], default="both")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -302,6 +520,13 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
+    if args.workload == "config2":
+        import torch
+
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+        torch.cuda.set_device(dev)
+        print(json.dumps({"workload": "config2", "result": run_config2(args, dev)}))
+        return
     r64 = run_ours(args, rank, world, "fp64")
     r = run_ours(args, rank, world, "c64")
     if rank != 0:
@@ -330,8 +555,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64 (fp32 propagation, fp64 factorisation/accumulation)",
             "data": "synthetic",
-            "config": {"workload": "config1: 2048 TDSE instances (64 r x 32 z Gaussian focus), 8001 sites, "
-                                   "%d steps; chosen form = complex64 propagation" % r["S"],
+            "config": {"workload": "%s: %d TDSE instances (%d r x %d z Gaussian focus), 8001 sites, "
+                                   "%d steps; chosen form = complex64 propagation"
+                                   % (args.workload, r["n_inst"], WORKLOADS[args.workload][0],
+                                      WORKLOADS[args.workload][1], r["S"]),
                        "instances": r["n_inst"], "sites": 8001, "steps_per_instance": r["S"],
                        "l2": "flushed between steps (256 MB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -339,8 +566,14 @@ def main():
             "e2e": {"value": world * site_steps / (r["e2e_ms"] * 1e-3), "unit": "site-steps/s",
                     "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
             "gpu_launches": 3 * args.steps}
+    if not args.no_hankel:
+        import torch
+
+        line["hankel"] = run_hankel(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(r["t"], r["fields"], os.cpu_count() or 1)
+        if not args.no_hankel:
+            line["hankel"]["cpu_baseline"] = hankel_cpu_baseline()
     print(json.dumps(line))
 
 

@@ -3,13 +3,15 @@
 // Same Crank-Nicolson-Numerov step and the same partitioned solve as the FP64 kernel
 // (tdse_kernels.cu, tdse_solver.cuh), with:
 //   * the factorisation computed in FP64 (build_grids_kernel) and rounded once to FP32;
-//   * the wavefunction, the sweeps and the chunk products in FP32 registers: each of the
-//     256 threads keeps its M <= 32 sites of psi, of the local sweep and of the running
-//     chunk products (F forward, then G backward) in registers for the whole pulse;
-//   * the per-site tables in shared memory, 20 bytes per site: 1/beta (complex), the
-//     off-diagonal factor w_j = dt/2 (-1/(2dx^2) + V_j/12) from which h_j = 6 a_j /beta_j and
-//     g_j = 6 c_j /beta_j are re-derived (a_j = 1/12 + i w_{j-1}, c_j = 1/12 + i w_{j+1}), -V'
-//     and the (real) ground state -- nothing per step goes to L2 but the four observables;
+//   * the wavefunction and the sweep in FP32 registers: each of the 256 threads keeps its
+//     M <= 48 sites of psi and of the sweep in registers for the whole pulse.  Instead of
+//     storing the chunk products of the partitioned solve, each sweep is run twice: once
+//     from zero to get the chunk-boundary carry for the CTA scan, once from the exact carry
+//     (five passes per step, registers 4M floats);
+//   * the per-site tables in shared memory, 16 bytes per site: 1/beta (complex), V_j and the
+//     (real) ground state.  h_j = 6 a_j/beta_j and g_j = 6 c_j/beta_j are re-derived from
+//     1/beta and w_q = dt/2 (-1/(2dx^2) + V_q/12) (a_j = 1/12 + i w_{j-1}, c_j = 1/12 + i w_{j+1}),
+//     and -V'_j = -x_j V_j^3 -- nothing per step goes to L2 but the four observables;
 //   * the phase e^{+i E dt x}: the chunk-start angle is formed and reduced mod 2 pi in
 //     float-float arithmetic, then e^{i E dt dx i} per site from a 32-entry table;
 //   * the observables summed per thread with Kahan compensation, across the warp with
@@ -49,7 +51,7 @@ __device__ __forceinline__ cf shdn(cf v, int d)
 }
 
 // Table slots (floats), each L = 256*M long, site j = t*M + i at q = i*256 + t.
-enum { T_IBRE = 0, T_IBIM, T_W, T_GV, T_PSI0, T_SLOTS };
+enum { T_IBRE = 0, T_IBIM, T_V, T_PSI0, T_SLOTS };
 
 // forward scan of Y_t = b_t + c_t Y_{t-1} over the CTA, exclusive (see tdse_solver.cuh)
 __device__ __forceinline__ cf scan_fwd(cf c, cf b, cf* sc, cf* sb)
@@ -180,20 +182,23 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
         }
         const float* ibre = tab + T_IBRE * L;
         const float* ibim = tab + T_IBIM * L;
-        const float* ww = tab + T_W * L;
-        const float* gv = tab + T_GV * L;
+        const float* vv = tab + T_V * L;
         const float* p0 = tab + T_PSI0 * L;
         // ---- state: psi in registers, initialised from the ground state
-        cf psi[M], yl[M], fg[M];
+        cf psi[M], yy[M];
         const int64_t s0 = (int64_t)t * M;
 #pragma unroll
         for (int i = 0; i < M; i++) psi[i] = cf{p0[i * kThreads + t], 0.f};
-        // chunk start x as a float-float pair (phase angle) and as a float (<x>)
+        // chunk start x as a float-float pair (phase angle) and as a float (<x>, -V')
         const double xs_d = (s0 < n) ? G.x[s0] : 0.0;
         const float xs_hi = (float)xs_d, xs_lo = (float)(xs_d - (double)xs_hi);
         const float dxf = (float)G.dx;
         const double dt = G.dt;
-        const float w6 = 6.0f;
+        // 6 w_q = 6 dt/2 (-1/(2 dx^2)) + (dt/4) V_q.  The constant is carried as a float-float
+        // pair (c_hi + c_lo): rounded once to float it would be the same error at every site,
+        // a slightly different kinetic scale whose phase error grows step after step.
+        const double c6 = 6.0 * 0.5 * dt * (-0.5 / (G.dx * G.dx));
+        const float c_hi = (float)c6, c_lo = (float)(c6 - (double)c_hi), c1 = (float)(0.25 * dt);
         if (lane == 0) bfirst[w] = psi[0];
         if (lane == 31) blast[w] = psi[M - 1];
         __syncthreads();
@@ -217,6 +222,24 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             }
         }
         double tt = I.tmin;
+        // h_j and g_j of site (i, t): 6 a_j /beta_j and 6 c_j /beta_j (zero at the grid ends)
+        // (1/2 + i 6 w) * ib with 6 w = c_hi + (c_lo + c1 V) kept unsummed
+        auto off_diag = [&](float v, float ir, float ii) -> cf {
+            const float t1 = fmaf(c1, v, c_lo);
+            return cf{fmaf(-t1, ii, fmaf(-c_hi, ii, 0.5f * ir)), fmaf(t1, ir, fmaf(c_hi, ir, 0.5f * ii))};
+        };
+        auto h_at = [&](int i) -> cf {
+            const int q = i * kThreads + t;
+            const float vl = (i == 0) ? ((t == 0) ? 0.f : vv[(M - 1) * kThreads + t - 1]) : vv[q - kThreads];
+            const cf r = off_diag(vl, ibre[q], ibim[q]);
+            return (s0 + i == 0) ? cf{0.f, 0.f} : r;
+        };
+        auto g_at = [&](int i) -> cf {
+            const int q = i * kThreads + t;
+            const float vr = (i == M - 1) ? ((t == kThreads - 1) ? 0.f : vv[t + 1]) : vv[q + kThreads];
+            const cf r = off_diag(vr, ibre[q], ibim[q]);
+            return (s0 + i >= n - 1) ? cf{0.f, 0.f} : r;
+        };
 
         for (int64_t k = 0; k < S; k++) {
             // FP64 work of a step is spread over three warps so that no single warp holds the
@@ -249,10 +272,10 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
                 o_e[k + 1] = Fk;
             }
             if (w == kWarps - 1) {
-                if (lane < M) {  // per-site phase factors e^{i F dt dx i}, i < M
+                for (int i = lane; i < M; i += 32) {  // per-site phase factors e^{i F dt dx i}, i < M
                     float sn, cs;
-                    sincosf((float)(Fk * dt * G.dx) * (float)lane, &sn, &cs);
-                    wtab[lane] = cf{cs, sn};
+                    sincosf((float)(Fk * dt * G.dx) * (float)i, &sn, &cs);
+                    wtab[i] = cf{cs, sn};
                 }
                 if (lane == 31) {
                     const double fdt = Fk * dt;
@@ -261,10 +284,11 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
                     s_alo = (float)(fdt - (double)a_hi);
                 }
             }
-            // ---- pass 1: right-hand side 2 M2 psi, local forward sweep, forward products F
+            // right-hand side 2 M2 psi at site i (neighbours across threads by shuffle/shared)
             cf left = shup(psi[M - 1], 1), right = shdn(psi[0], 1);
             if (lane == 0) left = (w == 0) ? cf{0.f, 0.f} : blast[w - 1];
             if (lane == 31) right = (w == kWarps - 1) ? cf{0.f, 0.f} : bfirst[w + 1];
+            // ---- pass 1: local forward sweep from zero: chunk-end value and product of (-h)
             cf yprev{0.f, 0.f}, Fp{1.f, 0.f};
 #pragma unroll
             for (int i = 0; i < M; i++) {
@@ -272,36 +296,37 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
                 const cf pm = (i == 0) ? left : psi[i - 1];
                 const cf pn = (i == M - 1) ? right : psi[i + 1];
                 const cf r{fmaf(10.f, psi[i].re, pm.re + pn.re), fmaf(10.f, psi[i].im, pm.im + pn.im)};
-                const cf ib{ibre[q], ibim[q]};
-                // a_j = 1/12 + i w_{j-1}; h_j = a_j / beta_j = (6 a_j) (ib/6)
-                const float wl = (i == 0) ? ((t == 0) ? 0.f : ww[(M - 1) * kThreads + t - 1]) : ww[q - kThreads];
-                cf h = cmul(cf{0.5f, w6 * wl}, ib);
-                if (s0 + i == 0) h = cf{0.f, 0.f};
-                const cf y = cfms(h, yprev, cmul(ib, r));
-                yl[i] = y;
-                yprev = y;
+                const cf h = h_at(i);
+                yprev = cfms(h, yprev, cmul(cf{ibre[q], ibim[q]}, r));
                 Fp = cmul(Fp, cf{-h.re, -h.im});
-                fg[i] = Fp;
             }
-            const cf yin = scan_fwd(fg[M - 1], yprev, sc, sb);
-            // ---- pass 2: forward correction, local backward sweep, backward products G
+            cf yc = scan_fwd(Fp, yprev, sc, sb);  // exact y at the end of the previous chunk
+            // ---- pass 2: forward sweep again from the exact carry, kept in registers
+#pragma unroll
+            for (int i = 0; i < M; i++) {
+                const int q = i * kThreads + t;
+                const cf pm = (i == 0) ? left : psi[i - 1];
+                const cf pn = (i == M - 1) ? right : psi[i + 1];
+                const cf r{fmaf(10.f, psi[i].re, pm.re + pn.re), fmaf(10.f, psi[i].im, pm.im + pn.im)};
+                yc = cfms(h_at(i), yc, cmul(cf{ibre[q], ibim[q]}, r));
+                yy[i] = yc;
+            }
+            // ---- pass 3: local backward sweep from zero: chunk-start value and product of (-g)
             cf unext{0.f, 0.f}, Gp{1.f, 0.f};
 #pragma unroll
             for (int i = M - 1; i >= 0; i--) {
-                const int q = i * kThreads + t;
-                const cf y = cfma(fg[i], yin, yl[i]);
-                const cf ib{ibre[q], ibim[q]};
-                const float wr = (i == M - 1) ? ((t == kThreads - 1) ? 0.f : ww[t + 1]) : ww[q + kThreads];
-                cf g = cmul(cf{0.5f, w6 * wr}, ib);
-                if (s0 + i >= n - 1) g = cf{0.f, 0.f};
-                const cf u = cfms(g, unext, y);
-                yl[i] = u;
-                unext = u;
+                const cf g = g_at(i);
+                unext = cfms(g, unext, yy[i]);
                 Gp = cmul(Gp, cf{-g.re, -g.im});
-                fg[i] = Gp;
             }
-            const cf uin = scan_bwd(fg[0], unext, sc + kWarps, sb + kWarps);
-            // ---- pass 3: backward correction, CN update, phase, observables
+            cf uc = scan_bwd(Gp, unext, sc + kWarps, sb + kWarps);  // exact u at the start of the next chunk
+            // ---- pass 4: backward sweep again from the exact carry
+#pragma unroll
+            for (int i = M - 1; i >= 0; i--) {
+                uc = cfms(g_at(i), uc, yy[i]);
+                yy[i] = uc;
+            }
+            // ---- pass 5: CN update, phase, observables
             // chunk-start angle F dt x_s in float-float, reduced mod 2 pi
             const float a_hi = s_ahi, a_lo = s_alo;
             float th_hi = a_hi * xs_hi;
@@ -321,14 +346,15 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             for (int i = 0; i < M; i++) {
                 const int q = i * kThreads + t;
                 const int64_t j = s0 + i;
-                const cf u = cfma(fg[i], uin, yl[i]);
-                const cf d = u - psi[i];
+                const cf d = yy[i] - psi[i];
                 const cf ph = cmul(phs, wtab[i]);
                 const cf pn = cmul(ph, d);
                 psi[i] = pn;
                 const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
-                const float xj = xs_hi + dxf * (float)i;
-                const float terms[4] = {n2 * gv[q], n2 * xj, pn.re * p0[q], -pn.im * p0[q]};
+                const float xj = fmaf(dxf, (float)i, xs_hi);
+                const float vj = vv[q];
+                const float gvj = -xj * vj * vj * vj;  // -V' = x (a^2+x^2)^-3/2 = -x V^3
+                const float terms[4] = {n2 * gvj, n2 * xj, pn.re * p0[q], -pn.im * p0[q]};
 #pragma unroll
                 for (int c = 0; c < 4; c++) {  // Kahan
                     const float y = terms[c] - acc_c[c];
@@ -427,18 +453,16 @@ __global__ void __launch_bounds__(kThreads) build_c64_kernel(const mma_tdse_grid
     const mma_tdse_grid G = grids[blockIdx.x];
     const int64_t n = G.n, m = G.m, Lm = m * kThreads, M = G.m32, L = M * kThreads;
     const cd* ctab = reinterpret_cast<const cd*>(G.cn_tab);
-    const double hdt = 0.5 * G.dt;
     for (int64_t q = threadIdx.x; q < L; q += kThreads) {
         const int64_t i = q / kThreads, t = q % kThreads, j = t * M + i;
-        float v[T_SLOTS] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        float v[T_SLOTS] = {0.f, 0.f, 0.f, 0.f};
         if (j < n) {
             const int64_t q64 = (j % m) * kThreads + j / m;  // FP64 table layout
             const cd ib6 = ctab[0 * Lm + q64];
             const double vj = -1.0 / sqrt(G.trg_a * G.trg_a + G.x[j] * G.x[j]);
             v[T_IBRE] = (float)ib6.re;
             v[T_IBIM] = (float)ib6.im;
-            v[T_W] = (float)(hdt * (-0.5 / (G.dx * G.dx)) + hdt * 1 / 12. * vj);
-            v[T_GV] = (float)G.gv[j];
+            v[T_V] = (float)vj;
             v[T_PSI0] = (float)G.psi0[2 * j];
         }
 #pragma unroll
@@ -457,7 +481,7 @@ extern "C" int mma_tdse_build_c64_tables(const mma_tdse_grid* grids_dev, const m
     if (n_grids <= 0 || !grids_dev || !grids_host) return MMA_ERR_ARG;
     for (int g = 0; g < n_grids; g++) {
         const mma_tdse_grid& G = grids_host[g];
-        if (!G.c64_tab || G.m32 < G.m || G.m32 > 32 || G.m32 % 8 != 0 || G.m32 * kThreads < G.n) return MMA_ERR_ARG;
+        if (!G.c64_tab || G.m32 < G.m || G.m32 > 48 || G.m32 % 8 != 0 || G.m32 * kThreads < G.n) return MMA_ERR_ARG;
     }
     c64::build_c64_kernel<<<n_grids, kThreads, 0, (cudaStream_t)stream>>>(grids_dev);
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
@@ -486,6 +510,8 @@ extern "C" int mma_tdse_propagate_c64_impl(const mma_tdse_instance* insts, int n
         case 16: return launch_c64<16>(A, grid_ctas, st);
         case 24: return launch_c64<24>(A, grid_ctas, st);
         case 32: return launch_c64<32>(A, grid_ctas, st);
+        case 40: return launch_c64<40>(A, grid_ctas, st);
+        case 48: return launch_c64<48>(A, grid_ctas, st);
         default: return MMA_ERR_TOO_LARGE;
     }
 }

@@ -229,6 +229,12 @@ __global__ void __launch_bounds__(kThreads) build_grids_kernel(const mma_tdse_gr
         const double xmax = __dmul_rn(__dmul_rn(0.5, (double)num_r), dx);
         for (int64_t j = t; j < n; j += kThreads) G.x[j] = __dsub_rn(__dmul_rn((double)j, dx), xmax);
         __syncthreads();
+    }
+    // V_j into gv[] for the factorisations (gv receives -V' at the end)
+    for (int64_t j = t; j < n; j += kThreads) G.gv[j] = soft_coulomb(G.x[j], a);
+    __syncthreads();
+    const double* V = G.gv;
+    if (mode == 0) {
         // ground-state tables (tridiag.c:101-115)
         double* gtab = G.gs_tab;
         for (int64_t q = t; q < GS_SLOTS * L; q += kThreads) gtab[q] = 0.0;
@@ -236,10 +242,10 @@ __global__ void __launch_bounds__(kThreads) build_grids_kernel(const mma_tdse_gr
         if (t == 0) {
             const double E = G.Eguess, k0 = -0.5 / (dx * dx), d0 = 1.0 / (dx * dx);
             auto row = [&](int64_t j, double& aj, double& bj, double& cj) {
-                double vj = soft_coulomb(G.x[j], a);
-                aj = (j > 0) ? k0 - E / 12.0 + soft_coulomb(G.x[j - 1], a) / 12.0 : 0.0;
+                const double vj = V[j];
+                aj = (j > 0) ? k0 - E / 12.0 + V[j - 1] / 12.0 : 0.0;
                 bj = 10.0 * vj / 12.0 + d0 - 10.0 * E / 12.0;
-                cj = (j + 1 < n) ? k0 - E / 12.0 + soft_coulomb(G.x[j + 1], a) / 12.0 : 0.0;
+                cj = (j + 1 < n) ? k0 - E / 12.0 + V[j + 1] / 12.0 : 0.0;
             };
             factorise<double>(n, m, gtab + GS_IB12 * L, gtab + GS_H * L, gtab + GS_G * L, 1.0 / 12.0, row);
         }
@@ -251,8 +257,6 @@ __global__ void __launch_bounds__(kThreads) build_grids_kernel(const mma_tdse_gr
         ground_state(G, gtab, work, work + L, work + 2 * L, red, sc, sb, G.psi0);
         __syncthreads();
     }
-    for (int64_t j = t; j < n; j += kThreads) G.gv[j] = minus_grad_v(G.x[j], a);
-    __syncthreads();
     // Crank-Nicolson tables (prop.c:138-159): row j sub (1/12, w_{j-1}), diag (10/12, d_j),
     // super (1/12, w_{j+1}); w_q = dt/2 (-1/(2dx^2) + V_q/12), d_q = dt/2 (1/dx^2 + 10 V_q/12).
     // The right-hand side is 2 M2 psi = (psi_{j-1} + 10 psi_j + psi_{j+1})/6 and the new state
@@ -263,17 +267,18 @@ __global__ void __launch_bounds__(kThreads) build_grids_kernel(const mma_tdse_gr
     if (t == 0) {
         const double hdt = 0.5 * dt;
         auto row = [&](int64_t j, cd& aj, cd& bj, cd& cj) {
-            double vj = soft_coulomb(G.x[j], a);
-            aj = (j > 0) ? cd{1.0 / 12.0, hdt * (-0.5 / (dx * dx)) + hdt * 1 / 12. * soft_coulomb(G.x[j - 1], a)}
-                         : cd{0.0, 0.0};
+            const double vj = V[j];
+            aj = (j > 0) ? cd{1.0 / 12.0, hdt * (-0.5 / (dx * dx)) + hdt * 1 / 12. * V[j - 1]} : cd{0.0, 0.0};
             bj = cd{10.0 / 12.0, hdt * (1.0 / (dx * dx)) + hdt * 10 / 12. * vj};
-            cj = (j + 1 < n) ? cd{1.0 / 12.0, hdt * (-0.5 / (dx * dx)) + hdt * 1 / 12. * soft_coulomb(G.x[j + 1], a)}
-                             : cd{0.0, 0.0};
+            cj = (j + 1 < n) ? cd{1.0 / 12.0, hdt * (-0.5 / (dx * dx)) + hdt * 1 / 12. * V[j + 1]} : cd{0.0, 0.0};
         };
         factorise<cd>(n, m, ctab + CN_IB6 * L, ctab + CN_H * L, ctab + CN_G * L, 1.0 / 6.0, row);
     }
     __syncthreads();
     chunk_products<cd>(m, ctab + CN_H * L, ctab + CN_G * L, ctab + CN_F * L, ctab + CN_GG * L);
+    __syncthreads();
+    for (int64_t j = t; j < n; j += kThreads) G.gv[j] = minus_grad_v(G.x[j], a);
+    __syncthreads();
     for (int64_t i = 0; i < m; i++) {
         int64_t j = t * m + i, q = i * kThreads + t;
         if (j < n) {

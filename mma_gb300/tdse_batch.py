@@ -156,8 +156,8 @@ class TDSEGrids:
         self.m32 = np.array([((m + 7) // 8) * 8 for m in self.m])
         self.c64 = bool(c64)
         if self.c64:
-            if self.m32.max() > 32:
-                raise ValueError("the complex64 form takes grids of at most 8192 sites")
+            if self.m32.max() > 48:
+                raise ValueError("the complex64 form takes grids of at most 12288 sites")
             c_sizes = C64_SLOTS * THREADS * self.m32
             self.c64_buf = torch.zeros(int(c_sizes.sum()), dtype=torch.float32, device=self.device)
             c_off = np.concatenate([[0], np.cumsum(c_sizes)])[:-1]
@@ -201,128 +201,273 @@ class TDSEGrids:
 
 
 class BatchResult(dict):
-    """Packed outputs of a batch; ``series(i)`` gives instance i's six series."""
+    """Outputs of a batch.  ``series(i)`` gives instance i's six series, ``spectrum(i)``
+    its source-term spectrum; uniform batches also carry [n_inst, ...] views."""
 
     def series(self, i):
         o, S = self["out_off"][i], self["S"][i]
         blk = self["outputs"][o:o + 6 * (S + 1)].view(6, S + 1)
         return {k: blk[s, :S] for s, k in enumerate(("tgrid", "Efield", "sourceterm", "PopTot", "PopInt", "expval"))}
 
+    def spectrum(self, i):
+        g, row = self["spec_index"][i]
+        return self["spec_groups"][g]["F"][row]
+
+    def omegagrid(self, i):
+        g, _ = self["spec_index"][i]
+        return self["spec_groups"][g]["omega"]
+
+
+SERIES = ("tgrid", "Efield", "sourceterm", "PopTot", "PopInt", "expval")
+
+
+class TDSEBatchPlan:
+    """A batch of TDSE instances with every device buffer allocated once.
+
+    ``launch()`` issues the whole device pipeline -- Fourier interpolation of the
+    fields (one cuFFT batch per field length), the persistent propagation kernel
+    (one launch per kernel shape: all FP64 instances together, complex64 instances
+    per table width), the output spectra (one batch per series length) -- on one
+    stream, with no host synchronisation, so ``capture()`` can record it as a CUDA
+    graph and ``replay()`` re-runs it on new fields written by ``load_fields``.
+
+    Instances are laid out in the outputs grouped by series length (each group is one
+    strided spectrum batch) and handed to the device work queue longest first (the
+    cost of an instance is sites x steps), which balances uneven batches.
+    """
+
+    def __init__(self, grids, n_field, dt_field, grid_ids=None, dt_req=None, tmin=0.0, precision="fp64",
+                 spectra=True, psi_final=False, snap_every=0, tmax=None, grid_ctas=0):
+        lib = _sig()
+        self.lib = lib
+        if precision not in PRECISIONS:
+            raise ValueError("precision must be one of %s" % list(PRECISIONS))
+        self.grids = grids
+        dev = grids.device
+        self.device = dev
+        nf = np.atleast_1d(np.asarray(n_field, dtype=np.int64))
+        n_inst = len(nf)
+        if n_inst == 0:
+            raise ValueError("empty batch")
+        if nf.min() < 2:
+            raise ValueError("every field needs at least 2 samples")
+        self.n_inst, self.nf = n_inst, nf
+        k1, dt = refine(dt_field, dt_req if dt_req is not None else grids.dt)
+        if abs(dt - grids.dt) > 1e-12 * grids.dt:
+            raise ValueError("grids were built for dt=%g but this batch refines to dt=%g" % (grids.dt, dt))
+        self.k1, self.dt, self.dt_field = k1, dt, dt_field
+        gid = np.zeros(n_inst, dtype=np.int64) if grid_ids is None else np.asarray(grid_ids, dtype=np.int64)
+        if gid.shape != (n_inst,) or gid.min() < 0 or gid.max() >= len(grids):
+            raise ValueError("grid_ids must index the grids")
+        self.gid = gid
+        S = n_steps(nf, k1)
+        self.S = S
+        self.prec = PRECISIONS[precision]
+        if self.prec == 1 and not grids.c64:
+            raise ValueError("build the grids with c64=True for the complex64 form")
+        # raw and refined field buffers, grouped by raw length
+        self.len_groups = []
+        raw_total = 0
+        fld_off = np.zeros(n_inst, dtype=np.int64)
+        off = 0
+        for L in np.unique(nf):
+            idx = np.nonzero(nf == L)[0]
+            self.len_groups.append((int(L), idx, raw_total, off))
+            for j, i in enumerate(idx):
+                fld_off[i] = off + j * k1 * int(L)
+            raw_total += len(idx) * int(L)
+            off += len(idx) * k1 * int(L)
+        self.raw = torch.zeros(raw_total, dtype=torch.float64, device=dev)
+        self.fld = torch.zeros(off, dtype=torch.float64, device=dev)
+        # output layout grouped by series length
+        out_off = np.zeros(n_inst, dtype=np.int64)
+        self.s_groups = []
+        off = 0
+        for s_len in np.unique(S):
+            idx = np.nonzero(S == s_len)[0]
+            self.s_groups.append((int(s_len), idx, off))
+            for j, i in enumerate(idx):
+                out_off[i] = off + j * 6 * (int(s_len) + 1)
+            off += len(idx) * 6 * (int(s_len) + 1)
+        self.out_off = out_off
+        self.outputs = torch.zeros(off, dtype=torch.float64, device=dev)
+        self.psi_off = np.full(n_inst, -1, dtype=np.int64)
+        self.psi_buf = None
+        if psi_final:
+            sizes = 2 * grids.n[gid]
+            self.psi_off = np.concatenate([[0], np.cumsum(sizes)])[:-1]
+            self.psi_buf = torch.zeros(int(sizes.sum()), dtype=torch.float64, device=dev)
+        self.snap_off = np.full(n_inst, -1, dtype=np.int64)
+        self.n_snap = np.zeros(n_inst, dtype=np.int64)
+        self.snap_buf = None
+        if snap_every:
+            self.n_snap = S // snap_every
+            sizes = self.n_snap * 2 * grids.n[gid]
+            self.snap_off = np.concatenate([[0], np.cumsum(sizes)])[:-1]
+            self.snap_buf = torch.zeros(int(sizes.sum()), dtype=torch.float64, device=dev)
+        self.gate_floor = np.zeros(n_inst)
+        recs = (InstRec * n_inst)()
+        for i in range(n_inst):
+            r = recs[i]
+            r.grid, r.n_steps, r.field_off, r.n_field = int(gid[i]), int(S[i]), int(fld_off[i]), int(k1 * nf[i])
+            r.out_off, r.psi_off, r.snap_off = int(out_off[i]), int(self.psi_off[i]), int(self.snap_off[i])
+            r.snap_every, r.n_snap = max(int(snap_every), 1), int(self.n_snap[i]) if snap_every else 0
+            r.tmin, r.gate_floor = float(tmin), 0.0
+        self.recs = recs
+        # propagation launches: instances split by kernel shape, longest first within each
+        cost = grids.n[gid].astype(np.float64) * S
+        if self.prec == 1:
+            shapes = grids.m32[gid]
+        else:
+            shapes = np.zeros(n_inst, dtype=np.int64)
+        self.launches = []
+        for shape in sorted(np.unique(shapes), reverse=True):
+            idx = np.nonzero(shapes == shape)[0]
+            idx = idx[np.argsort(-cost[idx], kind="stable")]
+            max_m = int(shape) if self.prec == 1 else int(grids.m[np.unique(gid[idx])].max())
+            ctas = grid_ctas or lib.mma_tdse_default_ctas(max_m, self.prec)
+            ctas = min(ctas, len(idx))
+            sb = int(lib.mma_tdse_scratch_bytes(max_m, ctas, self.prec))
+            self.launches.append(dict(idx=idx, max_m=max_m, ctas=ctas,
+                                      scratch=torch.empty(max(sb, 8), dtype=torch.uint8, device=dev), sbytes=sb,
+                                      counter=torch.zeros(1, dtype=torch.int32, device=dev)))
+        self._upload_records()
+        # spectra buffers per series length (rows are the instances of the group)
+        self.spectra = spectra
+        self.spec_groups = []
+        self.spec_index = {}
+        if spectra:
+            for g, (s_len, idx, off) in enumerate(self.s_groups):
+                nc = s_len // 2 + 1
+                tm = tmax if tmax is not None else (int(nf[idx[0]]) - 1) * dt_field
+                fs = torch.zeros(len(idx), 2 * nc, dtype=torch.float64, device=dev)
+                self.spec_groups.append(dict(s=s_len, idx=idx, off=off, tmax=tm, fs=fs,
+                                             fm=torch.zeros(len(idx), nc, dtype=torch.float64, device=dev),
+                                             omega=torch.zeros(nc, dtype=torch.float64, device=dev),
+                                             F=torch.view_as_complex(fs.view(len(idx), nc, 2))))
+                for row, i in enumerate(idx):
+                    self.spec_index[int(i)] = (g, row)
+        self.graph = None
+
+    def _upload_records(self):
+        for L in self.launches:
+            sub = (InstRec * len(L["idx"]))(*[self.recs[i] for i in L["idx"]])
+            L["d_insts"] = torch.frombuffer(bytearray(bytes(sub)), dtype=torch.uint8).to(self.device)
+
+    def load_fields(self, fields):
+        """Copy the raw fields (a [n_inst, n_f] tensor or a list of 1-D tensors) into the
+        plan's device buffer (on the current stream; no host synchronisation)."""
+        rows = [fields[i] for i in range(fields.shape[0])] if torch.is_tensor(fields) and fields.dim() == 2 \
+            else list(fields)
+        if len(rows) != self.n_inst:
+            raise ValueError("expected %d fields" % self.n_inst)
+        for L, idx, raw_off, _ in self.len_groups:
+            dst = self.raw[raw_off:raw_off + len(idx) * L].view(len(idx), L)
+            if torch.is_tensor(fields) and fields.dim() == 2:
+                dst.copy_(fields[torch.as_tensor(idx, device=fields.device)].to(torch.float64), non_blocking=True)
+            else:
+                for j, i in enumerate(idx):
+                    if rows[i].numel() != L:
+                        raise ValueError("field %d has the wrong length" % i)
+                    dst[j].copy_(rows[i].to(self.device, torch.float64), non_blocking=True)
+        if self.k1 > 1:  # round-off floor of the zero gate after a genuine interpolation
+            changed = False
+            for L, idx, raw_off, _ in self.len_groups:
+                mx = self.raw[raw_off:raw_off + len(idx) * L].view(len(idx), L).abs().amax(dim=1).cpu().numpy()
+                for j, i in enumerate(idx):
+                    v = 1e-13 * float(mx[j])
+                    if self.recs[i].gate_floor != v:
+                        self.recs[i].gate_floor = v
+                        changed = True
+            if changed:
+                self._upload_records()
+
+    def check_fields(self):
+        if not bool(torch.isfinite(self.raw).all()):
+            raise ValueError("field has non-finite samples")
+
+    def launch(self, stream=None, _events=None):
+        """Issue the device pipeline on `stream` (default: the current stream)."""
+        lib = self.lib
+        stream = stream or torch.cuda.current_stream()
+        st = ctypes.c_void_p(stream.cuda_stream)
+        for L, idx, raw_off, fo in self.len_groups:
+            _check(lib.mma_tdse_prepare_fields(self.raw.data_ptr() + 8 * raw_off, len(idx), L, self.k1,
+                                               self.fld.data_ptr() + 8 * fo, st), "mma_tdse_prepare_fields")
+        if _events is not None:
+            _events[0].record(stream)
+        for Lc in self.launches:
+            B = BufRec(self.fld.data_ptr(), self.outputs.data_ptr(),
+                       self.psi_buf.data_ptr() if self.psi_buf is not None else None,
+                       self.snap_buf.data_ptr() if self.snap_buf is not None else None, Lc["counter"].data_ptr(),
+                       Lc["scratch"].data_ptr(), Lc["sbytes"])
+            _check(lib.mma_tdse_propagate(Lc["d_insts"].data_ptr(), len(Lc["idx"]), self.grids.dev_recs.data_ptr(),
+                                          ctypes.byref(B), Lc["max_m"], Lc["ctas"], self.prec, st),
+                   "mma_tdse_propagate")
+        if _events is not None:
+            _events[1].record(stream)
+        for G in self.spec_groups:
+            s = G["s"]
+            nc = s // 2 + 1
+            _check(lib.mma_tdse_spectra(self.outputs.data_ptr() + 8 * (G["off"] + 2 * (s + 1)), 6 * (s + 1),
+                                        len(G["idx"]), s, self.dt, G["tmax"], G["fs"].data_ptr(), 2 * nc,
+                                        G["fm"].data_ptr(), nc, G["omega"].data_ptr(), st), "mma_tdse_spectra")
+
+    def capture(self):
+        """Record launch() as a CUDA graph (after one eager run that creates the cuFFT plans)."""
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.launch(s)
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch()
+        self.graph = g
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+
+    def result(self):
+        res = BatchResult(outputs=self.outputs, out_off=self.out_off, S=self.S, k1=self.k1, dt=self.dt,
+                          n_field=self.nf, psi_off=self.psi_off, psi_final=self.psi_buf, snapshots=self.snap_buf,
+                          snap_off=self.snap_off, n_snap=self.n_snap, grid_ids=self.gid,
+                          ctas=[L["ctas"] for L in self.launches], spec_groups=self.spec_groups,
+                          spec_index=self.spec_index)
+        if len(self.s_groups) == 1:
+            s_len, idx, off = self.s_groups[0]
+            if np.array_equal(idx, np.arange(self.n_inst)):
+                blk = self.outputs.view(self.n_inst, 6, s_len + 1)
+                for j, k in enumerate(SERIES):
+                    res[k] = blk[:, j, :s_len]
+                if self.spectra:
+                    G = self.spec_groups[0]
+                    res["Fsourceterm"], res["FsourcetermM2"], res["omegagrid"] = G["F"], G["fm"], G["omega"]
+        return res
+
 
 def run_batch(grids, fields, dt_field, grid_ids=None, dt_req=None, tmin=0.0, spectra=True, psi_final=False,
               snap_every=0, precision="fp64", grid_ctas=0, stream=None, tmax=None, _events=None):
-    """Propagate a batch of instances.
+    """Propagate a batch of instances (one-shot form of TDSEBatchPlan).
 
     fields: float64 cuda tensor [n_inst, n_f] (uniform) or a list of 1-D tensors
     (uneven lengths).  grid_ids: per-instance grid index (default all 0).
-    Returns a BatchResult with packed ``outputs`` plus, for uniform batches, views
+    Returns a BatchResult with packed ``outputs``; for uniform batches also views
     ``sourceterm``, ``PopTot``, ``PopInt``, ``expval``, ``Efield``, ``tgrid``
     [n_inst, S] and spectra ``Fsourceterm`` [n_inst, S//2+1] (complex128),
     ``FsourcetermM2``, ``omegagrid``.
     """
-    lib = _sig()
-    if precision not in PRECISIONS:
-        raise ValueError("precision must be one of %s" % list(PRECISIONS))
-    dev = grids.device
     uniform = torch.is_tensor(fields) and fields.dim() == 2
-    rows = [fields[i] for i in range(fields.shape[0])] if uniform else list(fields)
-    n_inst = len(rows)
-    if n_inst == 0:
-        raise ValueError("empty batch")
-    k1, dt = refine(dt_field, dt_req if dt_req is not None else grids.dt)
-    if abs(dt - grids.dt) > 1e-12 * grids.dt:
-        raise ValueError("grids were built for dt=%g but this batch refines to dt=%g" % (grids.dt, dt))
-    gid = np.zeros(n_inst, dtype=np.int64) if grid_ids is None else np.asarray(grid_ids, dtype=np.int64)
-    if gid.shape != (n_inst,) or gid.min() < 0 or gid.max() >= len(grids):
-        raise ValueError("grid_ids must index the grids")
-    nf = np.array([int(r.numel()) for r in rows], dtype=np.int64)
-    if nf.min() < 2:
-        raise ValueError("every field needs at least 2 samples")
-    st = _stream_ptr(stream)
-    S = n_steps(nf, k1)
-    # refined fields, grouped by raw length for batched interpolation
-    fld_off = np.concatenate([[0], np.cumsum(k1 * nf)])[:-1]
-    fld = torch.empty(int((k1 * nf).sum()), dtype=torch.float64, device=dev)
-    gate_floor = np.zeros(n_inst)
-    for L in np.unique(nf):
-        idx = np.nonzero(nf == L)[0]
-        raw = torch.stack([rows[i].to(device=dev, dtype=torch.float64) for i in idx]) if not uniform else \
-            fields[torch.as_tensor(idx, device=dev)].to(torch.float64).contiguous()
-        if not torch.isfinite(raw).all():
-            raise ValueError("field has non-finite samples")
-        out = torch.empty(len(idx), k1 * int(L), dtype=torch.float64, device=dev)
-        _check(lib.mma_tdse_prepare_fields(raw.data_ptr(), len(idx), int(L), k1, out.data_ptr(), st),
-               "mma_tdse_prepare_fields")
-        if k1 > 1:
-            gate_floor[idx] = 1e-13 * raw.abs().amax(dim=1).cpu().numpy()
-        for j, i in enumerate(idx):
-            fld[fld_off[i]:fld_off[i] + k1 * L].copy_(out[j])
-    out_off = np.concatenate([[0], np.cumsum(6 * (S + 1))])[:-1]
-    outputs = torch.zeros(int((6 * (S + 1)).sum()), dtype=torch.float64, device=dev)
-    psi_off = np.full(n_inst, -1, dtype=np.int64)
-    psi_buf = None
-    if psi_final:
-        sizes = 2 * grids.n[gid]
-        psi_off = np.concatenate([[0], np.cumsum(sizes)])[:-1]
-        psi_buf = torch.zeros(int(sizes.sum()), dtype=torch.float64, device=dev)
-    snap_off = np.full(n_inst, -1, dtype=np.int64)
-    n_snap = np.zeros(n_inst, dtype=np.int64)
-    snap_buf = None
-    if snap_every:
-        n_snap = S // snap_every
-        sizes = n_snap * 2 * grids.n[gid]
-        snap_off = np.concatenate([[0], np.cumsum(sizes)])[:-1]
-        snap_buf = torch.zeros(int(sizes.sum()), dtype=torch.float64, device=dev)
-    insts = (InstRec * n_inst)()
-    for i in range(n_inst):
-        r = insts[i]
-        r.grid, r.n_steps, r.field_off, r.n_field = int(gid[i]), int(S[i]), int(fld_off[i]), int(k1 * nf[i])
-        r.out_off, r.psi_off, r.snap_off = int(out_off[i]), int(psi_off[i]), int(snap_off[i])
-        r.snap_every, r.n_snap = max(int(snap_every), 1), int(n_snap[i]) if snap_every else 0
-        r.tmin, r.gate_floor = float(tmin), float(gate_floor[i])
-    d_insts = torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(dev)
-    max_m = int(grids.m[np.unique(gid)].max())
-    prec = PRECISIONS[precision]
-    if prec == 1:
-        if not grids.c64:
-            raise ValueError("build the grids with c64=True for the complex64 form")
-        m32s = np.unique(grids.m32[np.unique(gid)])
-        if len(m32s) != 1:
-            raise ValueError("one complex64 launch needs grids of one m32; split the batch by grids.m32")
-        max_m = int(m32s[0])
-    ctas = grid_ctas or lib.mma_tdse_default_ctas(max_m, prec)
-    ctas = min(ctas, n_inst)
-    sbytes = lib.mma_tdse_scratch_bytes(max_m, ctas, prec)
-    scratch = torch.empty(max(int(sbytes), 8), dtype=torch.uint8, device=dev)
-    counter = torch.zeros(1, dtype=torch.int32, device=dev)
-    B = BufRec(fld.data_ptr(), outputs.data_ptr(), psi_buf.data_ptr() if psi_buf is not None else None,
-               snap_buf.data_ptr() if snap_buf is not None else None, counter.data_ptr(), scratch.data_ptr(),
-               int(sbytes))
-    if _events is not None:  # timing hook: events around the propagation launch only
-        _events[0].record(stream if stream is not None else torch.cuda.current_stream())
-    _check(lib.mma_tdse_propagate(d_insts.data_ptr(), n_inst, grids.dev_recs.data_ptr(), ctypes.byref(B), max_m, ctas,
-                                  prec, st), "mma_tdse_propagate")
-    if _events is not None:
-        _events[1].record(stream if stream is not None else torch.cuda.current_stream())
-    res = BatchResult(outputs=outputs, out_off=out_off, S=S, k1=k1, dt=dt, n_field=nf, psi_off=psi_off,
-                      psi_final=psi_buf, snapshots=snap_buf, snap_off=snap_off, n_snap=n_snap, grid_ids=gid,
-                      ctas=ctas, _keep=(d_insts, scratch, counter, fld))
-    if uniform and len(np.unique(S)) == 1:
-        s = int(S[0])
-        blk = outputs.view(n_inst, 6, s + 1)
-        for j, k in enumerate(("tgrid", "Efield", "sourceterm", "PopTot", "PopInt", "expval")):
-            res[k] = blk[:, j, :s]
-        if spectra:
-            nc = s // 2 + 1
-            if tmax is None:  # the reference's tgrid[Nf-1] - tgrid[0] (singleTDSE.c:50)
-                tmax = (int(nf[0]) - 1) * dt_field
-            fs = torch.empty(n_inst, 2 * nc, dtype=torch.float64, device=dev)
-            fm = torch.empty(n_inst, nc, dtype=torch.float64, device=dev)
-            om = torch.empty(nc, dtype=torch.float64, device=dev)
-            _check(lib.mma_tdse_spectra(outputs.data_ptr() + 8 * 2 * (s + 1), 6 * (s + 1), n_inst, s, dt, tmax,
-                                        fs.data_ptr(), 2 * nc, fm.data_ptr(), nc, om.data_ptr(), st),
-                   "mma_tdse_spectra")
-            res["Fsourceterm"] = torch.view_as_complex(fs.view(n_inst, nc, 2))
-            res["FsourcetermM2"] = fm
-            res["omegagrid"] = om
+    nf = [fields.shape[1]] * fields.shape[0] if uniform else [int(f.numel()) for f in fields]
+    plan = TDSEBatchPlan(grids, nf, dt_field, grid_ids=grid_ids, dt_req=dt_req, tmin=tmin, precision=precision,
+                         spectra=spectra, psi_final=psi_final, snap_every=snap_every, tmax=tmax, grid_ctas=grid_ctas)
+    plan.load_fields(fields)
+    plan.check_fields()
+    plan.launch(stream, _events=_events)
+    res = plan.result()
+    res["_plan"] = plan
     return res
