@@ -527,9 +527,15 @@ def main():
         torch.cuda.set_device(dev)
         print(json.dumps({"workload": "config2", "result": run_config2(args, dev)}))
         return
-    r64 = run_ours(args, rank, world, "fp64")
-    r = run_ours(args, rank, world, "c64")
+    r64 = run_ours(args, rank, world, "fp64") if args.forms in ("both", "fp64") else None
+    r = run_ours(args, rank, world, "c64") if args.forms in ("both", "c64") else None
     if rank != 0:
+        return
+    if r is None or r64 is None:  # single-form run (profiling): a short line, no form comparison
+        one = r or r64
+        print(json.dumps({"metric": METRIC, "value": one["value"], "unit": "site-steps/s", "forms": args.forms,
+                          "workload": args.workload, "ms_per_step": one["ms_per_step"],
+                          "kernel_ms": one["kernel_ms"]}))
         return
     errs = form_errors(r, r64)
     site_steps = r["n_inst"] * 8001.0 * r["S"]

@@ -173,9 +173,11 @@ const char *mma_last_error_message(void);
  *   cn_tab   [14 L]        Crank-Nicolson solve tables (complex)  (written by build)
  *   gs_tab   [5 L]         ground-state solve tables (real)       (written by build)
  *   result   [4]           {Einit, iterations, status, |dE| at stop}
- *   c64_tab  [5 * 256 * m32] floats, tables of the complex64 form (precision 1), laid
- *            out for m32 = ceil(m/8)*8 <= 32 sites per thread; NULL when unused
+ *   c64_tab  [4 * 256 * m32] floats, tables of the complex64 form (precision 1), laid
+ *            out for m32 = ceil(m/8)*8 <= 48 sites per thread; NULL when unused
  *            (written by mma_tdse_build_c64_tables)
+ *   adj_tab  [10 L] doubles, solve tables of A^H for the adjoint (NULL when unused;
+ *            written by mma_tdse_build_grids when not NULL)
  * The record has 8-byte fields only, so its layout is the same in every ABI. */
 typedef struct mma_tdse_grid {
     int64_t n, m;
@@ -184,6 +186,7 @@ typedef struct mma_tdse_grid {
     double *x, *gv, *psi0, *cn_tab, *gs_tab, *result;
     int64_t m32;
     float *c64_tab;
+    double *adj_tab;
 } mma_tdse_grid;
 
 /* One TDSE instance of a batch (offsets are in doubles). */
@@ -199,6 +202,9 @@ typedef struct mma_tdse_instance {
     int64_t n_snap;      /* snapshots kept; the last slot always holds the final state */
     double tmin;         /* start time (the reference's inputs.tmin) */
     double gate_floor;   /* |f| <= gate_floor counts as 0 in the zero-gate test (0 = exact) */
+    int64_t ckpt_off;    /* adjoint checkpoints: state psi_{cK} for c = 0, 1, ... (2n doubles each)
+                            in buffers.snapshots from this offset, or -1 */
+    int64_t ckpt_every;  /* K: steps between checkpoints (0 = none) */
 } mma_tdse_instance;
 
 typedef struct mma_tdse_buffers {
@@ -262,6 +268,29 @@ int mma_tdse_propagate_noalloc(const mma_tdse_instance *insts, int n_inst, const
 
 /* Size in bytes of the fixed work-space array behind mma_tdse_propagate_noalloc. */
 size_t mma_tdse_noalloc_capacity_bytes(void);
+
+/* ------------------------------------------------------------------------- */
+/* Adjoint (gradient of a spectral yield with respect to the field)            */
+/* ------------------------------------------------------------------------- */
+/* No counterpart in the reference (the differentiable form).  For each instance the loss
+ *   L = dt^2/(2 pi) sum_{q in Q} |DFT_q(s)|^2,  s = sourceterm samples 0..S-1,
+ *   Q = {q : w_lo <= 2 pi q / tmax <= w_hi}
+ * (the FsourcetermM2 values of the reference's spectrum summed over a band).
+ * mma_tdse_loss_grad: L and a_n = dL/ds_n for each instance, from the sourceterm series
+ *   in `outputs` (layout of mma_tdse_propagate); loss [n_inst], a [sum(S+1)] at the
+ *   instances' out_off/6 ... see a_off; tmax per instance.
+ * mma_tdse_adjoint: dL/dF_k for k = 0..S-1 (F_k = the gated field of step k) by the
+ *   adjoint Crank-Nicolson recursion, backwards from the last step, recomputing the
+ *   forward states between the checkpoints the forward pass stored (instance.ckpt_*).
+ *   Grids need adj_tab.  FP64.  grad [sum S] at grad_off[i]; scratch from
+ *   mma_tdse_adjoint_scratch_bytes. */
+int mma_tdse_loss_grad(const mma_tdse_instance *insts, int n_inst, const double *outputs, const double *tmax,
+                       double dt, double w_lo, double w_hi, double *loss, double *a, const int64_t *a_off,
+                       void *stream);
+size_t mma_tdse_adjoint_scratch_bytes(int max_m, int max_ckpt_every, int grid_ctas);
+int mma_tdse_adjoint(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
+                     const mma_tdse_buffers *bufs, const double *a, const int64_t *a_off, double *grad,
+                     const int64_t *grad_off, int max_m, int max_ckpt_every, int grid_ctas, void *stream);
 
 /* Fourier interpolation (1DTDSE/sources/tools_fftw3.c:24-68) of n_batch fields of
  * equal length n_raw (rows of `raw`, contiguous) by factor k1 into `interp`

@@ -171,69 +171,96 @@ __device__ __forceinline__ void ff_acc(float& hi, float& lo, float part)
 }
 
 // ------------------------------------------------------------------------ fast form, stage 1
-// z-contraction B_m[w, r] = sum_k tau_k v_k^m A_k[w, r]: one thread per (w, r), source read once.
+// Per-plane constants, independent of frequency, computed once per call:
+//   ptab[k*(MM+2) + m] = tau_k v_k^m  (m < MM),  ptab[k*(MM+2) + MM, +MM+1] = 1/(2 D_k) as (hi, lo).
 template <int MM>
-__global__ void __launch_bounds__(kThreads) fast_stage1(mma_hankel_problem P, mma_hankel_fast_plan_t F,
-                                                        const double* og, const double* rg, const double* zg,
-                                                        const void* src, const double2* pre, float2* Bp)
+__global__ void fast_plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, const double* zg, float* ptab)
 {
-    extern __shared__ float smem[];
-    const int64_t o = blockIdx.y, Nz = P.n_z, Nr = P.n_r, No = P.n_omega;
-    float* coef = smem;                                           // Nz * MM
-    float2* k2 = reinterpret_cast<float2*>(smem + ((Nz * MM + 1) / 2) * 2);  // Nz: k/(2 D_k) (hi, lo)
-    float2* pr = k2 + Nz;                                         // Nz: pre-factor
-    const double k = og[o] / kC;
-    for (int64_t q = threadIdx.x; q < Nz; q += blockDim.x) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P.n_z; q += (int64_t)gridDim.x * blockDim.x) {
         const double D = P.distance - zg[q];
         const double lam = F.d_ref / D;
         const double v = (1.0 - lam * lam) / F.sigma;
-        double c = trap_w(zg, q, Nz);
+        double c = trap_w(zg, q, P.n_z);
+        float* row = ptab + q * (MM + 2);
         for (int m = 0; m < MM; m++) {
-            coef[q * MM + m] = (float)c;
+            row[m] = (float)c;
             c *= v;
         }
         float hi, lo;
-        split_d(k / (2.0 * D), hi, lo);
-        k2[q] = make_float2(hi, lo);
+        split_d(1.0 / (2.0 * D), hi, lo);
+        row[MM] = hi;
+        row[MM + 1] = lo;
+    }
+}
+
+// z-contraction B_m[w, r] = sum_k tau_k v_k^m A_k[w, r]: one thread per (w, r), source read once,
+// four planes in flight per thread.
+template <int MM>
+__global__ void __launch_bounds__(kThreads) fast_stage1(mma_hankel_problem P, const double* og, const double* rg,
+                                                        const void* src, const double2* pre, const float* ptab,
+                                                        float2* Bp)
+{
+    extern __shared__ float smem[];
+    const int64_t o = blockIdx.y, Nz = P.n_z, Nr = P.n_r, No = P.n_omega;
+    constexpr int RW = MM + 2;
+    float* tabs = smem;                                                   // Nz * RW
+    float2* pr = reinterpret_cast<float2*>(smem + ((Nz * RW + 1) / 2) * 2);  // Nz: pre-factor
+    for (int64_t q = threadIdx.x; q < Nz * RW; q += blockDim.x) tabs[q] = ptab[q];
+    for (int64_t q = threadIdx.x; q < Nz; q += blockDim.x) {
         const double2 pf = pre ? pre[q * No + o] : make_double2(1.0, 0.0);
         pr[q] = make_float2((float)pf.x, (float)pf.y);
     }
     __syncthreads();
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= Nr) return;  // no barrier below
+    float kh, kl;  // k_w as float-float
+    split_d(og[o] / kC, kh, kl);
     const double rr = rg[r];
     float r2h, r2l;
     split_d(rr * rr, r2h, r2l);
+    // k r^2 as float-float; the plane angle is (k r^2) * (1/(2 D_k))
+    const float kr2h = kh * r2h;
+    const float kr2l = fmaf(kh, r2h, -kr2h) + fmaf(kh, r2l, kl * r2h);
     const float wr = (float)(trap_w(rg, r, Nr) * rr);
     float2 part[MM], hi[MM], lo[MM];
 #pragma unroll
     for (int m = 0; m < MM; m++) part[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
-    for (int64_t kz = 0; kz < Nz; kz++) {
-        const float2 s = load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r, P.source_c128);
-        const float2 pf = pr[kz];
-        float2 a = make_float2(fmaf(pf.x, s.x, -pf.y * s.y), fmaf(pf.x, s.y, pf.y * s.x));
-        if (P.near_field) {
-            const float2 kk = k2[kz];
-            const float th = kk.x * r2h;
-            const float te = fmaf(kk.x, r2h, -th) + fmaf(kk.x, r2l, kk.y * r2h);
-            float sn, cs;
-            sincosf(reduce_2pi(th, te), &sn, &cs);  // e^{-i theta} = (cs, -sn)
-            a = make_float2(fmaf(a.x, cs, a.y * sn), fmaf(a.y, cs, -a.x * sn));
-        }
-        a.x *= wr;
-        a.y *= wr;
-        const float* cz = coef + kz * MM;
+    const int64_t base = o * P.omega_stride + r;
+    for (int64_t k0 = 0; k0 < Nz; k0 += 4) {
+        float2 sv[4];
 #pragma unroll
-        for (int m = 0; m < MM; m++) {
-            part[m].x = fmaf(cz[m], a.x, part[m].x);
-            part[m].y = fmaf(cz[m], a.y, part[m].y);
-        }
-        if ((kz & 15) == 15 || kz == Nz - 1) {
+        for (int u = 0; u < 4; u++)
+            sv[u] = (k0 + u < Nz) ? load_src_f(src, (k0 + u) * P.plane_stride + base, P.source_c128)
+                                  : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t kz = k0 + u;
+            if (kz >= Nz) break;
+            const float* row = tabs + kz * RW;
+            const float2 pf = pr[kz];
+            float2 a = make_float2(fmaf(pf.x, sv[u].x, -pf.y * sv[u].y), fmaf(pf.x, sv[u].y, pf.y * sv[u].x));
+            if (P.near_field) {
+                const float ih = row[MM], il = row[MM + 1];
+                const float th = kr2h * ih;
+                const float te = fmaf(kr2h, ih, -th) + fmaf(kr2h, il, kr2l * ih);
+                float sn, cs;
+                sincosf(reduce_2pi(th, te), &sn, &cs);  // e^{-i theta} = (cs, -sn)
+                a = make_float2(fmaf(a.x, cs, a.y * sn), fmaf(a.y, cs, -a.x * sn));
+            }
+            a.x *= wr;
+            a.y *= wr;
 #pragma unroll
             for (int m = 0; m < MM; m++) {
-                ff_acc(hi[m].x, lo[m].x, part[m].x);
-                ff_acc(hi[m].y, lo[m].y, part[m].y);
-                part[m] = make_float2(0.f, 0.f);
+                part[m].x = fmaf(row[m], a.x, part[m].x);
+                part[m].y = fmaf(row[m], a.y, part[m].y);
+            }
+            if ((kz & 15) == 15 || kz == Nz - 1) {
+#pragma unroll
+                for (int m = 0; m < MM; m++) {
+                    ff_acc(hi[m].x, lo[m].x, part[m].x);
+                    ff_acc(hi[m].y, lo[m].y, part[m].y);
+                    part[m] = make_float2(0.f, 0.f);
+                }
             }
         }
     }
@@ -461,23 +488,30 @@ extern "C" int mma_hankel_fast_plan(const double* zg, int64_t nz, double distanc
     return MMA_OK;
 }
 
+// scratch: B [n_omega][n_terms][n_r] complex float, then the per-plane table (n_z rows of n_terms+2 floats)
+static size_t bp_bytes(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
+{
+    return (sizeof(float2) * (size_t)p->n_omega * (size_t)plan->n_terms * (size_t)p->n_r + 255) / 256 * 256;
+}
+
 extern "C" size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
 {
     if (!p || !plan) return 0;
-    return sizeof(float2) * (size_t)p->n_omega * (size_t)plan->n_terms * (size_t)p->n_r;
+    return bp_bytes(p, plan) + sizeof(float) * (size_t)p->n_z * (size_t)(plan->n_terms + 2);
 }
 
 namespace {
 template <int MM>
 int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, const double* og, const double* rg,
                 const double* zg, const double* rho, const void* src, const double2* pre, double2* ff,
-                float2* Bp, cudaStream_t st)
+                float2* Bp, float* ptab, cudaStream_t st)
 {
-    const size_t s1 = sizeof(float) * (((size_t)p->n_z * MM + 1) / 2 * 2) + sizeof(float2) * 2 * (size_t)p->n_z;
+    const size_t s1 = sizeof(float) * (((size_t)p->n_z * (MM + 2) + 1) / 2 * 2) + sizeof(float2) * (size_t)p->n_z;
     if (s1 > 200 * 1024) return MMA_ERR_TOO_LARGE;
+    fast_plane_table<MM><<<(unsigned)((p->n_z + 127) / 128), 128, 0, st>>>(*p, *plan, zg, ptab);
     cudaFuncSetAttribute(fast_stage1<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
     dim3 g1((unsigned)((p->n_r + kThreads - 1) / kThreads), (unsigned)p->n_omega);
-    fast_stage1<MM><<<g1, kThreads, s1, st>>>(*p, *plan, og, rg, zg, src, pre, Bp);
+    fast_stage1<MM><<<g1, kThreads, s1, st>>>(*p, og, rg, src, pre, ptab, Bp);
     int rtile = (int)(p->n_r < 512 ? p->n_r : 512);
     while ((size_t)(MM + 1) * rtile * sizeof(float2) > 96 * 1024 && rtile > 32) rtile /= 2;
     const size_t s2 = (size_t)(MM + 1) * rtile * sizeof(float2);
@@ -501,16 +535,17 @@ extern "C" int mma_hankel_fast(const mma_hankel_problem* p, const mma_hankel_fas
     const double2* pre2 = reinterpret_cast<const double2*>(pre);
     double2* ff2 = reinterpret_cast<double2*>(ff);
     float2* Bp = reinterpret_cast<float2*>(scratch);
+    float* ptab = reinterpret_cast<float*>(static_cast<char*>(scratch) + bp_bytes(p, plan));
     int rc;
     switch (plan->n_terms) {
-        case 8: rc = launch_fast<8>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
-        case 12: rc = launch_fast<12>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
-        case 16: rc = launch_fast<16>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
-        case 20: rc = launch_fast<20>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
-        case 24: rc = launch_fast<24>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
-        case 32: rc = launch_fast<32>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
-        case 40: rc = launch_fast<40>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
-        case 48: rc = launch_fast<48>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, st); break;
+        case 8: rc = launch_fast<8>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
+        case 12: rc = launch_fast<12>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
+        case 16: rc = launch_fast<16>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
+        case 20: rc = launch_fast<20>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
+        case 24: rc = launch_fast<24>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
+        case 32: rc = launch_fast<32>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
+        case 40: rc = launch_fast<40>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
+        case 48: rc = launch_fast<48>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
         default: return MMA_ERR_ARG;
     }
     if (rc != MMA_OK) return rc;

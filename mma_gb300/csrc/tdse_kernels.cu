@@ -19,18 +19,9 @@
 #include "../../include/mma_tdse.h"
 #include "common.cuh"
 #include "tdse_solver.cuh"
+#include "tdse_step.cuh"
 
 namespace mma {
-
-// Slots of the complex CN table (each L = m*kThreads complex entries, chunk-interleaved).
-enum { CN_IB6 = 0, CN_H, CN_F, CN_G, CN_GG, CN_PSI0, CN_GVX, CN_SLOTS };
-// Slots of the real ground-state table.
-enum { GS_IB12 = 0, GS_H, GS_F, GS_G, GS_GG, GS_SLOTS };
-
-__device__ __forceinline__ double soft_coulomb(double x, double a) { return -1.0 / sqrt(a * a + x * x); }
-__device__ __forceinline__ double minus_grad_v(double x, double a) { return x * pow(a * a + x * x, -1.5); }
-
-__device__ __forceinline__ int64_t qidx(int64_t j, int64_t m) { return (j % m) * kThreads + (j / m); }
 
 // ------------------------------------------------------------------------------------------
 // Sequential factorisation of one tridiagonal matrix (thread 0), results chunk-interleaved.
@@ -277,6 +268,26 @@ __global__ void __launch_bounds__(kThreads) build_grids_kernel(const mma_tdse_gr
     __syncthreads();
     chunk_products<cd>(m, ctab + CN_H * L, ctab + CN_G * L, ctab + CN_F * L, ctab + CN_GG * L);
     __syncthreads();
+    if (G.adj_tab) {
+        // A^H for the adjoint: row j has sub = super = 1/12 - i w_j and diagonal 10/12 - i d_j
+        // (the conjugate transpose of A's rows j-1, j, j+1); right-hand side used as is.
+        cd* atab = reinterpret_cast<cd*>(G.adj_tab);
+        for (int64_t q = t; q < ADJ_SLOTS * L; q += kThreads) atab[q] = cd{0.0, 0.0};
+        __syncthreads();
+        if (t == 0) {
+            const double hdt = 0.5 * dt;
+            auto row = [&](int64_t j, cd& aj, cd& bj, cd& cj) {
+                const double wj = hdt * (-0.5 / (dx * dx)) + hdt * 1 / 12. * V[j];
+                aj = (j > 0) ? cd{1.0 / 12.0, -wj} : cd{0.0, 0.0};
+                bj = cd{10.0 / 12.0, -(hdt * (1.0 / (dx * dx)) + hdt * 10 / 12. * V[j])};
+                cj = (j + 1 < n) ? cd{1.0 / 12.0, -wj} : cd{0.0, 0.0};
+            };
+            factorise<cd>(n, m, atab + CN_IB6 * L, atab + CN_H * L, atab + CN_G * L, 1.0, row);
+        }
+        __syncthreads();
+        chunk_products<cd>(m, atab + CN_H * L, atab + CN_G * L, atab + CN_F * L, atab + CN_GG * L);
+        __syncthreads();
+    }
     for (int64_t j = t; j < n; j += kThreads) G.gv[j] = minus_grad_v(G.x[j], a);
     __syncthreads();
     for (int64_t i = 0; i < m; i++) {
@@ -304,21 +315,6 @@ struct PropArgs {
     int64_t max_L;
 };
 
-// First index where the reference's zero gate opens: the first k with f[k] f[k+1] <= 0
-// (prop.c:125-134); samples at and beyond n_field are zero, and samples with
-// |f| <= floor count as zero in this test (floor is 0 unless the field was
-// Fourier-interpolated, where it absorbs the transform's round-off).
-__device__ int64_t gate_index(const double* f, int64_t n_field, int64_t n_steps, double floor_)
-{
-    for (int64_t k = 0; k < n_steps; k++) {
-        double a = (k < n_field) ? f[k] : 0.0, b = (k + 1 < n_field) ? f[k + 1] : 0.0;
-        if (fabs(a) <= floor_) a = 0.0;
-        if (fabs(b) <= floor_) b = 0.0;
-        if (a * b <= 0.0) return k;
-    }
-    return n_steps;
-}
-
 template <bool PSI_SMEM>
 __global__ void __launch_bounds__(kThreads, 1) propagate_fp64_kernel(PropArgs P)
 {
@@ -340,8 +336,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_fp64_kernel(PropArgs P)
         const mma_tdse_grid G = P.grids[I.grid];
         const int64_t n = G.n, m = G.m, L = m * kThreads, S = I.n_steps;
         const cd* tab = reinterpret_cast<const cd*>(G.cn_tab);
-        const cd *ib6 = tab + CN_IB6 * L, *hh = tab + CN_H * L, *FF = tab + CN_F * L, *gg = tab + CN_G * L,
-                 *GG = tab + CN_GG * L, *P0 = tab + CN_PSI0 * L, *GVX = tab + CN_GVX * L;
+        const cd *P0 = tab + CN_PSI0 * L, *GVX = tab + CN_GVX * L;
         const double* f = P.fields + I.field_off;
         double* out = P.outputs + I.out_off;
         double *o_t = out, *o_e = out + (S + 1), *o_src = out + 2 * (S + 1), *o_ptot = out + 3 * (S + 1),
@@ -393,6 +388,13 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_fp64_kernel(PropArgs P)
         double tt = I.tmin;
         const int64_t s0 = t * m;
         const double xs = (s0 < n) ? GVX[t].im : 0.0;
+        const bool ckpt = I.ckpt_every > 0 && I.ckpt_off >= 0 && P.snapshots;
+        auto store_state = [&](int64_t slot) {  // natural order, 2n doubles per slot
+            double* dst = P.snapshots + I.ckpt_off + slot * 2 * n;
+            for (int64_t i = 0; i < m; i++)
+                if (s0 + i < n) st2(dst + 2 * (s0 + i), psi[i * kThreads + t]);
+        };
+        if (ckpt) store_state(0);
 
         for (int64_t k = 0; k < S; k++) {
             const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : f[k];
@@ -414,46 +416,9 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_fp64_kernel(PropArgs P)
                 o_t[k + 1] = tt;
                 o_e[k + 1] = Fk;
             }
-            // ---- pass 1: local forward sweep of the right-hand side 2 M2 psi
-            cd pm = (t == 0) ? cd{0.0, 0.0} : psi[(m - 1) * kThreads + t - 1];
-            cd pc = psi[t];
-            cd yprev{0.0, 0.0};
-            for (int64_t i = 0; i < m; i++) {
-                int64_t q = i * kThreads + t;
-                cd pn = (i + 1 < m) ? psi[q + kThreads] : ((t + 1 < kThreads) ? psi[t + 1] : cd{0.0, 0.0});
-                cd r{fma(10.0, pc.re, pm.re + pn.re), fma(10.0, pc.im, pm.im + pn.im)};
-                cd y = cfms(hh[q], yprev, cmul(ib6[q], r));
-                yl[q] = y;
-                yprev = y;
-                pm = pc;
-                pc = pn;
-            }
-            const cd yin = scan_forward<cd>(FF[(m - 1) * kThreads + t], yprev, sc, sb);
-            // ---- pass 2: local backward sweep with the forward correction
-            cd unext{0.0, 0.0};
-            for (int64_t i = m - 1; i >= 0; i--) {
-                int64_t q = i * kThreads + t;
-                cd y = cfma(FF[q], yin, yl[q]);
-                cd u = cfms(gg[q], unext, y);
-                yl[q] = u;
-                unext = u;
-            }
-            const cd uin = scan_backward<cd>(GG[t], unext, sc + kWarps, sb + kWarps);
-            // ---- pass 3: backward correction, CN update, phase e^{+i F dt x}, observables
-            double sn, cs;
-            sincos(Fk * dt * xs, &sn, &cs);
-            cd ph{cs, sn};
-            sincos(Fk * dt * dx, &sn, &cs);
-            const cd z{cs, sn};
             double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-            for (int64_t i = 0; i < m; i++) {
-                int64_t q = i * kThreads + t;
-                int64_t j = s0 + i;
-                cd u = cfma(GG[q], uin, yl[q]);
-                cd d = u - psi[q];
-                cd pn = cmul(ph, d);
-                psi[q] = pn;
-                ph = cmul(ph, z);
+            cn_step_fp64(psi, yl, tab, m, L, Fk, dt, dx, xs, sc, sb, [&](int64_t q, int64_t i, const cd& pn) {
+                const int64_t j = s0 + i;
                 const double n2 = fma(pn.re, pn.re, pn.im * pn.im);
                 const cd gx = GVX[q];
                 const cd p0 = P0[q];
@@ -462,7 +427,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_fp64_kernel(PropArgs P)
                 acc[2] = fma(pn.re, p0.re, fma(pn.im, p0.im, acc[2]));
                 acc[3] = fma(pn.re, p0.im, fma(-pn.im, p0.re, acc[3]));
                 if (j >= lo && j <= hi) acc[4] += n2;
-            }
+            });
 #pragma unroll
             for (int c = 0; c < 5; c++)
 #pragma unroll
@@ -470,6 +435,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_fp64_kernel(PropArgs P)
             if (lane == 0)
 #pragma unroll
                 for (int c = 0; c < 5; c++) red[w * 5 + c] = acc[c];
+            if (ckpt && (k + 1) % I.ckpt_every == 0 && k + 1 < S) store_state((k + 1) / I.ckpt_every);
             if (I.snap_off >= 0 && P.snapshots) {  // prop.c:248-263
                 int64_t slot = -1;
                 if (k % I.snap_every == 0 && k / I.snap_every < I.n_snap - 1) slot = k / I.snap_every;

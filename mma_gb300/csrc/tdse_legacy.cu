@@ -101,6 +101,7 @@ int alloc_grid(DevGrid& g, int num_r, double dx, double a, double dt, double x_i
     g.h.result = p;
     g.h.m32 = 0;
     g.h.c64_tab = nullptr;
+    g.h.adj_tab = nullptr;
     if (cudaMemcpy(g.d, &g.h, sizeof(mma_tdse_grid), cudaMemcpyHostToDevice) != cudaSuccess) return MMA_ERR_CUDA;
     return MMA_OK;
 }
@@ -255,6 +256,8 @@ extern "C" void call1DTDSE(inputs_def* in, outputs_def* out)
     I.n_snap = n_snap;
     I.tmin = in->tmin;
     I.gate_floor = 0.0;
+    I.ckpt_off = -1;
+    I.ckpt_every = 0;
     if (k1 > 1) {
         double fmax = 0.0;
         for (int i = 0; i < nf; i++) fmax = fmax > fabs(in->Efield.Field[i]) ? fmax : fabs(in->Efield.Field[i]);

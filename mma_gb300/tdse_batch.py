@@ -36,13 +36,14 @@ class GridRec(Structure):
     _fields_ = [("n", c_int64), ("m", c_int64), ("dx", c_double), ("trg_a", c_double), ("dt", c_double),
                 ("x_int", c_double), ("Eguess", c_double), ("CV", c_double), ("max_iter", c_int64),
                 ("x", c_void_p), ("gv", c_void_p), ("psi0", c_void_p), ("cn_tab", c_void_p), ("gs_tab", c_void_p),
-                ("result", c_void_p), ("m32", c_int64), ("c64_tab", c_void_p)]
+                ("result", c_void_p), ("m32", c_int64), ("c64_tab", c_void_p), ("adj_tab", c_void_p)]
 
 
 class InstRec(Structure):
     _fields_ = [("grid", c_int64), ("n_steps", c_int64), ("field_off", c_int64), ("n_field", c_int64),
                 ("out_off", c_int64), ("psi_off", c_int64), ("snap_off", c_int64), ("snap_every", c_int64),
-                ("n_snap", c_int64), ("tmin", c_double), ("gate_floor", c_double)]
+                ("n_snap", c_int64), ("tmin", c_double), ("gate_floor", c_double), ("ckpt_off", c_int64),
+                ("ckpt_every", c_int64)]
 
 
 class BufRec(Structure):
@@ -115,7 +116,7 @@ class TDSEGrids:
     (already refined).  The ground states are computed on construction.
     """
 
-    def __init__(self, params, dt, device="cuda", stream=None, c64=False):
+    def __init__(self, params, dt, device="cuda", stream=None, c64=False, adjoint=False):
         lib = _sig()
         self.device = torch.device(device)
         self.dt = float(dt)
@@ -154,6 +155,13 @@ class TDSEGrids:
         self.m = np.array([s[1] for s in sizes])
         self.max_m = int(self.m.max())
         self.m32 = np.array([((m + 7) // 8) * 8 for m in self.m])
+        self.adjoint = bool(adjoint)
+        if self.adjoint:  # A^H solve tables (10 L doubles per grid)
+            a_sizes = 10 * THREADS * self.m
+            self.adj_buf = torch.zeros(int(a_sizes.sum()), dtype=torch.float64, device=self.device)
+            a_off = np.concatenate([[0], np.cumsum(a_sizes)])[:-1]
+            for r, o in zip(recs, a_off):
+                r.adj_tab = self.adj_buf.data_ptr() + 8 * int(o)
         self.c64 = bool(c64)
         if self.c64:
             if self.m32.max() > 48:
@@ -313,6 +321,7 @@ class TDSEBatchPlan:
             r.out_off, r.psi_off, r.snap_off = int(out_off[i]), int(self.psi_off[i]), int(self.snap_off[i])
             r.snap_every, r.n_snap = max(int(snap_every), 1), int(self.n_snap[i]) if snap_every else 0
             r.tmin, r.gate_floor = float(tmin), 0.0
+            r.ckpt_off, r.ckpt_every = -1, 0
         self.recs = recs
         # propagation launches: instances split by kernel shape, longest first within each
         cost = grids.n[gid].astype(np.float64) * S
