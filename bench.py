@@ -145,6 +145,62 @@ def run_config2(args, device):
     return out
 
 
+def run_config4(args, device):
+    """Adjoint: 256 instances on the config-1 grid (every 8th instance of the config-1 focus),
+    L = harmonic yield over [21, 31] omega0, checkpoints every 256 steps; timing of the
+    forward + adjoint gradient against the forward alone, and central finite differences
+    (h = 1e-6 a.u.) at 32 random samples per instance (each finite-difference pass perturbs
+    one sample in every instance: the instances are independent)."""
+    import torch
+
+    from mma_gb300.tdse_adjoint import yield_and_grad
+    from mma_gb300.tdse_batch import TDSEGrids
+
+    n_inst = 256 if args.workload == "config4" else 16
+    t, fields_np = focus_fields()
+    fields = torch.tensor(fields_np[::len(fields_np) // n_inst][:n_inst], device=device)
+    dtf = t[1] - t[0]
+    band = (21 * OMEGA0, 31 * OMEGA0)
+    grids = TDSEGrids([dict(num_r=8000, dx=0.1, trg_a=A_CONFIG)], dt=dtf, adjoint=True)
+    yield_and_grad(grids, fields[:2], dtf, band)  # warm-up
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    e[0].record()
+    L0, _ = yield_and_grad(grids, fields, dtf, band, want_grad=False)
+    e[1].record()
+    L, g = yield_and_grad(grids, fields, dtf, band, ckpt_every=256)
+    e[2].record()
+    torch.cuda.synchronize()
+    t_fwd, t_grad = e[0].elapsed_time(e[1]) * 1e-3, e[1].elapsed_time(e[2]) * 1e-3
+    n_samples = 32 if args.workload == "config4" else 4
+    rng = np.random.default_rng(0)
+    nf = fields.shape[1]
+    idx = np.stack([rng.choice(np.arange(4, nf - 4), size=n_samples, replace=False) for _ in range(n_inst)])
+    h = 1e-6
+    fd = np.zeros((n_inst, n_samples))
+    rows = torch.arange(n_inst, device=device)
+    for j in range(n_samples):
+        cols = torch.as_tensor(idx[:, j], device=device)
+        fp = fields.clone()
+        fm = fields.clone()
+        fp[rows, cols] += h
+        fm[rows, cols] -= h
+        Lp, _ = yield_and_grad(grids, fp, dtf, band, want_grad=False)
+        Lm, _ = yield_and_grad(grids, fm, dtf, band, want_grad=False)
+        fd[:, j] = ((Lp - Lm) / (2 * h)).cpu().numpy()
+    gn = g.cpu().numpy()
+    ga = np.take_along_axis(gn, idx, axis=1)
+    scale = np.abs(gn).max(axis=1, keepdims=True)
+    err = np.abs(ga - fd) / scale
+    return {"instances": n_inst, "steps": int(nf + 2), "sites": 8001, "checkpoint_every": 256,
+            "band_omega0": [21, 31], "forward_s": t_fwd, "forward_plus_adjoint_s": t_grad,
+            "gradient_cost_in_forwards": t_grad / t_fwd,
+            "site_steps_per_s_gradient": n_inst * 8001.0 * (nf + 2) / t_grad,
+            "fd": {"h": h, "samples_per_instance": n_samples,
+                   "max_abs_err_over_max_grad": float(err.max()), "median": float(np.median(err))},
+            "loss_matches_forward": float(torch.max(torch.abs(L - L0) / L0))}
+
+
 HANKEL_FLOP_PER_TERM = 8.0  # one complex multiply-accumulate per (omega, plane, rho, r) term
 
 
@@ -353,6 +409,7 @@ WORKLOADS = {
     # name: (n_r, n_z, n_cycles, hankel n_omega)
     "config1": (64, 32, 10, 2048),
     "config2": (64, 32, 10, 2048),  # uneven batch (run_config2), reported on its own line
+    "config4": (64, 32, 10, 2048),  # adjoint gradients (run_config4), reported on its own line
     "small": (8, 19, 2, 128),  # profiling case: same grids, fewer instances, shorter pulses
 }
 
@@ -447,17 +504,30 @@ def run_ours(args, rank, world, precision):
 
 def form_errors(test, ref, omega0=OMEGA0):
     """Errors of a form against the FP64 form on the same batch (the FP64 form equals the
-    oracle within 1e-8): worst-instance plateau |F|^2 (H11-H41) and dipole relative L2."""
+    oracle within 1e-8), on the plateau |F|^2 (H11-H41) and the dipole (sourceterm):
+
+    * ``plateau_rel_err_batch``: ||a - b|| / ||b|| over every instance together, the error that
+      reaches the far field (which sums the instances);
+    * median / p90 / max over the instances whose plateau holds at least 1e-3 of the strongest
+      instance's plateau energy; instances at the weak-field edge of a focus have no plateau
+      (cutoff below H11) and their relative error is the ratio of two round-off levels, so it
+      is reported apart (``plateau_rel_err_max_all``)."""
     import torch
 
     om = ref["omega"]
     sel = (om >= 11 * omega0) & (om <= 41 * omega0)
     a = test["spectrum"][:, sel].abs() ** 2
     b = ref["spectrum"][:, sel].abs() ** 2
-    pl = (torch.linalg.norm(a - b, dim=1) / torch.linalg.norm(b, dim=1))
+    nb = torch.linalg.norm(b, dim=1)
+    pl = torch.linalg.norm(a - b, dim=1) / nb
+    sig = nb >= 1e-3 * nb.max()
+    ps = pl[sig]
     st = (torch.linalg.norm(test["sourceterm"] - ref["sourceterm"], dim=1) /
           torch.linalg.norm(ref["sourceterm"], dim=1))
-    return {"plateau_rel_err_max": float(pl.max()), "plateau_rel_err_median": float(pl.median()),
+    return {"plateau_rel_err_batch": float(torch.linalg.norm(a - b) / torch.linalg.norm(b)),
+            "plateau_rel_err_median": float(ps.median()), "plateau_rel_err_p90": float(torch.quantile(ps, 0.9)),
+            "plateau_rel_err_max": float(ps.max()), "plateau_instances": int(sig.sum()),
+            "plateau_rel_err_max_all": float(pl.max()),
             "dipole_rel_l2_max": float(st.max()), "dipole_rel_l2_median": float(st.median())}
 
 
@@ -520,12 +590,13 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
-    if args.workload == "config2":
+    if args.workload in ("config2", "config4"):
         import torch
 
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
         torch.cuda.set_device(dev)
-        print(json.dumps({"workload": "config2", "result": run_config2(args, dev)}))
+        fn = run_config2 if args.workload == "config2" else run_config4
+        print(json.dumps({"workload": args.workload, "result": fn(args, dev)}))
         return
     r64 = run_ours(args, rank, world, "fp64") if args.forms in ("both", "fp64") else None
     r = run_ours(args, rank, world, "c64") if args.forms in ("both", "c64") else None
@@ -546,7 +617,7 @@ def main():
             "frac": achieved / peak if peak else None,
             "traffic": prof.get("dram_bytes_per_launch"),
             "peak_source": "measured live: FP32 FMA loop on every SM (mma_probe_fma_peak)",
-            "kernel": "propagate_c64_kernel<32>", "flops_per_site_step": FLOPS_PER_SITE_STEP}
+            "kernel": "propagate_c64_smem_kernel<32>", "flops_per_site_step": FLOPS_PER_SITE_STEP}
     a64 = FLOPS_PER_SITE_STEP * site_steps / (r64["kernel_ms"] * 1e-3)
     forms = {
         "tdse_plain_fp64": {"site_steps_per_s": r64["value"], "ms_per_step": r64["ms_per_step"],
@@ -577,7 +648,7 @@ def main():
 
         line["hankel"] = run_hankel(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
     if not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(r["t"], r["fields"], os.cpu_count() or 1)
+        line["cpu_baseline"] = cpu_baseline(r["t"], r["fields"], 4 * (os.cpu_count() or 1))
         if not args.no_hankel:
             line["hankel"]["cpu_baseline"] = hankel_cpu_baseline()
     print(json.dumps(line))

@@ -447,6 +447,290 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
     }
 }
 
+// Shared-memory form for M <= 32 (grids up to 8192 sites): the wavefunction lives in shared
+// memory next to the tables (24 bytes per site), which leaves registers for the chunk products
+// F and G, so each sweep runs once (three passes per step); the population window is summed
+// from shared memory by the threads whose chunk meets it; the observables use blocked
+// two-sum accumulation (8 sites in FP32, then an error-free update of a float-float pair).
+template <int M>
+__global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
+{
+    extern __shared__ float tab[];  // T_SLOTS * L floats, then psi [L] complex float
+    __shared__ cf sc[2 * kWarps], sb[2 * kWarps];
+    __shared__ float red_hi[kWarps * 4], red_lo[kWarps * 4], red_pi[kWarps];
+    __shared__ cf wtab[M];
+    __shared__ float s_ahi, s_alo;
+    __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    constexpr int L = kThreads * M;
+    cf* psi = reinterpret_cast<cf*>(tab + T_SLOTS * L);
+    if (t == 0) s_grid = -1;
+
+    for (;;) {
+        if (t == 0) s_inst = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int64_t inst = s_inst;
+        if (inst >= P.n_inst) break;
+        const mma_tdse_instance I = P.insts[inst];
+        const mma_tdse_grid G = P.grids[I.grid];
+        const int64_t n = G.n, S = I.n_steps;
+        if (s_grid != I.grid)
+            for (int q = t; q < T_SLOTS * L; q += kThreads) tab[q] = G.c64_tab[q];
+        __syncthreads();
+        if (t == 0) {
+            s_grid = I.grid;
+            s_gate = gate_index32(P.fields + I.field_off, I.n_field, S, I.gate_floor);
+            const int64_t num_r = n - 1;
+            int64_t lo = -1, hi;
+            if (!(-G.x_int < G.x[0])) {
+                int64_t i = 0;
+                while (i < num_r && !(-G.x_int <= G.x[i + 1])) i++;
+                lo = i;
+            }
+            if (G.x_int < G.x[0]) {
+                hi = 0;
+            } else {
+                int64_t i = 0;
+                while (i < num_r && !(G.x_int <= G.x[i + 1])) i++;
+                hi = (i < num_r) ? i + 1 : num_r + 1;
+            }
+            s_lo = lo < 0 ? 0 : lo;
+            s_hi = hi > num_r ? num_r : hi;
+        }
+        const float* ibre = tab + T_IBRE * L;
+        const float* ibim = tab + T_IBIM * L;
+        const float* vv = tab + T_V * L;
+        const float* p0 = tab + T_PSI0 * L;
+        const int64_t s0 = (int64_t)t * M;
+#pragma unroll
+        for (int i = 0; i < M; i++) psi[i * kThreads + t] = cf{p0[i * kThreads + t], 0.f};
+        const double xs_d = (s0 < n) ? G.x[s0] : 0.0;
+        const float xs_hi = (float)xs_d, xs_lo = (float)(xs_d - (double)xs_hi);
+        const float dxf = (float)G.dx;
+        const double dt = G.dt;
+        const double c6 = 6.0 * 0.5 * dt * (-0.5 / (G.dx * G.dx));
+        const float c_hi = (float)c6, c_lo = (float)(c6 - (double)c_hi), c1 = (float)(0.25 * dt);
+        __syncthreads();
+        const int64_t lo = s_lo, hi = s_hi, gate = s_gate;
+        // this thread's part of the population window [lo, hi], as chunk indices
+        const int win_a = (int)max((int64_t)0, lo - s0), win_b = (int)min((int64_t)M - 1, hi - s0);
+        const double* f = P.fields + I.field_off;
+        double* out = P.outputs + I.out_off;
+        double *o_t = out, *o_e = out + (S + 1), *o_src = out + 2 * (S + 1), *o_ptot = out + 3 * (S + 1),
+               *o_pint = out + 4 * (S + 1), *o_x = out + 5 * (S + 1);
+        {
+            double v[1] = {0.0};
+            for (int64_t j = t; j < n; j += kThreads)
+                if (j >= lo && j <= hi) v[0] += G.psi0[2 * j] * G.psi0[2 * j] + G.psi0[2 * j + 1] * G.psi0[2 * j + 1];
+            block_sum<1>(v, reinterpret_cast<double*>(red_hi));
+            if (t == 0) {
+                o_t[0] = I.tmin;
+                o_e[0] = 0.0;
+                o_src[0] = 0.0;
+                o_ptot[0] = 1.0;
+                o_pint[0] = v[0];
+                o_x[0] = 0.0;
+            }
+        }
+        double tt = I.tmin;
+        auto off_diag = [&](float v, float ir, float ii) -> cf {
+            const float t1 = fmaf(c1, v, c_lo);
+            return cf{fmaf(-t1, ii, fmaf(-c_hi, ii, 0.5f * ir)), fmaf(t1, ir, fmaf(c_hi, ir, 0.5f * ii))};
+        };
+        cf yl[M], fg[M];
+
+        for (int64_t k = 0; k < S; k++) {
+            if (w == 0 && k > 0) {  // observables of the previous step: two-sum over warps, FP64 finish
+                const int c = lane >> 3, q = lane & 7;
+                float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
+#pragma unroll
+                for (int d = 4; d >= 1; d >>= 1) {
+                    const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
+                    const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
+                    float s2, e2;
+                    two_sum(hs, oh, s2, e2);
+                    hs = s2;
+                    ls += ol + e2;
+                }
+                const double v = (double)hs + (double)ls;
+                const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
+                if (lane == 0) o_src[k] = -v + o_e[k];
+                if (lane == 8) o_x[k] = v;
+                if (lane == 16) o_ptot[k] = fma(pr, pr, pim * pim);
+                if (lane == 24) {
+                    float pi_sum = 0.f;
+                    for (int qq = 0; qq < kWarps; qq++) pi_sum += red_pi[qq];
+                    o_pint[k] = (double)pi_sum;
+                }
+            }
+            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : f[k];
+            if (w == 1 && lane == 0) {
+                tt += dt;
+                o_t[k + 1] = tt;
+                o_e[k + 1] = Fk;
+            }
+            if (w == kWarps - 1) {
+                for (int i = lane; i < M; i += 32) {
+                    float sn, cs;
+                    sincosf((float)(Fk * dt * G.dx) * (float)i, &sn, &cs);
+                    wtab[i] = cf{cs, sn};
+                }
+                if (lane == 31) {
+                    const double fdt = Fk * dt;
+                    const float a_hi = (float)fdt;
+                    s_ahi = a_hi;
+                    s_alo = (float)(fdt - (double)a_hi);
+                }
+            }
+            // ---- pass 1: right-hand side 2 M2 psi, local forward sweep, forward products F
+            cf pm = (t == 0) ? cf{0.f, 0.f} : psi[(M - 1) * kThreads + t - 1];
+            cf pc = psi[t];
+            cf yprev{0.f, 0.f}, Fp{1.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < M; i++) {
+                const int q = i * kThreads + t;
+                const cf pn = (i + 1 < M) ? psi[q + kThreads] : ((t + 1 < kThreads) ? psi[t + 1] : cf{0.f, 0.f});
+                const cf r{fmaf(10.f, pc.re, pm.re + pn.re), fmaf(10.f, pc.im, pm.im + pn.im)};
+                const float vl = (i == 0) ? ((t == 0) ? 0.f : vv[(M - 1) * kThreads + t - 1]) : vv[q - kThreads];
+                const cf ib{ibre[q], ibim[q]};
+                cf h = off_diag(vl, ib.re, ib.im);
+                if (s0 + i == 0) h = cf{0.f, 0.f};
+                yprev = cfms(h, yprev, cmul(ib, r));
+                yl[i] = yprev;
+                Fp = cmul(Fp, cf{-h.re, -h.im});
+                fg[i] = Fp;
+                pm = pc;
+                pc = pn;
+            }
+            const cf yin = scan_fwd(fg[M - 1], yprev, sc, sb);
+            // ---- pass 2: forward correction, local backward sweep, backward products G
+            cf unext{0.f, 0.f}, Gp{1.f, 0.f};
+#pragma unroll
+            for (int i = M - 1; i >= 0; i--) {
+                const int q = i * kThreads + t;
+                const cf y = cfma(fg[i], yin, yl[i]);
+                const float vr = (i == M - 1) ? ((t == kThreads - 1) ? 0.f : vv[t + 1]) : vv[q + kThreads];
+                cf g = off_diag(vr, ibre[q], ibim[q]);
+                if (s0 + i >= n - 1) g = cf{0.f, 0.f};
+                unext = cfms(g, unext, y);
+                yl[i] = unext;
+                Gp = cmul(Gp, cf{-g.re, -g.im});
+                fg[i] = Gp;
+            }
+            const cf uin = scan_bwd(fg[0], unext, sc + kWarps, sb + kWarps);
+            // ---- pass 3: backward correction, CN update, phase, observables
+            const float a_hi = s_ahi, a_lo = s_alo;
+            const float th_hi = a_hi * xs_hi;
+            const float th_lo = fmaf(a_hi, xs_hi, -th_hi) + fmaf(a_hi, xs_lo, a_lo * xs_hi);
+            const float kk = rintf(th_hi * (float)kInvTwoPi);
+            float red = fmaf(-kk, 6.28125f, th_hi);
+            red = fmaf(-kk, 1.93500518798828125e-3f, red);
+            red = fmaf(-kk, 3.0199159819370158e-07f, red) + th_lo;
+            float sn, cs;
+            sincosf(red, &sn, &cs);
+            const cf phs{cs, sn};
+            float ahi[4] = {0.f, 0.f, 0.f, 0.f}, alo[4] = {0.f, 0.f, 0.f, 0.f}, part[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < M; i++) {
+                const int q = i * kThreads + t;
+                const cf u = cfma(fg[i], uin, yl[i]);
+                const cf d = u - psi[q];
+                const cf pn = cmul(cmul(phs, wtab[i]), d);
+                psi[q] = pn;
+                const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
+                const float xj = fmaf(dxf, (float)i, xs_hi);
+                const float vj = vv[q], pj = p0[q];
+                part[0] = fmaf(n2, -xj * vj * vj * vj, part[0]);  // -V' = -x V^3
+                part[1] = fmaf(n2, xj, part[1]);
+                part[2] = fmaf(pn.re, pj, part[2]);
+                part[3] = fmaf(-pn.im, pj, part[3]);
+                if ((i & 7) == 7 || i == M - 1) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        float s2, e2;
+                        two_sum(ahi[c], part[c], s2, e2);
+                        ahi[c] = s2;
+                        alo[c] += e2;
+                        part[c] = 0.f;
+                    }
+                }
+            }
+            float pint = 0.f;
+            for (int i = win_a; i <= win_b; i++) {  // the few sites of the window (own chunk)
+                const cf p = psi[i * kThreads + t];
+                pint = fmaf(p.re, p.re, fmaf(p.im, p.im, pint));
+            }
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) {
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float oh = __shfl_xor_sync(0xffffffffu, ahi[c], d);
+                    const float ol = __shfl_xor_sync(0xffffffffu, alo[c], d);
+                    float s2, e2;
+                    two_sum(ahi[c], oh, s2, e2);
+                    ahi[c] = s2;
+                    alo[c] += ol + e2;
+                }
+                pint += __shfl_xor_sync(0xffffffffu, pint, d);
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    red_hi[w * 4 + c] = ahi[c];
+                    red_lo[w * 4 + c] = alo[c];
+                }
+                red_pi[w] = pint;
+            }
+            if (I.snap_off >= 0 && P.snapshots) {  // prop.c:248-263
+                int64_t slot = -1;
+                if (k % I.snap_every == 0 && k / I.snap_every < I.n_snap - 1) slot = k / I.snap_every;
+                if (k == S - 1) slot = I.n_snap - 1;
+                if (slot >= 0) {
+                    double* sp = P.snapshots + I.snap_off + slot * 2 * n;
+                    for (int i = 0; i < M; i++)
+                        if (s0 + i < n) {
+                            sp[2 * (s0 + i)] = psi[i * kThreads + t].re;
+                            sp[2 * (s0 + i) + 1] = psi[i * kThreads + t].im;
+                        }
+                }
+            }
+            __syncthreads();
+        }
+        if (w == 0) {  // observables of the last step
+            const int c = lane >> 3, q = lane & 7;
+            float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
+#pragma unroll
+            for (int d = 4; d >= 1; d >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
+                const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
+                float s2, e2;
+                two_sum(hs, oh, s2, e2);
+                hs = s2;
+                ls += ol + e2;
+            }
+            const double v = (double)hs + (double)ls;
+            const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
+            if (lane == 0) o_src[S] = -v + o_e[S];
+            if (lane == 8) o_x[S] = v;
+            if (lane == 16) o_ptot[S] = fma(pr, pr, pim * pim);
+            if (lane == 24) {
+                float pi_sum = 0.f;
+                for (int qq = 0; qq < kWarps; qq++) pi_sum += red_pi[qq];
+                o_pint[S] = (double)pi_sum;
+            }
+        }
+        if (P.psi_final && I.psi_off >= 0) {
+            double* pf = P.psi_final + I.psi_off;
+            for (int i = 0; i < M; i++)
+                if (s0 + i < n) {
+                    pf[2 * (s0 + i)] = psi[i * kThreads + t].re;
+                    pf[2 * (s0 + i) + 1] = psi[i * kThreads + t].im;
+                }
+        }
+        __syncthreads();
+    }
+}
+
 // Complex64 tables from the FP64 grid data, laid out for M32 sites per thread.
 __global__ void __launch_bounds__(kThreads) build_c64_kernel(const mma_tdse_grid* grids)
 {
@@ -491,9 +775,16 @@ namespace {
 template <int M>
 int launch_c64(const c64::Args& A, int ctas, cudaStream_t st)
 {
-    const size_t smem = (size_t)c64::T_SLOTS * kThreads * M * sizeof(float);
-    cudaFuncSetAttribute(c64::propagate_c64_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    c64::propagate_c64_kernel<M><<<ctas, kThreads, smem, st>>>(A);
+    if constexpr (M <= 32) {  // wavefunction in shared memory next to the tables
+        const size_t smem = (size_t)c64::T_SLOTS * kThreads * M * sizeof(float) + (size_t)kThreads * M * 8;
+        cudaFuncSetAttribute(c64::propagate_c64_smem_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        c64::propagate_c64_smem_kernel<M><<<ctas, kThreads, smem, st>>>(A);
+    } else {  // wavefunction in registers, five-pass re-sweep
+        const size_t smem = (size_t)c64::T_SLOTS * kThreads * M * sizeof(float);
+        cudaFuncSetAttribute(c64::propagate_c64_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        c64::propagate_c64_kernel<M><<<ctas, kThreads, smem, st>>>(A);
+    }
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }
 }  // namespace
