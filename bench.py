@@ -106,7 +106,7 @@ def run_config2(args, device):
     n_inst = 4096 if args.workload == "config2" else 256
     params, fields, E0 = config2_instances(n_inst)
     t0 = time.perf_counter()
-    g64 = TDSEGrids(params, dt=0.25, c64=True)
+    g64 = TDSEGrids(params, dt=0.25, c64=True, c64_threads="auto")
     torch.cuda.synchronize()
     t_grids = time.perf_counter() - t0
     tf = [torch.tensor(f, device=device) for f in fields]
@@ -261,6 +261,9 @@ def run_hankel(args, device):
     e1.record(stream)
     torch.cuda.synchronize()
     t_e2e = e0.elapsed_time(e1) * 1e-3
+    h2d_bytes, d2h_bytes = host_src.numel() * 8, host_ff.numel() * 16
+    del ffe, dsrc, host_src
+    allp = run_all_planes(args, target, z, rho, pre, flush, stream)
     out = {"workload": "config3: N_r=512, N_z=256 (255 planes integrated), N_omega=2048, N_rho=256, D=1 m, "
                        "complex64 source, constant XUV index n=1-1e-5+1e-7i, near-field factor on",
            "terms": terms, "flop_per_term": HANKEL_FLOP_PER_TERM,
@@ -270,9 +273,107 @@ def run_hankel(args, device):
                            "truncation_bound": plan["trunc_bound"],
                            "per_harmonic_rel_err_vs_plain": {"max": float(ph.max()), "median": float(np.median(ph))},
                            "includes": "FF_integrated plus entry and exit plane transforms"},
-           "e2e_fast": {"seconds": t_e2e, "h2d_bytes": host_src.numel() * 8, "d2h_bytes": host_ff.numel() * 16,
-                        "tflops_algorithmic": HANKEL_FLOP_PER_TERM * terms / t_e2e / 1e12}}
+           "e2e_fast": {"seconds": t_e2e, "h2d_bytes": h2d_bytes, "d2h_bytes": d2h_bytes,
+                        "tflops_algorithmic": HANKEL_FLOP_PER_TERM * terms / t_e2e / 1e12},
+           "all_planes": allp}
     return out
+
+
+def tc_geometry(n_terms, n_omega, n_rho, n_z, n_r):
+    """Padded GEMM extents of the tensor-core plane form: rows (rho, m), columns (plane, re/im), inner r."""
+    mm = {8: 8, 12: 16, 16: 16, 20: 32, 24: 32, 32: 32}[int(n_terms)]
+    rc = 2 * (128 // mm)
+    n_rb = -(-n_rho // rc)
+    zpad = -(-n_z // 128) * 128
+    rpad = -(-n_r // 32) * 32
+    rows = n_omega * n_rb * rc * mm
+    return {"terms": mm, "rows": rows, "cols": 2 * zpad, "inner": rpad,
+            "flops_executed": 2.0 * 3 * rows * 2 * zpad * rpad,
+            "flops_useful": 2.0 * 3 * n_omega * n_rho * mm * 2 * n_z * n_r}
+
+
+def run_all_planes(args, target, z, rho, pre, flush, stream):
+    """Every plane transform of config 3 (what Hankel_long's cumulative results need): the
+    tensor-core split-precision form (three FP16 GEMM terms per product, FP32 accumulation) against
+    the direct FP32 form (one J0 per term) and the plain FP64 form; errors per harmonic and plane
+    against the plain form."""
+    import torch
+
+    from mma_gb300 import hankel as H
+
+    Nz, No, Nr = target.source.shape
+    allp = list(range(Nz))
+
+    def call(form, via="auto", events=None):
+        return H.far_field(target.ogrid, target.rgrid, z, rho, target.source, 1.0, pre, True, planes=allp,
+                           form=form, planes_via=via, _events=events)
+
+    for _ in range(2):
+        call("fast", "tc")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t_all, t_k = [], []
+    ptc = plan = None
+    for _ in range(max(args.steps, 3)):
+        ptc = None
+        flush.add_(1.0)
+        e0.record(stream)
+        _, ptc, plan = call("fast", "tc", (k0, k1))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_all.append(e0.elapsed_time(e1) * 1e-3)
+        t_k.append(k0.elapsed_time(k1) * 1e-3)
+    P_tc = torch.stack([ptc[k] for k in allp])
+    del ptc
+    flush.add_(1.0)
+    e0.record(stream)
+    _, pdir, _ = call("fast", "direct")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_dir = e0.elapsed_time(e1) * 1e-3
+    P_dir = torch.stack([pdir[k] for k in allp])
+    del pdir
+    flush.add_(1.0)
+    e0.record(stream)
+    _, p64, _ = call("plain")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = e0.elapsed_time(e1) * 1e-3
+    P64 = torch.stack([p64[k] for k in allp])
+    del p64
+    nrm = torch.linalg.norm(P64, dim=1)  # [plane, omega]
+    e_tc = (torch.linalg.norm(P_tc - P64, dim=1) / nrm).flatten()
+    e_dir = (torch.linalg.norm(P_dir - P64, dim=1) / nrm).flatten()
+    del P_tc, P_dir, P64
+    geo = tc_geometry(plan["n_terms"], No, len(rho), Nz, Nr)
+    tk = float(np.median(t_k))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("bf16_tflops")
+    ach = geo["flops_executed"] / tk / 1e12
+    terms = float(No) * Nz * len(rho) * Nr
+    return {"planes": Nz, "tc_series_terms": geo["terms"],
+            "tensor_core": {"seconds": float(np.median(t_all)), "kernel_seconds": tk,
+                            "tflops_executed": ach, "tflops_useful": geo["flops_useful"] / tk / 1e12,
+                            "tflops_algorithmic": HANKEL_FLOP_PER_TERM * terms / float(np.median(t_all)) / 1e12,
+                            "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                                         "frac": ach / peak if peak else None,
+                                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst; FP16 dense "
+                                                        "runs at the BF16 rate)"},
+                            "gemm": geo,
+                            "per_harmonic_rel_err_vs_plain": {"max": float(e_tc.max()),
+                                                              "median": float(e_tc.median())},
+                            "includes": "FF_integrated (fast form) + plane tables + B operand + tensor-core "
+                                        "kernel; kernel_seconds is the tensor-core kernel alone"},
+            "direct_fp32": {"seconds": t_dir, "per_harmonic_rel_err_vs_plain": {"max": float(e_dir.max()),
+                                                                                 "median": float(e_dir.median())}},
+            "plain_fp64": {"seconds": t_plain},
+            "speedup_tc_vs_direct": t_dir / float(np.median(t_all)),
+            "speedup_tc_vs_plain": t_plain / float(np.median(t_all))}
 
 
 def hankel_cpu_baseline(cores=None):
@@ -410,6 +511,7 @@ WORKLOADS = {
     "config1": (64, 32, 10, 2048),
     "config2": (64, 32, 10, 2048),  # uneven batch (run_config2), reported on its own line
     "config4": (64, 32, 10, 2048),  # adjoint gradients (run_config4), reported on its own line
+    "config3": (64, 32, 10, 2048),  # the far field alone (run_hankel), reported on its own line
     "small": (8, 19, 2, 128),  # profiling case: same grids, fewer instances, shorter pulses
 }
 
@@ -429,7 +531,8 @@ def run_ours(args, rank, world, precision):
     tmax = t[-1] - t[0]
     n_inst = fields_np.shape[0]
     fields = torch.tensor(fields_np, device=dev)
-    grids = TDSEGrids([dict(num_r=8000, dx=0.1, trg_a=A_CONFIG)], dt=dtf, c64=(precision == "c64"))
+    grids = TDSEGrids([dict(num_r=8000, dx=0.1, trg_a=A_CONFIG)], dt=dtf, c64=(precision == "c64"),
+                      c64_threads="auto" if precision == "c64" else None)
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
     stream = torch.cuda.current_stream()
     plan = TDSEBatchPlan(grids, [fields.shape[1]] * n_inst, dtf, tmax=tmax, precision=precision)
@@ -495,7 +598,10 @@ def run_ours(args, rank, world, precision):
         e_ms.append(e2e_ev[0].elapsed_time(e2e_ev[1]))
     e2e_ms = float(np.mean(e_ms))
 
+    from mma_gb300 import autotune
+
     out = dict(value=value, ms_per_step=ms_step, S=S, n_inst=n_inst, kernel_ms=k_ms, peak=peak,
+               cta_threads=int(grids.c64_threads[0]), m32=int(grids.m32[0]), autotune=autotune.last_report(),
                clocks=clk.summary(), e2e_ms=e2e_ms, h2d=host_fields.numel() * 8, d2h=host_out.numel() * 16,
                t=t, fields=fields_np, spectrum=res["Fsourceterm"], omega=res["omegagrid"],
                sourceterm=res["sourceterm"])
@@ -590,12 +696,12 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
-    if args.workload in ("config2", "config4"):
+    if args.workload in ("config2", "config3", "config4"):
         import torch
 
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
         torch.cuda.set_device(dev)
-        fn = run_config2 if args.workload == "config2" else run_config4
+        fn = {"config2": run_config2, "config3": run_hankel, "config4": run_config4}[args.workload]
         print(json.dumps({"workload": args.workload, "result": fn(args, dev)}))
         return
     r64 = run_ours(args, rank, world, "fp64") if args.forms in ("both", "fp64") else None
@@ -617,7 +723,8 @@ def main():
             "frac": achieved / peak if peak else None,
             "traffic": prof.get("dram_bytes_per_launch"),
             "peak_source": "measured live: FP32 FMA loop on every SM (mma_probe_fma_peak)",
-            "kernel": "propagate_c64_smem_kernel<32>", "flops_per_site_step": FLOPS_PER_SITE_STEP}
+            "kernel": "propagate_c64_smem_kernel<%d, %d>" % (r["m32"], r["cta_threads"]),
+            "flops_per_site_step": FLOPS_PER_SITE_STEP}
     a64 = FLOPS_PER_SITE_STEP * site_steps / (r64["kernel_ms"] * 1e-3)
     forms = {
         "tdse_plain_fp64": {"site_steps_per_s": r64["value"], "ms_per_step": r64["ms_per_step"],
@@ -626,6 +733,8 @@ def main():
                                 world * site_steps / (r64["e2e_ms"] * 1e-3)},
         "tdse_chosen_c64": {"site_steps_per_s": r["value"], "ms_per_step": r["ms_per_step"],
                             "kernel_ms": r["kernel_ms"], "speedup_vs_plain": r["value"] / r64["value"],
+                            "cta_threads": r["cta_threads"], "sites_per_thread": r["m32"],
+                            "autotune_seconds_per_probe_batch": r["autotune"],
                             "error_vs_fp64": errs},
     }
     line = {"metric": METRIC, "value": r["value"], "unit": "site-steps/s", "n_gpus": world, "steps": args.steps,

@@ -13,6 +13,13 @@ extern "C" {
  * Used as the roofline denominator of the arithmetic-bound kernels. */
 int mma_probe_fma_peak(int precision, double *flops_per_s);
 
+/* Self-test of the tensor-core building blocks used by mma_hankel_planes_tc: one tile
+ * D[128][256] = A[128][32] * B[256][32]^T with FP16 A, B (row-major, device pointers) and FP32 D,
+ * through tcgen05.mma with the operands in 64-byte-swizzled shared memory.  A is staged by
+ * threads; B by threads (use_tma = 0) or by a TMA tiled load (use_tma = 1).  *status (device)
+ * is 0 on success, non-zero if a bounded wait gave up. */
+int mma_tc_selftest(const void *A, const void *B, float *D, int use_tma, int *status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

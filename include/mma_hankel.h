@@ -71,6 +71,35 @@ int mma_hankel_fast(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *p
                     double *ff, const int64_t *plane_slot, int n_planes, double *planes, void *scratch,
                     size_t scratch_bytes, void *stream);
 
+/* Tensor-core form of the per-plane transforms (the split-precision form), for calls that
+ * request many planes (the cumulative results of Hankel_long, :640-672).  Same series as
+ * mma_hankel_fast with the number of terms rounded up to 8, 16 or 32, arranged per frequency as
+ * a GEMM with rows (rho, m), inner dimension r, columns (plane, re/im):
+ *   B = per-plane tables A_k[w, r] (FP16 hi + lo, scaled per row), read by TMA;
+ *   A = K_m(k r rho / d_ref) scaled per m (FP16 hi + lo), generated on CUDA cores;
+ *   tcgen05.mma hi*hi + hi*lo + lo*hi into FP32 accumulators in TMEM; the epilogue applies
+ *   v_k^m and reduces over m.
+ * Writes planes[plane_slot[k]] for every k with plane_slot[k] >= 0 (n_planes >= 1).
+ * Requires n_r <= 1024 and a plan with n_terms <= 32 (else MMA_ERR_UNSUPPORTED).  Scratch of
+ * mma_hankel_planes_tc_scratch_bytes (256-byte aligned).  mma_hankel_planes_tc_status
+ * synchronises the stream and returns MMA_ERR_TIMEOUT if a bounded wait in the kernel gave up. */
+size_t mma_hankel_planes_tc_scratch_bytes(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan);
+int mma_hankel_planes_tc(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan, const double *ogrid,
+                         const double *rgrid, const double *zgrid, const double *rho, const void *source,
+                         const double *pre, const int64_t *plane_slot, int n_planes, double *planes, void *scratch,
+                         size_t scratch_bytes, void *stream);
+int mma_hankel_planes_tc_status(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan,
+                                const void *scratch, void *stream);
+/* The two halves of mma_hankel_planes_tc: _prepare builds the per-plane tables and the B operand
+ * in scratch (depends on the source, pre-factor, grids and plan); _run launches the tensor-core
+ * kernel (depends on rho, within the plan's y_max, and on the requested planes). */
+int mma_hankel_planes_tc_prepare(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan,
+                                 const double *ogrid, const double *rgrid, const double *zgrid, const void *source,
+                                 const double *pre, void *scratch, size_t scratch_bytes, void *stream);
+int mma_hankel_planes_tc_run(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan, const double *ogrid,
+                             const double *rgrid, const double *rho, const int64_t *plane_slot, int n_planes,
+                             double *planes, void *scratch, size_t scratch_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,7 +38,8 @@ typedef enum {
     MMA_ERR_CUFFT = 4,        /* a cuFFT call failed */
     MMA_ERR_TOO_LARGE = 5,    /* grid does not fit the selected kernel's limits */
     MMA_ERR_NO_DEVICE = 6,    /* no CUDA device: there is no CPU fallback */
-    MMA_ERR_UNSUPPORTED = 7   /* option the reference accepts but never implemented (velocity gauge) */
+    MMA_ERR_UNSUPPORTED = 7,  /* option the reference accepts but never implemented (velocity gauge) */
+    MMA_ERR_TIMEOUT = 8       /* a bounded wait inside a kernel gave up (the kernel returned early) */
 } mma_status;
 
 /* ------------------------------------------------------------------------- */
@@ -178,6 +179,8 @@ const char *mma_last_error_message(void);
  *            (written by mma_tdse_build_c64_tables)
  *   adj_tab  [10 L] doubles, solve tables of A^H for the adjoint (NULL when unused;
  *            written by mma_tdse_build_grids when not NULL)
+ *   c64_threads  CTA size the c64 tables are laid out for: 0 or 256 (m32 <= 48),
+ *            512 (m32 8 or 16) or 1024 (m32 8); c64_tab then holds 4 * c64_threads * m32 floats
  * The record has 8-byte fields only, so its layout is the same in every ABI. */
 typedef struct mma_tdse_grid {
     int64_t n, m;
@@ -187,6 +190,7 @@ typedef struct mma_tdse_grid {
     int64_t m32;
     float *c64_tab;
     double *adj_tab;
+    int64_t c64_threads;
 } mma_tdse_grid;
 
 /* One TDSE instance of a batch (offsets are in doubles). */
@@ -241,6 +245,17 @@ int mma_tdse_build_c64_tables(const mma_tdse_grid *grids_dev, const mma_tdse_gri
  *                  compensation and finished in FP64; needs c64 tables (n <= 8192) */
 int mma_tdse_propagate(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
                        const mma_tdse_buffers *bufs, int max_m, int grid_ctas, int precision, void *stream);
+
+/* mma_tdse_propagate with the CTA size of the complex64 form chosen by the caller (0 = 256):
+ * every instance's grid must carry c64 tables of shape (cta_threads, max_m), see
+ * mma_tdse_grid.c64_threads; instances whose grid has another shape get NaN outputs.
+ * For precision 0 cta_threads must be 0 or 256. */
+int mma_tdse_propagate_ex(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
+                          const mma_tdse_buffers *bufs, int max_m, int cta_threads, int grid_ctas, int precision,
+                          void *stream);
+
+/* 1 if the complex64 form has a kernel for CTA size cta_threads (0 = 256) and m32 sites per thread. */
+int mma_tdse_c64_shape_ok(int cta_threads, int m32);
 
 /* Scratch bytes mma_tdse_propagate needs for these arguments. */
 size_t mma_tdse_scratch_bytes(int max_m, int grid_ctas, int precision);

@@ -41,8 +41,8 @@ __device__ __forceinline__ double shfl_xor(double v, int d) { return __shfl_xor_
 __device__ __forceinline__ double shfl_idx(double v, int l) { return __shfl_sync(0xffffffffu, v, l); }
 
 // Sum of NV doubles over the CTA.  Every thread gets the totals; the order of the
-// additions is fixed, so the result is reproducible.  `red` holds kWarps*NV doubles.
-template <int NV>
+// additions is fixed, so the result is reproducible.  `red` holds NW*NV doubles (NW warps).
+template <int NV, int NW = kWarps>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double* red)
 {
 #pragma unroll
@@ -58,7 +58,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* red)
     for (int k = 0; k < NV; k++) {
         double s = 0.0;
 #pragma unroll
-        for (int q = 0; q < kWarps; q++) s += red[q * NV + k];
+        for (int q = 0; q < NW; q++) s += red[q * NV + k];
         v[k] = s;
     }
     __syncthreads();

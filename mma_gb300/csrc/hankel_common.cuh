@@ -1,0 +1,111 @@
+// hankel_common.cuh -- helpers shared by the far-field kernels (hankel.cu, hankel_tc.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/mma_hankel.h"
+
+namespace mma {
+namespace hk {
+
+constexpr double kC = 299792458.0;  // shared_python/units.py:3
+
+__device__ __forceinline__ double trap_w(const double* x, int64_t i, int64_t n)
+{
+    double w = 0.0;
+    if (i + 1 < n) w += 0.5 * (x[i + 1] - x[i]);
+    if (i > 0) w += 0.5 * (x[i] - x[i - 1]);
+    return w;
+}
+
+__device__ __forceinline__ double2 load_src_d(const void* src, int64_t idx, int64_t c128)
+{
+    if (c128) return reinterpret_cast<const double2*>(src)[idx];
+    const float2 v = reinterpret_cast<const float2*>(src)[idx];
+    return make_double2(v.x, v.y);
+}
+
+__device__ __forceinline__ float2 load_src_f(const void* src, int64_t idx, int64_t c128)
+{
+    if (c128) {
+        const double2 v = reinterpret_cast<const double2*>(src)[idx];
+        return make_float2((float)v.x, (float)v.y);
+    }
+    return reinterpret_cast<const float2*>(src)[idx];
+}
+
+// ------------------------------------------------------------------------ fast form helpers
+__device__ __forceinline__ void split_d(double v, float& hi, float& lo)
+{
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// (yh + yl) reduced mod 2 pi with 2 pi = C1 + C2 + C3 (C1, C2 short enough that k*C is exact)
+__device__ __forceinline__ float reduce_2pi(float yh, float yl)
+{
+    const float kk = rintf(yh * 0.159154943f);
+    float r = fmaf(-kk, 6.28125f, yh);
+    r = fmaf(-kk, 1.93500518798828125e-3f, r);
+    r = fmaf(-kk, 3.0199159819370158e-07f, r);
+    return r + yl;
+}
+
+// J0 and J1 in FP32 from the rational/asymptotic approximations of Abramowitz & Stegun
+// 9.4.1, 9.4.4 (x < 3) and 9.4.3, 9.4.6 (x >= 3; modulus and phase, |error| < 1e-7 absolute),
+// with the phase argument x reduced mod 2 pi in float-float (x = yh + yl).
+template <bool WANT_J1>
+__device__ __forceinline__ void bessel01(float yh, float yl, float& J0, float& J1)
+{
+    if (yh < 3.0f) {
+        const float y = yh + yl;
+        const float u = (y * 0.333333343f) * (y * 0.333333343f);
+        J0 = fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, 0.0002100f, -0.0039444f), 0.0444479f), -0.3163866f),
+                                      1.2656208f), -2.2499997f), 1.0f);
+        if (WANT_J1)
+            J1 = y * fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, 0.00001109f, -0.00031761f), 0.00443319f),
+                                               -0.03954289f), 0.21093573f), -0.56249985f), 0.5f);
+    } else {
+        const float t = 3.0f / yh;
+        const float red = reduce_2pi(yh, yl);
+        const float sq = rsqrtf(yh);
+        const float f0 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.00014476f, -0.00072805f), 0.00137237f),
+                                                   -0.00009512f), -0.00552740f), -0.00000077f), 0.79788456f);
+        const float p0 = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.00013558f, -0.00029333f), -0.00054125f),
+                                               0.00262573f), -0.00003954f), -0.04166397f);
+        J0 = f0 * sq * cosf(red - 0.785398163f + p0);
+        if (WANT_J1) {
+            const float f1 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, -0.00020033f, 0.00113653f), -0.00249511f),
+                                                       0.00017105f), 0.01659667f), 0.00000156f), 0.79788456f);
+            const float p1 = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, -0.00029166f, 0.00079824f), 0.00074348f),
+                                                   -0.00637879f), 0.00005650f), 0.12499612f);
+            J1 = f1 * sq * cosf(red - 2.35619449f + p1);
+        }
+    }
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// add a partial sum into a float-float accumulator (hi, lo)
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float part)
+{
+    float s, e;
+    two_sum(hi, part, s, e);
+    hi = s;
+    lo += e;
+}
+
+inline bool valid(const mma_hankel_problem* p)
+{
+    return p && p->n_omega > 0 && p->n_r > 1 && p->n_z > 0 && p->n_rho > 0 && p->distance == p->distance &&
+           p->plane_stride >= 0 && p->omega_stride >= p->n_r;
+}
+
+}  // namespace hk
+}  // namespace mma

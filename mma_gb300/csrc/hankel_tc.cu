@@ -1,0 +1,761 @@
+// hankel_tc.cu -- per-plane far-field transforms of many planes on the 5th-generation tensor
+// cores: the split-precision (three-term FP16, FP32 accumulation) form of
+// Hankel/Hankel_transform.py:452-519 as called for every plane by Hankel_long (:523-686) when
+// the cumulative results are requested.
+//
+// For frequency w and plane k (D_k = distance - z_k, y = k_w r rho / d_ref, lambda_k = d_ref/D_k):
+//   P_k[w, rho] = sum_r J0(lambda_k y) A_k[w, r]
+//              = sum_m v_k^m (sigma y / 2)^m J_m(y) / m! ... = sum_m v_k^m C_m[rho, k],
+//   C_m[rho, k] = sum_r K_m[rho, r] A_k[w, r],   K_m(y) = (sigma y/2)^m J_m(y)/m!,
+// (the Bessel multiplication theorem; v_k = (1 - lambda_k^2)/sigma).  Per frequency this is a
+// GEMM with rows (rho, m), inner dimension r and columns (plane, re/im):
+//   * B (the per-plane source tables A_k[w, r], scaled per row to |.| <= 1 and split into FP16
+//     hi + lo) is prepared once by prep_b and read by TMA (64-byte swizzle);
+//   * A (the kernel K_m, scaled per m to |.| <= 1 and split into FP16 hi + lo) is generated in
+//     shared memory by eight CUDA-core warps (J0/J1 seeds, then the recurrence in m);
+//   * one thread issues tcgen05.mma (M = 128, N = 256, K = 16): hi*hi + hi*lo + lo*hi into two
+//     FP32 accumulators in TMEM (two row tiles share each B stage);
+//   * the epilogue reads TMEM, applies v_k^m / s_m, reduces over m across lanes and writes the
+//     requested planes (complex128, [slot][rho][w]).
+// Every mbarrier wait is bounded (time and a CTA-wide abort flag); a timeout sets a status word
+// and the kernel drains its tensor-core work and frees TMEM before returning.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "../../include/mma_diag.h"
+#include "../../include/mma_hankel.h"
+#include "../../include/mma_tdse.h"
+#include "hankel_common.cuh"
+#include "tc_sm100.cuh"
+
+namespace mma {
+namespace hk {
+namespace tcf {
+
+using namespace mma::tc;
+
+constexpr int KB = 32;       // r per K-block: 32 FP16 = one 64-byte swizzled row
+constexpr int NP = 128;      // planes per tile
+constexpr int NCOL = 2 * NP; // accumulator columns per row tile (re, im per plane)
+constexpr int MT = 2;        // row tiles (accumulators) per CTA tile
+constexpr int STAGES = 3;
+constexpr int GWARPS = 8;    // warps of one generator group (16 half-warps: 16 rho rows per pass)
+constexpr int NGEN = 2 * GWARPS;  // two groups take alternate K-blocks; all of them run the epilogue
+constexpr int THREADS = 32 * (2 + NGEN);
+constexpr uint32_t A_BYTES = 128 * KB * 2;  // one row tile, hi or lo: 8 KB
+constexpr uint32_t B_BYTES = NCOL * KB * 2; // hi or lo: 16 KB
+constexpr uint32_t B_OFF = MT * 2 * A_BYTES;
+constexpr uint32_t STAGE_BYTES = B_OFF + 2 * B_BYTES;  // 64 KB
+constexpr uint64_t WAIT_NS = 2000000000ull;             // 2 s per wait
+
+struct Params {
+    int64_t n_omega, n_r, n_z, n_rho;
+    int64_t rpad, zpad;       // r padded to KB, planes padded to NP
+    int64_t n_tiles, n_pb, n_rb;
+    double inv_cd;            // 1 / (c d_ref): y = w r rho inv_cd
+    float sigma;
+    const double* og;
+    const double* rg;
+    const double* rho;
+    const float* alpha;       // [n_omega][zpad]: scale of B rows (both re and im of plane k)
+    const float* ftab;        // [MM][zpad]: v_k^m / s_m
+    const int64_t* slot;      // [n_z]
+    double* planes;           // [n_planes][n_rho][n_omega] complex128
+    int* status;
+    const float2* rgf;        // [rpad] r as float-float (0 beyond n_r)
+    float inv_ymax, two_over_ymax;
+};
+
+__device__ __forceinline__ void fail(volatile int* abort_s, int* status, int code)
+{
+    *abort_s = 1;
+    atomicCAS(status, 0, code);
+}
+
+// reduce-scatter over G lanes of CH values: afterwards lane g of each group holds the group sum
+// of columns (g % G) * (CH / G) + j, j < CH / G, in v[j]
+template <int G, int CH>
+__device__ __forceinline__ void reduce_scatter(float (&v)[CH], int lane)
+{
+    int n = CH;
+#pragma unroll
+    for (int d = G / 2; d >= 1; d >>= 1) {
+        const bool up = (lane & d) != 0;
+        const int h = n / 2;
+#pragma unroll
+        for (int i = 0; i < CH / 2; i++) {
+            if (i < h) {
+                const float send = up ? v[i] : v[i + h];
+                const float keep = up ? v[i + h] : v[i];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, send, d);
+            }
+        }
+        n = h;
+    }
+}
+
+template <int MM>
+__global__ void __launch_bounds__(THREADS, 1)
+    planes_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo, Params P)
+{
+    constexpr int RT = 128 / MM;  // rho per row tile
+    constexpr int RC = MT * RT;   // rho per CTA tile
+    constexpr int CH = MM > 16 ? MM : 16;  // accumulator columns per epilogue step
+    static_assert(RC % 8 == 0, "rho rows per tile");
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+    uint64_t* full = bars;
+    uint64_t* empty = bars + STAGES;
+    uint64_t* acc_full = bars + 2 * STAGES;
+    uint64_t* acc_empty = acc_full + 1;
+    uint64_t* drain = acc_full + 2;
+    uint32_t* tmem_s = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort_s = reinterpret_cast<volatile int*>(tmem_s + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nkb = (int)(P.rpad / KB);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(&full[s], 1 + GWARPS);  // the producer + the generating group
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(acc_full, 1);
+        mbar_init(acc_empty, NGEN);
+        mbar_init(drain, 1);
+        *abort_s = 0;
+        fence_barrier_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(tmem_s, 512);
+        tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        tma_prefetch(&tm_hi);
+        tma_prefetch(&tm_lo);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_s;
+
+    if (warp == 0) {
+        // ---------------------------------------------------------------- TMA producer (B)
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int64_t tile = blockIdx.x; ok && tile < P.n_tiles; tile += gridDim.x) {
+                const int64_t o = tile / (P.n_pb * P.n_rb), pb = (tile / P.n_rb) % P.n_pb;
+                for (int kb = 0; kb < nkb; kb++, it++) {
+                    const uint32_t s = it % STAGES, ph = (it / STAGES) & 1u;
+                    if (!mbar_wait(&empty[s], ph ^ 1u, abort_s, WAIT_NS)) {
+                        fail(abort_s, P.status, 1);
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* st = smem + s * STAGE_BYTES + B_OFF;
+                    mbar_arrive_expect_tx(&full[s], 2 * B_BYTES);
+                    tma_load_3d(st, &tm_hi, &full[s], kb * KB, (int)(pb * NCOL), (int)o);
+                    tma_load_3d(st + B_BYTES, &tm_lo, &full[s], kb * KB, (int)(pb * NCOL), (int)o);
+                }
+            }
+            if (!ok) {  // let copies already issued land before the CTA leaves
+                const uint64_t t0 = global_ns();
+                while (global_ns() - t0 < 200000ull) {
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_f16_f32(128, NCOL);
+            uint32_t it = 0, tt = 0;
+            bool ok = true;
+            const uint32_t sbase = smem_u32(smem);
+            for (int64_t tile = blockIdx.x; ok && tile < P.n_tiles; tile += gridDim.x, tt++) {
+                if (!mbar_wait(acc_empty, (tt & 1u) ^ 1u, abort_s, WAIT_NS)) {
+                    fail(abort_s, P.status, 2);
+                    break;
+                }
+                tc_fence_after();
+                for (int kb = 0; kb < nkb; kb++, it++) {
+                    const uint32_t s = it % STAGES, ph = (it / STAGES) & 1u;
+                    if (!mbar_wait(&full[s], ph, abort_s, WAIT_NS)) {
+                        fail(abort_s, P.status, 3);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t st = sbase + s * STAGE_BYTES;
+#pragma unroll
+                    for (int ks = 0; ks < KB / 16; ks++) {
+                        const uint64_t bh = sdesc_sw64(st + B_OFF + ks * 32);
+                        const uint64_t bl = sdesc_sw64(st + B_OFF + B_BYTES + ks * 32);
+#pragma unroll
+                        for (int mt = 0; mt < MT; mt++) {
+                            const uint64_t ah = sdesc_sw64(st + mt * 2 * A_BYTES + ks * 32);
+                            const uint64_t al = sdesc_sw64(st + mt * 2 * A_BYTES + A_BYTES + ks * 32);
+                            const uint32_t d = tmem + (uint32_t)(mt * NCOL);
+                            mma_f16(d, ah, bh, idesc, (kb | ks) != 0);
+                            mma_f16(d, ah, bl, idesc, 1u);
+                            mma_f16(d, al, bh, idesc, 1u);
+                        }
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (ok) mma_commit(acc_full);
+            }
+            mma_commit(drain);  // all MMAs of this CTA complete before TMEM is freed
+            if (!mbar_wait(drain, 0u, abort_s, WAIT_NS)) fail(abort_s, P.status, 4);
+        }
+        __syncwarp();
+    } else {
+        // ---------------------------------------------------------------- generators + epilogue
+        const int gw = warp - 2;
+        const int grp = gw / GWARPS, gw8 = gw % GWARPS;  // generator group (alternate K-blocks), warp in it
+        const int hw = lane >> 4, k0 = 2 * (lane & 15);  // half-warp -> rho row; lane -> r pair (k0, k0+1)
+        constexpr int PASSES = (RC + 2 * GWARPS - 1) / (2 * GWARPS);
+        uint32_t it = 0, tt = 0;
+        bool ok = true;
+        const float tw = P.two_over_ymax, iy = P.inv_ymax;
+        for (int64_t tile = blockIdx.x; ok && tile < P.n_tiles; tile += gridDim.x, tt++) {
+            const int64_t o = tile / (P.n_pb * P.n_rb), pb = (tile / P.n_rb) % P.n_pb, rb = tile % P.n_rb;
+            const double kap = P.og[o] * P.inv_cd;
+            float kh[PASSES], kl[PASSES];  // k rho / d_ref of this half-warp's rows (float-float)
+#pragma unroll
+            for (int j = 0; j < PASSES; j++) {
+                const int q = gw8 + GWARPS * (2 * j + hw);
+                const int64_t ig = rb * RC + q;
+                split_d((q < RC && ig < P.n_rho) ? kap * P.rho[ig] : 0.0, kh[j], kl[j]);
+            }
+            for (int kb = 0; kb < nkb; kb++, it++) {
+                if ((int)(it & 1u) != grp) continue;  // the other group generates this K-block
+                const uint32_t s = it % STAGES, ph = (it / STAGES) & 1u;
+                // r and r+1 as float-float (hi0, lo0, hi1, lo1), loaded before the wait
+                const float4 rv = __ldg(reinterpret_cast<const float4*>(P.rgf) + ((int64_t)kb * KB + k0) / 2);
+                if (!mbar_wait(&empty[s], ph ^ 1u, abort_s, WAIT_NS)) {
+                    fail(abort_s, P.status, 5);
+                    ok = false;
+                    break;
+                }
+                uint8_t* st = smem + s * STAGE_BYTES;
+#pragma unroll
+                for (int j = 0; j < PASSES; j++) {
+                    const int q = gw8 + GWARPS * (2 * j + hw);  // rho row within the CTA tile
+                    if (q >= RC) continue;                   // uniform per half-warp
+                    const int mt = q / RT, rloc = q % RT;
+                    uint8_t* ah = st + mt * 2 * A_BYTES;
+                    uint8_t* al = ah + A_BYTES;
+                    const float y0h = kh[j] * rv.x, y0l = fmaf(kh[j], rv.x, -y0h) + fmaf(kh[j], rv.y, kl[j] * rv.x);
+                    const float y1h = kh[j] * rv.z, y1l = fmaf(kh[j], rv.z, -y1h) + fmaf(kh[j], rv.w, kl[j] * rv.z);
+                    float J00, J10, J01, J11;
+                    bessel01<true>(y0h, y0l, J00, J10);
+                    bessel01<true>(y1h, y1l, J01, J11);
+                    // K^_m = u^m J_m(y), u = y / y_max <= 1:  K^_{m+1} = (2m / y_max) K^_m - u^2 K^_{m-1}
+                    const float u0 = (y0h + y0l) * iy, u1 = (y1h + y1l) * iy;
+                    const float w0 = u0 * u0, w1 = u1 * u1;
+                    auto put2 = [&](int m, float x0, float x1) {
+                        const __half2 h = __floats2half2_rn(x0, x1);
+                        const float2 f = __half22float2(h);
+                        const __half2 l = __floats2half2_rn(x0 - f.x, x1 - f.y);
+                        const uint32_t off = sw64_offset((uint32_t)(rloc * MM + m), (uint32_t)k0);
+                        *reinterpret_cast<__half2*>(ah + off) = h;
+                        *reinterpret_cast<__half2*>(al + off) = l;
+                    };
+                    float a0 = J00, b0 = u0 * J10, a1 = J01, b1 = u1 * J11;
+                    put2(0, a0, a1);
+                    put2(1, b0, b1);
+#pragma unroll
+                    for (int m = 1; m + 1 < MM; m++) {
+                        const float c = (float)m * tw;
+                        const float n0 = fmaf(c, b0, -w0 * a0), n1 = fmaf(c, b1, -w1 * a1);
+                        put2(m + 1, n0, n1);
+                        a0 = b0;
+                        b0 = n0;
+                        a1 = b1;
+                        b1 = n1;
+                    }
+                }
+                fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[s]);
+            }
+            if (!ok) break;
+            // ------------------------------------------------------------ epilogue of this tile
+            if (!mbar_wait(acc_full, tt & 1u, abort_s, WAIT_NS)) {
+                fail(abort_s, P.status, 6);
+                break;
+            }
+            tc_fence_after();
+            // per-plane factors straight from global memory (ftab[m][plane], small and cached): no
+            // CTA-wide barrier here.  Group grp takes columns [grp * NCOL/2, (grp + 1) * NCOL/2).
+            const int mt = gw8 / 4, qd = warp % 4;
+            const int row = qd * 32 + lane;
+            const int m = row % MM;
+            const float* fm = P.ftab + (int64_t)m * P.zpad + pb * NP;
+            const int64_t ig = rb * RC + mt * RT + row / MM;
+            for (int c0 = grp * (NCOL / 2); c0 < (grp + 1) * (NCOL / 2); c0 += CH) {
+                float v[CH];
+                {
+                    float t16[16];
+                    const uint32_t ta = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(mt * NCOL + c0);
+                    tmem_ld16(ta, t16);
+#pragma unroll
+                    for (int j = 0; j < 16; j++) v[j] = t16[j];
+                    if constexpr (CH > 16) {
+                        tmem_ld16(ta + 16, t16);
+#pragma unroll
+                        for (int j = 0; j < 16; j++) v[(16 + j) % CH] = t16[j];
+                    }
+                }
+                float f[CH / 2];  // factors of the CH / 2 planes of these columns
+#pragma unroll
+                for (int q4 = 0; q4 < CH / 8; q4++) {
+                    const float4 f4 = __ldg(reinterpret_cast<const float4*>(fm + (c0 >> 1)) + q4);
+                    f[4 * q4] = f4.x;
+                    f[4 * q4 + 1] = f4.y;
+                    f[4 * q4 + 2] = f4.z;
+                    f[4 * q4 + 3] = f4.w;
+                }
+#pragma unroll
+                for (int j = 0; j < CH; j++) v[j] *= f[j >> 1];
+                reduce_scatter<MM, CH>(v, lane);
+#pragma unroll
+                for (int j = 0; j < CH / MM; j++) {
+                    const int col = c0 + (lane % MM) * (CH / MM) + j;
+                    const int64_t kz = pb * NP + (col >> 1);
+                    if (kz < P.n_z && ig < P.n_rho) {
+                        const int64_t sl = __ldg(P.slot + kz);
+                        if (sl >= 0)
+                            P.planes[((sl * P.n_rho + ig) * P.n_omega + o) * 2 + (col & 1)] =
+                                (double)(v[j] * __ldg(P.alpha + o * P.zpad + kz));
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 512);
+    }
+}
+
+// B operand: per (w, plane k) row the plane table A_k[w, r] = pre_k(w) e^{-i k r^2/(2 D_k)} r wr S_k[w, r]
+// (FP32, float-float phase), scaled by 1/alpha (alpha = max over r of |Re|, |Im|) and split into
+// FP16 hi + lo: Bh/Bl[w][2k + c][r], r padded to rpad, planes to zpad (zeros).
+// One CTA per frequency; each thread owns r pairs.
+constexpr int PREP_THREADS = 256;
+constexpr int PREP_PAIRS = 2;  // rpad <= 2 * 2 * 256 = 1024
+
+__global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, const double* og, const double* rg,
+                                                       const float2* dinv, const void* src, const double2* pre,
+                                                       __half* Bh, __half* Bl, float* alpha, int64_t rpad,
+                                                       int64_t zpad)
+{
+    __shared__ float wmax[2][PREP_THREADS / 32];
+    const int64_t o = blockIdx.x, Nr = P.n_r, No = P.n_omega;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    float kh, kl;
+    split_d(og[o] / kC, kh, kl);
+    float kr2h[2 * PREP_PAIRS], kr2l[2 * PREP_PAIRS], wr[2 * PREP_PAIRS];
+#pragma unroll
+    for (int i = 0; i < 2 * PREP_PAIRS; i++) {
+        const int64_t r = 2 * (t + (int64_t)PREP_THREADS * (i / 2)) + (i & 1);
+        kr2h[i] = kr2l[i] = wr[i] = 0.f;
+        if (r < Nr) {
+            const double rr = rg[r];
+            float r2h, r2l;
+            split_d(rr * rr, r2h, r2l);
+            kr2h[i] = kh * r2h;
+            kr2l[i] = fmaf(kh, r2h, -kr2h[i]) + fmaf(kh, r2l, kl * r2h);
+            wr[i] = (float)(trap_w(rg, r, Nr) * rr);
+        }
+    }
+    for (int64_t kz = 0; kz < zpad; kz++) {
+        float2 a[2 * PREP_PAIRS];
+        float mx = 0.f;
+        const bool live = kz < P.n_z;
+        const double2 pf = (live && pre) ? pre[kz * No + o] : make_double2(1.0, 0.0);
+        const float2 pr = make_float2((float)pf.x, (float)pf.y);
+        const float2 di = live ? dinv[kz] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < 2 * PREP_PAIRS; i++) {
+            const int64_t r = 2 * (t + (int64_t)PREP_THREADS * (i / 2)) + (i & 1);
+            a[i] = make_float2(0.f, 0.f);
+            if (live && r < Nr) {
+                const float2 sv = load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r, P.source_c128);
+                float2 v = make_float2(fmaf(pr.x, sv.x, -pr.y * sv.y), fmaf(pr.x, sv.y, pr.y * sv.x));
+                if (P.near_field) {
+                    const float th = kr2h[i] * di.x;
+                    const float te = fmaf(kr2h[i], di.x, -th) + fmaf(kr2h[i], di.y, kr2l[i] * di.x);
+                    float sn, cs;
+                    sincosf(reduce_2pi(th, te), &sn, &cs);  // e^{-i theta}
+                    v = make_float2(fmaf(v.x, cs, v.y * sn), fmaf(v.y, cs, -v.x * sn));
+                }
+                a[i] = make_float2(v.x * wr[i], v.y * wr[i]);
+                mx = fmaxf(mx, fmaxf(fabsf(a[i].x), fabsf(a[i].y)));
+            }
+        }
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+        const int par = (int)(kz & 1);
+        if (lane == 0) wmax[par][w] = mx;
+        __syncthreads();
+        float al = 0.f;
+#pragma unroll
+        for (int q = 0; q < PREP_THREADS / 32; q++) al = fmaxf(al, wmax[par][q]);
+        const float sc = al > 0.f ? 1.0f / al : 0.f;
+        if (t == 0) alpha[o * zpad + kz] = al;
+#pragma unroll
+        for (int p = 0; p < PREP_PAIRS; p++) {
+            const int64_t r0 = 2 * (t + (int64_t)PREP_THREADS * p);
+            if (r0 >= rpad) continue;
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                const float x0 = (c ? a[2 * p].y : a[2 * p].x) * sc;
+                const float x1 = (c ? a[2 * p + 1].y : a[2 * p + 1].x) * sc;
+                const __half h0 = __float2half_rn(x0), h1 = __float2half_rn(x1);
+                const __half l0 = __float2half_rn(x0 - __half2float(h0)), l1 = __float2half_rn(x1 - __half2float(h1));
+                const int64_t idx = ((o * 2 * zpad + 2 * kz + c) * rpad + r0) / 2;
+                reinterpret_cast<__half2*>(Bh)[idx] = __halves2half2(h0, h1);
+                reinterpret_cast<__half2*>(Bl)[idx] = __halves2half2(l0, l1);
+            }
+        }
+    }
+}
+
+// per plane: dinv = 1/(2 D_k) as (hi, lo); ftab[m][k] = v_k^m / s_m = (v_k x)^m / m!, x = sigma y_max / 2;
+// per radius: rgf = r as float-float
+__global__ void plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, const double* zg, const double* rg,
+                            int mm, int64_t zpad, int64_t rpad, float2* dinv, float* ftab, float2* rgf)
+{
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < rpad; q += (int64_t)gridDim.x * blockDim.x) {
+        float hi, lo;
+        split_d(q < P.n_r ? rg[q] : 0.0, hi, lo);
+        rgf[q] = make_float2(hi, lo);
+    }
+    const double x = 0.5 * F.sigma * F.y_max;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < zpad; q += (int64_t)gridDim.x * blockDim.x) {
+        if (q >= P.n_z) {
+            for (int m = 0; m < mm; m++) ftab[m * zpad + q] = 0.f;
+            continue;
+        }
+        const double D = P.distance - zg[q];
+        const double lam = F.d_ref / D;
+        const double v = (1.0 - lam * lam) / F.sigma;
+        double c = 1.0;
+        for (int m = 0; m < mm; m++) {
+            ftab[m * zpad + q] = (float)c;
+            c *= (x > 0.0 ? v * x : v) / (double)(m + 1);
+        }
+        float hi, lo;
+        split_d(1.0 / (2.0 * D), hi, lo);
+        dinv[q] = make_float2(hi, lo);
+    }
+}
+
+// ------------------------------------------------------------------------ self-test
+// One tile: D[128 x 256] = A[128 x 32] * B[256 x 32]^T in FP16 -> FP32, A staged by threads into
+// the SW64 layout, B by threads or by TMA.  Checks descriptors, swizzle and the TMEM mapping.
+__global__ void __launch_bounds__(128) tc_selftest_kernel(const __grid_constant__ CUtensorMap tm_b, const __half* A,
+                                                          const __half* B, float* D, int use_tma, int* status)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + 128 * 64;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sB + 256 * 64);
+    uint32_t* tmem_s = reinterpret_cast<uint32_t*>(bars + 2);
+    volatile int* abort_s = reinterpret_cast<volatile int*>(tmem_s + 1);
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    for (int i = t; i < 128 * 32; i += 128)
+        *reinterpret_cast<__half*>(sA + sw64_offset(i / 32, i % 32)) = A[i];
+    if (!use_tma)
+        for (int i = t; i < 256 * 32; i += 128)
+            *reinterpret_cast<__half*>(sB + sw64_offset(i / 32, i % 32)) = B[i];
+    if (t == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        *abort_s = 0;
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_s, 256);
+        tmem_relinquish();
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_s;
+    bool ok = true;
+    if (t == 0) {
+        if (use_tma) {
+            mbar_arrive_expect_tx(&bars[0], 256 * 64);
+            tma_load_3d(sB, &tm_b, &bars[0], 0, 0, 0);
+            if (!mbar_wait(&bars[0], 0u, abort_s, WAIT_NS)) {
+                fail(abort_s, status, 1);
+                ok = false;
+            }
+        }
+        if (ok) {
+            constexpr uint32_t idesc = idesc_f16_f32(128, 256);
+            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+            for (int ks = 0; ks < 2; ks++) mma_f16(tmem, sdesc_sw64(a0 + ks * 32), sdesc_sw64(b0 + ks * 32), idesc, ks > 0);
+        }
+        mma_commit(&bars[1]);
+    }
+    __syncthreads();
+    if (!mbar_wait(&bars[1], 0u, abort_s, WAIT_NS)) fail(abort_s, status, 2);
+    tc_fence_after();
+    if (!*abort_s) {
+        for (int c0 = 0; c0 < 256; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+            for (int j = 0; j < 16; j++) D[(warp * 32 + lane) * 256 + c0 + j] = v[j];
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 256);
+    }
+}
+
+// ------------------------------------------------------------------------ host helpers
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder()
+{
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
+// 3-D FP16 tensor [d2][d1][d0] (d0 contiguous), box {32, rows, 1}, 64-byte swizzle
+bool make_map(CUtensorMap* map, const void* base, uint64_t d0, uint64_t d1, uint64_t d2, uint32_t rows)
+{
+    EncodeTiled enc = encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {d0, d1, d2};
+    const cuuint64_t strides[2] = {d0 * 2, d0 * d1 * 2};
+    const cuuint32_t box[3] = {32, rows, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void*>(base), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int tc_terms(int64_t n_terms)
+{
+    for (int c : {8, 16, 32})
+        if (n_terms <= c) return c;
+    return -1;
+}
+
+struct Layout {
+    int mm;
+    int64_t rpad, zpad;
+    size_t off_bh, off_bl, off_alpha, off_ftab, off_dinv, off_rgf, off_status, total;
+};
+
+size_t up256(size_t x) { return (x + 255) / 256 * 256; }
+
+bool layout(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, Layout& L)
+{
+    L.mm = tc_terms(plan->n_terms);
+    if (L.mm < 0) return false;
+    L.rpad = (p->n_r + KB - 1) / KB * KB;
+    L.zpad = (p->n_z + NP - 1) / NP * NP;
+    if (L.rpad > 2 * 2 * PREP_THREADS) return false;
+    const size_t nb = (size_t)p->n_omega * 2 * L.zpad * L.rpad * sizeof(__half);
+    L.off_bh = 0;
+    L.off_bl = up256(nb);
+    L.off_alpha = L.off_bl + up256(nb);
+    L.off_ftab = L.off_alpha + up256(sizeof(float) * p->n_omega * L.zpad);
+    L.off_dinv = L.off_ftab + up256(sizeof(float) * L.zpad * L.mm);
+    L.off_rgf = L.off_dinv + up256(sizeof(float2) * L.zpad);
+    L.off_status = L.off_rgf + up256(sizeof(float2) * L.rpad);
+    L.total = L.off_status + 256;
+    return true;
+}
+
+size_t planes_smem() { return 1024 + STAGES * STAGE_BYTES + 256; }  // alignment slack, stages, barriers
+
+template <int MM>
+int launch_planes(const CUtensorMap& th, const CUtensorMap& tl, const Params& P, cudaStream_t st)
+{
+    const size_t smem = planes_smem();
+    if (cudaFuncSetAttribute(planes_tc_kernel<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return MMA_ERR_CUDA;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = P.n_tiles < sms ? P.n_tiles : sms;
+    planes_tc_kernel<MM><<<(unsigned)grid, THREADS, smem, st>>>(th, tl, P);
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
+
+}  // namespace tcf
+}  // namespace hk
+}  // namespace mma
+
+using namespace mma::hk;
+using namespace mma::hk::tcf;
+
+extern "C" size_t mma_hankel_planes_tc_scratch_bytes(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
+{
+    Layout L;
+    if (!p || !plan || !layout(p, plan, L)) return 0;
+    return L.total;
+}
+
+namespace {
+// checks shared by the entry points; fills the scratch layout
+int tc_check(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, const double* ogrid, const double* rgrid,
+             void* scratch, size_t scratch_bytes, Layout& L)
+{
+    if (!valid(p) || !plan || !ogrid || !rgrid) return MMA_ERR_ARG;
+    if (!(plan->sigma > 0.0) || !(plan->d_ref > 0.0)) return MMA_ERR_ARG;
+    if (!layout(p, plan, L)) return MMA_ERR_UNSUPPORTED;
+    if (!scratch || scratch_bytes < L.total || (reinterpret_cast<uintptr_t>(scratch) & 255)) return MMA_ERR_ARG;
+    if (p->n_omega > 2147483647LL || 2 * L.zpad > 2147483647LL) return MMA_ERR_TOO_LARGE;
+    return MMA_OK;
+}
+}  // namespace
+
+extern "C" int mma_hankel_planes_tc_prepare(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
+                                            const double* ogrid, const double* rgrid, const double* zgrid,
+                                            const void* source, const double* pre, void* scratch,
+                                            size_t scratch_bytes, void* stream)
+{
+    Layout L;
+    const int rc = tc_check(p, plan, ogrid, rgrid, scratch, scratch_bytes, L);
+    if (rc != MMA_OK) return rc;
+    if (!zgrid || !source) return MMA_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    char* sc = static_cast<char*>(scratch);
+    const int64_t nt = L.zpad > L.rpad ? L.zpad : L.rpad;
+    plane_table<<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(*p, *plan, zgrid, rgrid, L.mm, L.zpad, L.rpad,
+                                                               reinterpret_cast<float2*>(sc + L.off_dinv),
+                                                               reinterpret_cast<float*>(sc + L.off_ftab),
+                                                               reinterpret_cast<float2*>(sc + L.off_rgf));
+    prep_b<<<(unsigned)p->n_omega, PREP_THREADS, 0, st>>>(
+        *p, ogrid, rgrid, reinterpret_cast<const float2*>(sc + L.off_dinv), source,
+        reinterpret_cast<const double2*>(pre), reinterpret_cast<__half*>(sc + L.off_bh),
+        reinterpret_cast<__half*>(sc + L.off_bl), reinterpret_cast<float*>(sc + L.off_alpha), L.rpad, L.zpad);
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
+
+extern "C" int mma_hankel_planes_tc_run(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
+                                        const double* ogrid, const double* rgrid, const double* rho,
+                                        const int64_t* plane_slot, int n_planes, double* planes, void* scratch,
+                                        size_t scratch_bytes, void* stream)
+{
+    Layout L;
+    const int rc0 = tc_check(p, plan, ogrid, rgrid, scratch, scratch_bytes, L);
+    if (rc0 != MMA_OK) return rc0;
+    if (!rho || !plane_slot || !planes || n_planes < 1) return MMA_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    char* sc = static_cast<char*>(scratch);
+    int* status = reinterpret_cast<int*>(sc + L.off_status);
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+    CUtensorMap th, tl;
+    if (!make_map(&th, sc + L.off_bh, (uint64_t)L.rpad, (uint64_t)(2 * L.zpad), (uint64_t)p->n_omega, NCOL) ||
+        !make_map(&tl, sc + L.off_bl, (uint64_t)L.rpad, (uint64_t)(2 * L.zpad), (uint64_t)p->n_omega, NCOL))
+        return MMA_ERR_CUDA;
+    Params P;
+    std::memset(&P, 0, sizeof(P));
+    P.n_omega = p->n_omega;
+    P.n_r = p->n_r;
+    P.n_z = p->n_z;
+    P.n_rho = p->n_rho;
+    P.rpad = L.rpad;
+    P.zpad = L.zpad;
+    const int rc = MT * (128 / L.mm);
+    P.n_pb = L.zpad / NP;
+    P.n_rb = (p->n_rho + rc - 1) / rc;
+    P.n_tiles = p->n_omega * P.n_pb * P.n_rb;
+    P.inv_cd = 1.0 / (kC * plan->d_ref);
+    P.sigma = (float)plan->sigma;
+    P.og = ogrid;
+    P.rg = rgrid;
+    P.rho = rho;
+    P.alpha = reinterpret_cast<const float*>(sc + L.off_alpha);
+    P.ftab = reinterpret_cast<const float*>(sc + L.off_ftab);
+    P.slot = plane_slot;
+    P.planes = planes;
+    P.status = status;
+    P.rgf = reinterpret_cast<const float2*>(sc + L.off_rgf);
+    P.inv_ymax = plan->y_max > 0.0 ? (float)(1.0 / plan->y_max) : 0.f;
+    P.two_over_ymax = plan->y_max > 0.0 ? (float)(2.0 / plan->y_max) : 0.f;
+    switch (L.mm) {
+        case 8: return launch_planes<8>(th, tl, P, st);
+        case 16: return launch_planes<16>(th, tl, P, st);
+        case 32: return launch_planes<32>(th, tl, P, st);
+        default: return MMA_ERR_UNSUPPORTED;
+    }
+}
+
+extern "C" int mma_hankel_planes_tc(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
+                                    const double* ogrid, const double* rgrid, const double* zgrid, const double* rho,
+                                    const void* source, const double* pre, const int64_t* plane_slot, int n_planes,
+                                    double* planes, void* scratch, size_t scratch_bytes, void* stream)
+{
+    const int rc = mma_hankel_planes_tc_prepare(p, plan, ogrid, rgrid, zgrid, source, pre, scratch, scratch_bytes,
+                                                stream);
+    if (rc != MMA_OK) return rc;
+    return mma_hankel_planes_tc_run(p, plan, ogrid, rgrid, rho, plane_slot, n_planes, planes, scratch, scratch_bytes,
+                                    stream);
+}
+
+extern "C" int mma_hankel_planes_tc_status(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
+                                           const void* scratch, void* stream)
+{
+    Layout L;
+    if (!p || !plan || !scratch || !layout(p, plan, L)) return MMA_ERR_ARG;
+    int h = 0;
+    if (cudaMemcpyAsync(&h, static_cast<const char*>(scratch) + L.off_status, sizeof(int), cudaMemcpyDeviceToHost,
+                        (cudaStream_t)stream) != cudaSuccess ||
+        cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+        return MMA_ERR_CUDA;
+    return h == 0 ? MMA_OK : MMA_ERR_TIMEOUT;
+}
+
+extern "C" int mma_tc_selftest(const void* A, const void* B, float* D, int use_tma, int* status, void* stream)
+{
+    if (!A || !B || !D || !status) return MMA_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUtensorMap tb;
+    std::memset(&tb, 0, sizeof(tb));
+    if (use_tma && !make_map(&tb, B, 32, 256, 1, 256)) return MMA_ERR_CUDA;
+    const size_t smem = 1024 + 128 * 64 + 256 * 64 + 64;
+    if (cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return MMA_ERR_CUDA;
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+    tc_selftest_kernel<<<1, 128, smem, st>>>(tb, static_cast<const __half*>(A), static_cast<const __half*>(B), D,
+                                              use_tma, status);
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}

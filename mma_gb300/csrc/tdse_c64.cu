@@ -53,7 +53,8 @@ __device__ __forceinline__ cf shdn(cf v, int d)
 // Table slots (floats), each L = 256*M long, site j = t*M + i at q = i*256 + t.
 enum { T_IBRE = 0, T_IBIM, T_V, T_PSI0, T_SLOTS };
 
-// forward scan of Y_t = b_t + c_t Y_{t-1} over the CTA, exclusive (see tdse_solver.cuh)
+// forward scan of Y_t = b_t + c_t Y_{t-1} over the CTA of NW warps, exclusive (see tdse_solver.cuh)
+template <int NW = kWarps>
 __device__ __forceinline__ cf scan_fwd(cf c, cf b, cf* sc, cf* sb)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -71,12 +72,13 @@ __device__ __forceinline__ cf scan_fwd(cf c, cf b, cf* sc, cf* sb)
     }
     __syncthreads();
     cf yw{0.f, 0.f};
-    for (int q = 0; q < kWarps; q++)
+    for (int q = 0; q < NW; q++)
         if (q < w) yw = cfma(sc[q], yw, sb[q]);
     cf cp = shup(c, 1), bp = shup(b, 1);
     return lane == 0 ? yw : cfma(cp, yw, bp);
 }
 
+template <int NW = kWarps>
 __device__ __forceinline__ cf scan_bwd(cf c, cf b, cf* sc, cf* sb)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -94,7 +96,7 @@ __device__ __forceinline__ cf scan_bwd(cf c, cf b, cf* sc, cf* sb)
     }
     __syncthreads();
     cf uw{0.f, 0.f};
-    for (int q = kWarps - 1; q >= 0; q--)
+    for (int q = NW - 1; q >= 0; q--)
         if (q > w) uw = cfma(sc[q], uw, sb[q]);
     cf cp = shdn(c, 1), bp = shdn(b, 1);
     return lane == 31 ? uw : cfma(cp, uw, bp);
@@ -155,6 +157,12 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
         const mma_tdse_instance I = P.insts[inst];
         const mma_tdse_grid G = P.grids[I.grid];
         const int64_t n = G.n, S = I.n_steps;
+        if (G.m32 != M || (G.c64_threads ? G.c64_threads : kThreads) != kThreads) {  // tables of another shape
+            for (int64_t q = t; q < 6 * (S + 1); q += kThreads)
+                P.outputs[I.out_off + q] = __longlong_as_double(0x7ff8000000000000LL);
+            __syncthreads();
+            continue;
+        }
         // ---- tables into shared memory when the grid changes
         if (s_grid != I.grid) {
             for (int q = t; q < T_SLOTS * L; q += kThreads) tab[q] = G.c64_tab[q];
@@ -447,22 +455,26 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
     }
 }
 
-// Shared-memory form for M <= 32 (grids up to 8192 sites): the wavefunction lives in shared
-// memory next to the tables (24 bytes per site), which leaves registers for the chunk products
-// F and G, so each sweep runs once (three passes per step); the population window is summed
-// from shared memory by the threads whose chunk meets it; the observables use blocked
-// two-sum accumulation (8 sites in FP32, then an error-free update of a float-float pair).
-template <int M>
-__global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
+// Shared-memory form for T threads x M sites (T*M*24 bytes of shared memory: T = 256 with
+// M <= 32, T = 512 with M <= 16, T = 1024 with M = 8): the wavefunction lives in shared memory
+// next to the tables (24 bytes per site), which leaves registers for the chunk products F and
+// G, so each sweep runs once (three passes per step); the population window is summed from
+// shared memory by the threads whose chunk meets it; the observables use blocked two-sum
+// accumulation (8 sites in FP32, then an error-free update of a float-float pair).  The CTA
+// size T is chosen per grid (the tables are laid out for it); more threads per instance hide
+// more latency at the price of wider scans.
+template <int M, int T>
+__global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
 {
+    constexpr int NW = T / 32;
     extern __shared__ float tab[];  // T_SLOTS * L floats, then psi [L] complex float
-    __shared__ cf sc[2 * kWarps], sb[2 * kWarps];
-    __shared__ float red_hi[kWarps * 4], red_lo[kWarps * 4], red_pi[kWarps];
+    __shared__ cf sc[2 * NW], sb[2 * NW];
+    __shared__ float red_hi[NW * 4], red_lo[NW * 4], red_pi[NW];
     __shared__ cf wtab[M];
     __shared__ float s_ahi, s_alo;
     __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    constexpr int L = kThreads * M;
+    constexpr int L = T * M;
     cf* psi = reinterpret_cast<cf*>(tab + T_SLOTS * L);
     if (t == 0) s_grid = -1;
 
@@ -474,8 +486,13 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
         const mma_tdse_instance I = P.insts[inst];
         const mma_tdse_grid G = P.grids[I.grid];
         const int64_t n = G.n, S = I.n_steps;
+        if (G.m32 != M || (G.c64_threads ? G.c64_threads : kThreads) != T) {  // tables laid out for another shape
+            for (int64_t q = t; q < 6 * (S + 1); q += T) P.outputs[I.out_off + q] = __longlong_as_double(0x7ff8000000000000LL);
+            __syncthreads();
+            continue;
+        }
         if (s_grid != I.grid)
-            for (int q = t; q < T_SLOTS * L; q += kThreads) tab[q] = G.c64_tab[q];
+            for (int q = t; q < T_SLOTS * L; q += T) tab[q] = G.c64_tab[q];
         __syncthreads();
         if (t == 0) {
             s_grid = I.grid;
@@ -503,7 +520,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
         const float* p0 = tab + T_PSI0 * L;
         const int64_t s0 = (int64_t)t * M;
 #pragma unroll
-        for (int i = 0; i < M; i++) psi[i * kThreads + t] = cf{p0[i * kThreads + t], 0.f};
+        for (int i = 0; i < M; i++) psi[i * T + t] = cf{p0[i * T + t], 0.f};
         const double xs_d = (s0 < n) ? G.x[s0] : 0.0;
         const float xs_hi = (float)xs_d, xs_lo = (float)(xs_d - (double)xs_hi);
         const float dxf = (float)G.dx;
@@ -520,9 +537,9 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
                *o_pint = out + 4 * (S + 1), *o_x = out + 5 * (S + 1);
         {
             double v[1] = {0.0};
-            for (int64_t j = t; j < n; j += kThreads)
+            for (int64_t j = t; j < n; j += T)
                 if (j >= lo && j <= hi) v[0] += G.psi0[2 * j] * G.psi0[2 * j] + G.psi0[2 * j + 1] * G.psi0[2 * j + 1];
-            block_sum<1>(v, reinterpret_cast<double*>(red_hi));
+            block_sum<1, NW>(v, reinterpret_cast<double*>(red_hi));
             if (t == 0) {
                 o_t[0] = I.tmin;
                 o_e[0] = 0.0;
@@ -543,6 +560,12 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
             if (w == 0 && k > 0) {  // observables of the previous step: two-sum over warps, FP64 finish
                 const int c = lane >> 3, q = lane & 7;
                 float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
+                for (int qq = q + 8; qq < NW; qq += 8) {  // warps beyond 8: fold into lanes 0..31 first
+                    float s2, e2;
+                    two_sum(hs, red_hi[qq * 4 + c], s2, e2);
+                    hs = s2;
+                    ls += red_lo[qq * 4 + c] + e2;
+                }
 #pragma unroll
                 for (int d = 4; d >= 1; d >>= 1) {
                     const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
@@ -559,7 +582,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
                 if (lane == 16) o_ptot[k] = fma(pr, pr, pim * pim);
                 if (lane == 24) {
                     float pi_sum = 0.f;
-                    for (int qq = 0; qq < kWarps; qq++) pi_sum += red_pi[qq];
+                    for (int qq = 0; qq < NW; qq++) pi_sum += red_pi[qq];
                     o_pint[k] = (double)pi_sum;
                 }
             }
@@ -569,7 +592,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
                 o_t[k + 1] = tt;
                 o_e[k + 1] = Fk;
             }
-            if (w == kWarps - 1) {
+            if (w == NW - 1) {
                 for (int i = lane; i < M; i += 32) {
                     float sn, cs;
                     sincosf((float)(Fk * dt * G.dx) * (float)i, &sn, &cs);
@@ -583,15 +606,15 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
                 }
             }
             // ---- pass 1: right-hand side 2 M2 psi, local forward sweep, forward products F
-            cf pm = (t == 0) ? cf{0.f, 0.f} : psi[(M - 1) * kThreads + t - 1];
+            cf pm = (t == 0) ? cf{0.f, 0.f} : psi[(M - 1) * T + t - 1];
             cf pc = psi[t];
             cf yprev{0.f, 0.f}, Fp{1.f, 0.f};
 #pragma unroll
             for (int i = 0; i < M; i++) {
-                const int q = i * kThreads + t;
-                const cf pn = (i + 1 < M) ? psi[q + kThreads] : ((t + 1 < kThreads) ? psi[t + 1] : cf{0.f, 0.f});
+                const int q = i * T + t;
+                const cf pn = (i + 1 < M) ? psi[q + T] : ((t + 1 < T) ? psi[t + 1] : cf{0.f, 0.f});
                 const cf r{fmaf(10.f, pc.re, pm.re + pn.re), fmaf(10.f, pc.im, pm.im + pn.im)};
-                const float vl = (i == 0) ? ((t == 0) ? 0.f : vv[(M - 1) * kThreads + t - 1]) : vv[q - kThreads];
+                const float vl = (i == 0) ? ((t == 0) ? 0.f : vv[(M - 1) * T + t - 1]) : vv[q - T];
                 const cf ib{ibre[q], ibim[q]};
                 cf h = off_diag(vl, ib.re, ib.im);
                 if (s0 + i == 0) h = cf{0.f, 0.f};
@@ -602,14 +625,14 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
                 pm = pc;
                 pc = pn;
             }
-            const cf yin = scan_fwd(fg[M - 1], yprev, sc, sb);
+            const cf yin = scan_fwd<NW>(fg[M - 1], yprev, sc, sb);
             // ---- pass 2: forward correction, local backward sweep, backward products G
             cf unext{0.f, 0.f}, Gp{1.f, 0.f};
 #pragma unroll
             for (int i = M - 1; i >= 0; i--) {
-                const int q = i * kThreads + t;
+                const int q = i * T + t;
                 const cf y = cfma(fg[i], yin, yl[i]);
-                const float vr = (i == M - 1) ? ((t == kThreads - 1) ? 0.f : vv[t + 1]) : vv[q + kThreads];
+                const float vr = (i == M - 1) ? ((t == T - 1) ? 0.f : vv[t + 1]) : vv[q + T];
                 cf g = off_diag(vr, ibre[q], ibim[q]);
                 if (s0 + i >= n - 1) g = cf{0.f, 0.f};
                 unext = cfms(g, unext, y);
@@ -617,7 +640,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
                 Gp = cmul(Gp, cf{-g.re, -g.im});
                 fg[i] = Gp;
             }
-            const cf uin = scan_bwd(fg[0], unext, sc + kWarps, sb + kWarps);
+            const cf uin = scan_bwd<NW>(fg[0], unext, sc + NW, sb + NW);
             // ---- pass 3: backward correction, CN update, phase, observables
             const float a_hi = s_ahi, a_lo = s_alo;
             const float th_hi = a_hi * xs_hi;
@@ -632,7 +655,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
             float ahi[4] = {0.f, 0.f, 0.f, 0.f}, alo[4] = {0.f, 0.f, 0.f, 0.f}, part[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int i = 0; i < M; i++) {
-                const int q = i * kThreads + t;
+                const int q = i * T + t;
                 const cf u = cfma(fg[i], uin, yl[i]);
                 const cf d = u - psi[q];
                 const cf pn = cmul(cmul(phs, wtab[i]), d);
@@ -657,7 +680,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
             }
             float pint = 0.f;
             for (int i = win_a; i <= win_b; i++) {  // the few sites of the window (own chunk)
-                const cf p = psi[i * kThreads + t];
+                const cf p = psi[i * T + t];
                 pint = fmaf(p.re, p.re, fmaf(p.im, p.im, pint));
             }
 #pragma unroll
@@ -689,8 +712,8 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
                     double* sp = P.snapshots + I.snap_off + slot * 2 * n;
                     for (int i = 0; i < M; i++)
                         if (s0 + i < n) {
-                            sp[2 * (s0 + i)] = psi[i * kThreads + t].re;
-                            sp[2 * (s0 + i) + 1] = psi[i * kThreads + t].im;
+                            sp[2 * (s0 + i)] = psi[i * T + t].re;
+                            sp[2 * (s0 + i) + 1] = psi[i * T + t].im;
                         }
                 }
             }
@@ -699,6 +722,12 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
         if (w == 0) {  // observables of the last step
             const int c = lane >> 3, q = lane & 7;
             float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
+            for (int qq = q + 8; qq < NW; qq += 8) {
+                float s2, e2;
+                two_sum(hs, red_hi[qq * 4 + c], s2, e2);
+                hs = s2;
+                ls += red_lo[qq * 4 + c] + e2;
+            }
 #pragma unroll
             for (int d = 4; d >= 1; d >>= 1) {
                 const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
@@ -715,7 +744,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
             if (lane == 16) o_ptot[S] = fma(pr, pr, pim * pim);
             if (lane == 24) {
                 float pi_sum = 0.f;
-                for (int qq = 0; qq < kWarps; qq++) pi_sum += red_pi[qq];
+                for (int qq = 0; qq < NW; qq++) pi_sum += red_pi[qq];
                 o_pint[S] = (double)pi_sum;
             }
         }
@@ -723,22 +752,23 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_smem_kernel(Args P)
             double* pf = P.psi_final + I.psi_off;
             for (int i = 0; i < M; i++)
                 if (s0 + i < n) {
-                    pf[2 * (s0 + i)] = psi[i * kThreads + t].re;
-                    pf[2 * (s0 + i) + 1] = psi[i * kThreads + t].im;
+                    pf[2 * (s0 + i)] = psi[i * T + t].re;
+                    pf[2 * (s0 + i) + 1] = psi[i * T + t].im;
                 }
         }
         __syncthreads();
     }
 }
 
-// Complex64 tables from the FP64 grid data, laid out for M32 sites per thread.
+// Complex64 tables from the FP64 grid data, laid out for T = c64_threads threads x M32 sites.
 __global__ void __launch_bounds__(kThreads) build_c64_kernel(const mma_tdse_grid* grids)
 {
     const mma_tdse_grid G = grids[blockIdx.x];
-    const int64_t n = G.n, m = G.m, Lm = m * kThreads, M = G.m32, L = M * kThreads;
+    const int64_t T = G.c64_threads ? G.c64_threads : kThreads;
+    const int64_t n = G.n, m = G.m, Lm = m * kThreads, M = G.m32, L = M * T;
     const cd* ctab = reinterpret_cast<const cd*>(G.cn_tab);
-    for (int64_t q = threadIdx.x; q < L; q += kThreads) {
-        const int64_t i = q / kThreads, t = q % kThreads, j = t * M + i;
+    for (int64_t q = threadIdx.x; q < L; q += blockDim.x) {
+        const int64_t i = q / T, t = q % T, j = t * M + i;
         float v[T_SLOTS] = {0.f, 0.f, 0.f, 0.f};
         if (j < n) {
             const int64_t q64 = (j % m) * kThreads + j / m;  // FP64 table layout
@@ -759,28 +789,43 @@ __global__ void __launch_bounds__(kThreads) build_c64_kernel(const mma_tdse_grid
 
 using namespace mma;
 
+// Shapes (CTA threads T, sites per thread M) the complex64 form has kernels for.
+static bool c64_shape_ok(int64_t T, int64_t M)
+{
+    if (T == kThreads) return M == 8 || M == 16 || M == 24 || M == 32 || M == 40 || M == 48;
+    if (T == 512) return M == 8 || M == 16;
+    if (T == 1024) return M == 8;
+    return false;
+}
+
+extern "C" int mma_tdse_c64_shape_ok(int cta_threads, int m32)
+{
+    return c64_shape_ok(cta_threads ? cta_threads : kThreads, m32) ? 1 : 0;
+}
+
 extern "C" int mma_tdse_build_c64_tables(const mma_tdse_grid* grids_dev, const mma_tdse_grid* grids_host, int n_grids,
                                          void* stream)
 {
     if (n_grids <= 0 || !grids_dev || !grids_host) return MMA_ERR_ARG;
     for (int g = 0; g < n_grids; g++) {
         const mma_tdse_grid& G = grids_host[g];
-        if (!G.c64_tab || G.m32 < G.m || G.m32 > 48 || G.m32 % 8 != 0 || G.m32 * kThreads < G.n) return MMA_ERR_ARG;
+        const int64_t T = G.c64_threads ? G.c64_threads : kThreads;
+        if (!G.c64_tab || !c64_shape_ok(T, G.m32) || G.m32 * T < G.n) return MMA_ERR_ARG;
     }
     c64::build_c64_kernel<<<n_grids, kThreads, 0, (cudaStream_t)stream>>>(grids_dev);
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }
 
 namespace {
-template <int M>
+template <int M, int T>
 int launch_c64(const c64::Args& A, int ctas, cudaStream_t st)
 {
     if constexpr (M <= 32) {  // wavefunction in shared memory next to the tables
-        const size_t smem = (size_t)c64::T_SLOTS * kThreads * M * sizeof(float) + (size_t)kThreads * M * 8;
-        cudaFuncSetAttribute(c64::propagate_c64_smem_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        const size_t smem = (size_t)c64::T_SLOTS * T * M * sizeof(float) + (size_t)T * M * 8;
+        cudaFuncSetAttribute(c64::propagate_c64_smem_kernel<M, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
-        c64::propagate_c64_smem_kernel<M><<<ctas, kThreads, smem, st>>>(A);
-    } else {  // wavefunction in registers, five-pass re-sweep
+        c64::propagate_c64_smem_kernel<M, T><<<ctas, T, smem, st>>>(A);
+    } else {  // wavefunction in registers, five-pass re-sweep (T = 256)
         const size_t smem = (size_t)c64::T_SLOTS * kThreads * M * sizeof(float);
         cudaFuncSetAttribute(c64::propagate_c64_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         c64::propagate_c64_kernel<M><<<ctas, kThreads, smem, st>>>(A);
@@ -789,20 +834,26 @@ int launch_c64(const c64::Args& A, int ctas, cudaStream_t st)
 }
 }  // namespace
 
-// Launch of the complex64 form (called by mma_tdse_propagate for precision 1).
+// Launch of the complex64 form (called by mma_tdse_propagate_ex for precision 1): every
+// instance's grid must have tables of shape (cta_threads, m32).
 extern "C" int mma_tdse_propagate_c64_impl(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
-                                           const mma_tdse_buffers* bufs, int m32, int grid_ctas, void* stream)
+                                           const mma_tdse_buffers* bufs, int m32, int cta_threads, int grid_ctas,
+                                           void* stream)
 {
     c64::Args A{insts, n_inst, grids, bufs->fields, bufs->outputs, bufs->psi_final, bufs->snapshots, bufs->counter};
     cudaStream_t st = (cudaStream_t)stream;
+    const int T = cta_threads ? cta_threads : kThreads;
+    if (!c64_shape_ok(T, m32)) return MMA_ERR_TOO_LARGE;
     if (cudaMemsetAsync(bufs->counter, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+    if (T == 512) return m32 == 8 ? launch_c64<8, 512>(A, grid_ctas, st) : launch_c64<16, 512>(A, grid_ctas, st);
+    if (T == 1024) return launch_c64<8, 1024>(A, grid_ctas, st);
     switch (m32) {
-        case 8: return launch_c64<8>(A, grid_ctas, st);
-        case 16: return launch_c64<16>(A, grid_ctas, st);
-        case 24: return launch_c64<24>(A, grid_ctas, st);
-        case 32: return launch_c64<32>(A, grid_ctas, st);
-        case 40: return launch_c64<40>(A, grid_ctas, st);
-        case 48: return launch_c64<48>(A, grid_ctas, st);
+        case 8: return launch_c64<8, kThreads>(A, grid_ctas, st);
+        case 16: return launch_c64<16, kThreads>(A, grid_ctas, st);
+        case 24: return launch_c64<24, kThreads>(A, grid_ctas, st);
+        case 32: return launch_c64<32, kThreads>(A, grid_ctas, st);
+        case 40: return launch_c64<40, kThreads>(A, grid_ctas, st);
+        case 48: return launch_c64<48, kThreads>(A, grid_ctas, st);
         default: return MMA_ERR_TOO_LARGE;
     }
 }

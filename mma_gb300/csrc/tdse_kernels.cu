@@ -507,7 +507,8 @@ static int sm_count()
 }
 
 extern "C" int mma_tdse_propagate_c64_impl(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
-                                           const mma_tdse_buffers* bufs, int m32, int grid_ctas, void* stream);
+                                           const mma_tdse_buffers* bufs, int m32, int cta_threads, int grid_ctas,
+                                           void* stream);
 
 extern "C" int mma_tdse_default_ctas(int max_m, int precision)
 {
@@ -537,6 +538,13 @@ extern "C" size_t mma_tdse_scratch_bytes(int max_m, int grid_ctas, int precision
 extern "C" int mma_tdse_propagate(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
                                   const mma_tdse_buffers* bufs, int max_m, int grid_ctas, int precision, void* stream)
 {
+    return mma_tdse_propagate_ex(insts, n_inst, grids, bufs, max_m, 0, grid_ctas, precision, stream);
+}
+
+extern "C" int mma_tdse_propagate_ex(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
+                                     const mma_tdse_buffers* bufs, int max_m, int cta_threads, int grid_ctas,
+                                     int precision, void* stream)
+{
     if (n_inst <= 0) return MMA_OK;
     if (!insts || !grids || !bufs || !bufs->fields || !bufs->outputs || !bufs->counter || !bufs->scratch ||
         max_m < 1)
@@ -546,9 +554,10 @@ extern "C" int mma_tdse_propagate(const mma_tdse_instance* insts, int n_inst, co
     if (grid_ctas <= 0) grid_ctas = mma_tdse_default_ctas(max_m, precision);
     if (grid_ctas > n_inst) grid_ctas = n_inst;
     if (precision == 1) {
-        // max_m is the common m32 of the batch's complex64 tables (8, 16, 24 or 32)
-        return mma_tdse_propagate_c64_impl(insts, n_inst, grids, bufs, max_m, grid_ctas, stream);
+        // max_m is the common m32 of the batch's complex64 tables, cta_threads their CTA size
+        return mma_tdse_propagate_c64_impl(insts, n_inst, grids, bufs, max_m, cta_threads, grid_ctas, stream);
     }
+    if (cta_threads != 0 && cta_threads != kThreads) return MMA_ERR_UNSUPPORTED;
     if (bufs->scratch_bytes < mma_tdse_scratch_bytes(max_m, grid_ctas, precision)) return MMA_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(bufs->counter, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;

@@ -67,6 +67,19 @@ def _sig():
     lib.mma_hankel_fast.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p]
     lib.mma_hankel_fast.restype = c_int
+    lib.mma_hankel_planes_tc_scratch_bytes.argtypes = [P, POINTER(FastPlan)]
+    lib.mma_hankel_planes_tc_scratch_bytes.restype = c_size_t
+    lib.mma_hankel_planes_tc.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                         c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p]
+    lib.mma_hankel_planes_tc.restype = c_int
+    lib.mma_hankel_planes_tc_prepare.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p, c_void_p, c_void_p,
+                                                 c_void_p, c_void_p, c_size_t, c_void_p]
+    lib.mma_hankel_planes_tc_prepare.restype = c_int
+    lib.mma_hankel_planes_tc_run.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                                             c_void_p, c_void_p, c_size_t, c_void_p]
+    lib.mma_hankel_planes_tc_run.restype = c_int
+    lib.mma_hankel_planes_tc_status.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p]
+    lib.mma_hankel_planes_tc_status.restype = c_int
     lib._mma_hankel_sig = True
     return lib
 
@@ -216,10 +229,17 @@ def _dev(a, device):
     return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=device)
 
 
+TC_MIN_PLANES = 16  # from this many requested planes the fast form computes them on the tensor cores
+
+
 def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_field=True, planes=(), form="plain",
-              tol=1e-9, stream=None):
+              tol=1e-9, stream=None, planes_via="auto", _events=None):
     """Run the far-field kernels.  source: torch complex tensor [Nz, No, Nr] on the GPU.
-    Returns (FF [Nrho, No] complex128 tensor, {plane: [Nrho, No] tensor}, fast plan dict or None)."""
+    Returns (FF [Nrho, No] complex128 tensor, {plane: [Nrho, No] tensor}, fast plan dict or None).
+
+    With form="fast", requested planes are computed either directly (one FP32 J0 per term,
+    planes_via="direct") or by the tensor-core split-precision GEMM (planes_via="tc");
+    "auto" takes the tensor cores from TC_MIN_PLANES planes on, where the problem fits them."""
     lib = _sig()
     dev = source.device
     Nz, No, Nr = source.shape
@@ -258,10 +278,33 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
                "mma_hankel_fast_plan")
         nb = lib.mma_hankel_fast_scratch_bytes(ctypes.byref(prob), ctypes.byref(plan))
         scratch = torch.empty(int(nb), dtype=torch.uint8, device=dev)
+        ntc = int(lib.mma_hankel_planes_tc_scratch_bytes(ctypes.byref(prob), ctypes.byref(plan))) if planes else 0
+        if planes_via not in ("auto", "tc", "direct"):
+            raise ValueError("planes_via must be 'auto', 'tc' or 'direct'")
+        use_tc = bool(planes) and ntc > 0 and (planes_via == "tc" or (planes_via == "auto" and
+                                                                      len(planes) >= TC_MIN_PLANES))
+        if planes_via == "tc" and planes and ntc == 0:
+            raise HankelError("the tensor-core plane form does not support this problem (n_r > 1024 or > 32 terms)")
         _check(lib.mma_hankel_fast(ctypes.byref(prob), ctypes.byref(plan), og.data_ptr(), rg.data_ptr(), zg.data_ptr(),
-                                   rh.data_ptr(), S.data_ptr(), ptr(pre), ff.data_ptr(), ptr(slot), len(planes),
-                                   ptr(pl), scratch.data_ptr(), int(nb), st), "mma_hankel_fast")
+                                   rh.data_ptr(), S.data_ptr(), ptr(pre), ff.data_ptr(),
+                                   None if use_tc else ptr(slot), 0 if use_tc else len(planes),
+                                   None if use_tc else ptr(pl), scratch.data_ptr(), int(nb), st), "mma_hankel_fast")
+        if use_tc:
+            tcs = torch.empty(ntc, dtype=torch.uint8, device=dev)
+            _check(lib.mma_hankel_planes_tc_prepare(ctypes.byref(prob), ctypes.byref(plan), og.data_ptr(),
+                                                    rg.data_ptr(), zg.data_ptr(), S.data_ptr(), ptr(pre),
+                                                    tcs.data_ptr(), ntc, st), "mma_hankel_planes_tc_prepare")
+            if _events is not None:  # (start, end) CUDA events around the tensor-core kernel
+                _events[0].record(stream or torch.cuda.current_stream())
+            _check(lib.mma_hankel_planes_tc_run(ctypes.byref(prob), ctypes.byref(plan), og.data_ptr(), rg.data_ptr(),
+                                                rh.data_ptr(), slot.data_ptr(), len(planes), pl.data_ptr(),
+                                                tcs.data_ptr(), ntc, st), "mma_hankel_planes_tc_run")
+            if _events is not None:
+                _events[1].record(stream or torch.cuda.current_stream())
+            _check(lib.mma_hankel_planes_tc_status(ctypes.byref(prob), ctypes.byref(plan), tcs.data_ptr(), st),
+                   "mma_hankel_planes_tc (kernel status)")
         plan_d = plan.as_dict()
+        plan_d["planes_via"] = ("tc" if use_tc else "direct") if planes else None
     else:
         raise ValueError("form must be 'plain' or 'fast'")
     out_planes = {p: pl[i] for i, p in enumerate(planes)} if planes else {}

@@ -36,7 +36,8 @@ class GridRec(Structure):
     _fields_ = [("n", c_int64), ("m", c_int64), ("dx", c_double), ("trg_a", c_double), ("dt", c_double),
                 ("x_int", c_double), ("Eguess", c_double), ("CV", c_double), ("max_iter", c_int64),
                 ("x", c_void_p), ("gv", c_void_p), ("psi0", c_void_p), ("cn_tab", c_void_p), ("gs_tab", c_void_p),
-                ("result", c_void_p), ("m32", c_int64), ("c64_tab", c_void_p), ("adj_tab", c_void_p)]
+                ("result", c_void_p), ("m32", c_int64), ("c64_tab", c_void_p), ("adj_tab", c_void_p),
+                ("c64_threads", c_int64)]
 
 
 class InstRec(Structure):
@@ -72,6 +73,11 @@ def _sig():
     lib.mma_tdse_build_grids.restype = c_int
     lib.mma_tdse_propagate.argtypes = [c_void_p, c_int, c_void_p, POINTER(BufRec), c_int, c_int, c_int, c_void_p]
     lib.mma_tdse_propagate.restype = c_int
+    lib.mma_tdse_propagate_ex.argtypes = [c_void_p, c_int, c_void_p, POINTER(BufRec), c_int, c_int, c_int, c_int,
+                                          c_void_p]
+    lib.mma_tdse_propagate_ex.restype = c_int
+    lib.mma_tdse_c64_shape_ok.argtypes = [c_int, c_int]
+    lib.mma_tdse_c64_shape_ok.restype = c_int
     lib.mma_tdse_scratch_bytes.argtypes = [c_int, c_int, c_int]
     lib.mma_tdse_scratch_bytes.restype = c_size_t
     lib.mma_tdse_default_ctas.argtypes = [c_int, c_int]
@@ -114,9 +120,13 @@ class TDSEGrids:
     ``params``: list of dicts with num_r, dx, trg_a and optionally x_int (2.0),
     Eguess (-1.0), CV (1e-15), max_iter (1000).  ``dt`` is the propagation step
     (already refined).  The ground states are computed on construction.
+
+    ``c64_threads`` (complex64 form only): CTA size the complex64 tables are laid out for --
+    None or 256 (every grid), 512 or 1024 (grids that fit that shape, others 256), a list (per
+    grid), or "auto" (the autotuner's choice per grid size, mma_gb300.autotune).
     """
 
-    def __init__(self, params, dt, device="cuda", stream=None, c64=False, adjoint=False):
+    def __init__(self, params, dt, device="cuda", stream=None, c64=False, adjoint=False, c64_threads=None):
         lib = _sig()
         self.device = torch.device(device)
         self.dt = float(dt)
@@ -163,14 +173,35 @@ class TDSEGrids:
             for r, o in zip(recs, a_off):
                 r.adj_tab = self.adj_buf.data_ptr() + 8 * int(o)
         self.c64 = bool(c64)
+        self.c64_threads = np.full(len(recs), THREADS, dtype=np.int64)
         if self.c64:
             if self.m32.max() > 48:
                 raise ValueError("the complex64 form takes grids of at most 12288 sites")
-            c_sizes = C64_SLOTS * THREADS * self.m32
+            if isinstance(c64_threads, str):
+                if c64_threads != "auto":
+                    raise ValueError("c64_threads must be None, an int, a list or 'auto'")
+                from .autotune import choose_c64_threads
+
+                want = [choose_c64_threads(int(n), self.dt, self.params[g], device=self.device)
+                        for g, n in enumerate(self.n)]
+            elif c64_threads is None or np.isscalar(c64_threads):
+                want = [int(c64_threads or THREADS)] * len(recs)
+            else:
+                want = [int(t) for t in c64_threads]
+                if len(want) != len(recs):
+                    raise ValueError("one c64_threads entry per grid")
+            for g, t in enumerate(want):
+                m32 = -(-int(self.n[g]) // t)
+                m32 = -(-m32 // 8) * 8
+                if t != THREADS and lib.mma_tdse_c64_shape_ok(t, m32):
+                    self.c64_threads[g] = t
+                    self.m32[g] = m32
+            c_sizes = C64_SLOTS * self.c64_threads * self.m32
             self.c64_buf = torch.zeros(int(c_sizes.sum()), dtype=torch.float32, device=self.device)
             c_off = np.concatenate([[0], np.cumsum(c_sizes)])[:-1]
-            for r, m32, o in zip(recs, self.m32, c_off):
+            for r, m32, o, t in zip(recs, self.m32, c_off, self.c64_threads):
                 r.m32 = int(m32)
+                r.c64_threads = int(t)
                 r.c64_tab = self.c64_buf.data_ptr() + 4 * int(o)
         arr = (GridRec * len(recs))(*recs)
         self.host_recs = arr
@@ -325,19 +356,20 @@ class TDSEBatchPlan:
         self.recs = recs
         # propagation launches: instances split by kernel shape, longest first within each
         cost = grids.n[gid].astype(np.float64) * S
-        if self.prec == 1:
-            shapes = grids.m32[gid]
+        if self.prec == 1:  # kernel shape = (sites per thread, CTA size) of the complex64 tables
+            shapes = grids.m32[gid] * 4096 + grids.c64_threads[gid]
         else:
             shapes = np.zeros(n_inst, dtype=np.int64)
         self.launches = []
         for shape in sorted(np.unique(shapes), reverse=True):
             idx = np.nonzero(shapes == shape)[0]
             idx = idx[np.argsort(-cost[idx], kind="stable")]
-            max_m = int(shape) if self.prec == 1 else int(grids.m[np.unique(gid[idx])].max())
+            max_m = int(shape) // 4096 if self.prec == 1 else int(grids.m[np.unique(gid[idx])].max())
+            cta_threads = int(shape) % 4096 if self.prec == 1 else 0
             ctas = grid_ctas or lib.mma_tdse_default_ctas(max_m, self.prec)
             ctas = min(ctas, len(idx))
             sb = int(lib.mma_tdse_scratch_bytes(max_m, ctas, self.prec))
-            self.launches.append(dict(idx=idx, max_m=max_m, ctas=ctas,
+            self.launches.append(dict(idx=idx, max_m=max_m, ctas=ctas, cta_threads=cta_threads,
                                       scratch=torch.empty(max(sb, 8), dtype=torch.uint8, device=dev), sbytes=sb,
                                       counter=torch.zeros(1, dtype=torch.int32, device=dev)))
         self._upload_records()
@@ -410,9 +442,10 @@ class TDSEBatchPlan:
                        self.psi_buf.data_ptr() if self.psi_buf is not None else None,
                        self.snap_buf.data_ptr() if self.snap_buf is not None else None, Lc["counter"].data_ptr(),
                        Lc["scratch"].data_ptr(), Lc["sbytes"])
-            _check(lib.mma_tdse_propagate(Lc["d_insts"].data_ptr(), len(Lc["idx"]), self.grids.dev_recs.data_ptr(),
-                                          ctypes.byref(B), Lc["max_m"], Lc["ctas"], self.prec, st),
-                   "mma_tdse_propagate")
+            _check(lib.mma_tdse_propagate_ex(Lc["d_insts"].data_ptr(), len(Lc["idx"]),
+                                             self.grids.dev_recs.data_ptr(), ctypes.byref(B), Lc["max_m"],
+                                             Lc["cta_threads"], Lc["ctas"], self.prec, st),
+                   "mma_tdse_propagate_ex")
         if _events is not None:
             _events[1].record(stream)
         for G in self.spec_groups:

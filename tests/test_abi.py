@@ -134,3 +134,39 @@ def test_legacy_calls_report_errors_without_crashing():
         dll.call1DTDSE(inp2, out)
     inp2.gauge = 1
     E[3] = 0.0
+
+
+def test_c64_shapes():
+    """Kernel shapes of the complex64 form (no GPU call)."""
+    from mma_gb300.autotune import candidate_shapes
+
+    assert candidate_shapes(8001) == [(256, 32), (512, 16), (1024, 8)]
+    assert candidate_shapes(12001) == [(256, 48)]
+    assert candidate_shapes(601) == [(256, 8), (512, 8), (1024, 8)]
+
+
+def test_batched_record_layouts_match_mirrors():
+    """sizeof/offsetof of the batched and far-field records against their ctypes mirrors."""
+    from mma_gb300.hankel import FastPlan, HankelProblem
+    from mma_gb300.tdse_batch import BufRec, GridRec, InstRec
+
+    pairs = [("mma_tdse_grid", GridRec), ("mma_tdse_instance", InstRec), ("mma_tdse_buffers", BufRec),
+             ("mma_hankel_problem", HankelProblem), ("mma_hankel_fast_plan_t", FastPlan)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "mma_tdse.h"', '#include "mma_hankel.h"',
+             "int main(void){"]
+    for cname, cls in pairs:
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append("return 0;}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "probe.c")
+        open(c, "w").write("\n".join(lines))
+        exe = os.path.join(d, "probe")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = dict(l.split() for l in out if l.strip())
+    for cname, cls in pairs:
+        assert int(got[cname]) == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert int(got[cname + "." + f]) == getattr(cls, f).offset, (cname, f)

@@ -1,0 +1,106 @@
+"""Tensor-core form of the per-plane far-field transforms (split-precision FP16, FP32 accumulation).
+
+* the tcgen05 building blocks against a float32 matrix product of the same FP16 operands
+  (operands staged by threads, and B by TMA);
+* every plane against the plain FP64 form on a problem with ragged sizes (n_r, n_z, n_rho not
+  multiples of the tile sizes): per-harmonic relative L2 error over rho <= 2e-5, the bound
+  stated for the fast form;
+* the cumulative results of Hankel_long through the tensor-core planes against the reference's
+  own fixtures (Hankel_transform.py run on the same inputs).
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL = 2e-5
+
+
+def per_harmonic(a, b):
+    """max over omega of ||a[:, w] - b[:, w]|| / ||b[:, w]|| (arrays [rho, omega])."""
+    return float(np.max(np.linalg.norm(a - b, axis=0) / np.linalg.norm(b, axis=0)))
+
+
+@pytest.mark.parametrize("use_tma", [0, 1])
+def test_tcgen05_tile(gpu_lib, use_tma):
+    from mma_gb300._lib import load
+
+    lib = load()
+    lib.mma_tc_selftest.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.mma_tc_selftest.restype = ctypes.c_int
+    g = torch.Generator().manual_seed(3)
+    A = torch.randn(128, 32, generator=g).half().cuda()
+    B = torch.randn(256, 32, generator=g).half().cuda()
+    D = torch.full((128, 256), float("nan"), dtype=torch.float32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.mma_tc_selftest(A.data_ptr(), B.data_ptr(), D.data_ptr(), use_tma, status.data_ptr(), st) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    ref = A.float() @ B.float().T
+    assert torch.isfinite(D).all()
+    assert (D - ref).abs().max().item() <= 1e-5 * ref.abs().max().item()
+
+
+def _problem(n_omega=24, n_r=200, n_z=40, n_rho=50, seed=0, rho_max=5e-3):
+    omega0 = 0.057 / 2.4188843265857e-17
+    rgrid = np.linspace(0.0, 200e-6, n_r)
+    zgrid = np.linspace(-5e-3, 5e-3, n_z)
+    ogrid = np.linspace(10 * omega0, 42 * omega0, n_omega)
+    rho = np.linspace(0.0, rho_max, n_rho)
+    rng = np.random.default_rng(seed)
+    ph = rng.uniform(0, 2 * np.pi, size=(n_z, n_omega))
+    S = np.exp(-(rgrid / 50e-6) ** 2)[None, None, :] * np.exp(1j * ph)[:, :, None]
+    return zgrid, rgrid, ogrid, rho, torch.tensor(S, dtype=torch.complex64, device="cuda")
+
+
+@pytest.mark.parametrize("tol,rho_max,terms", [(1e-9, 5e-3, 16), (1e-6, 1e-3, 8), (1e-13, 5e-3, 32)],
+                         ids=["16 terms", "8 terms", "32 terms"])
+def test_all_planes_vs_plain(gpu_lib, tol, rho_max, terms):
+    from mma_gb300 import hankel as H
+
+    zg, rg, og, rho, S = _problem(rho_max=rho_max)
+    planes = list(range(len(zg)))
+    pre = np.exp(1j * np.linspace(0, 1, len(zg)))[:, None] * np.ones((1, len(og)))
+    _, p64, _ = H.far_field(og, rg, zg, rho, S, 1.0, pre, True, planes=planes, form="plain")
+    _, ptc, plan = H.far_field(og, rg, zg, rho, S, 1.0, pre, True, planes=planes, form="fast", tol=tol,
+                               planes_via="tc")
+    assert plan["planes_via"] == "tc"
+    assert {8: 8, 12: 16, 16: 16, 20: 32, 24: 32, 32: 32}[int(plan["n_terms"])] == terms
+    worst = max(per_harmonic(ptc[k].cpu().numpy(), p64[k].cpu().numpy()) for k in planes)
+    print("tensor-core planes, %d terms: worst per-harmonic error %.2e" % (plan["n_terms"], worst))
+    assert worst < TOL
+
+
+def test_selected_planes_only(gpu_lib):
+    """Planes not requested are not written; requested ones match the direct FP32 form."""
+    from mma_gb300 import hankel as H
+
+    zg, rg, og, rho, S = _problem(n_omega=8, n_z=20)
+    want = [0, 3, 19]
+    _, pd, _ = H.far_field(og, rg, zg, rho, S, 1.0, None, True, planes=want, form="fast", planes_via="direct")
+    _, pt, plan = H.far_field(og, rg, zg, rho, S, 1.0, None, True, planes=want, form="fast", planes_via="tc")
+    assert plan["planes_via"] == "tc" and sorted(pt) == want
+    for k in want:
+        assert per_harmonic(pt[k].cpu().numpy(), pd[k].cpu().numpy()) < TOL
+
+
+def test_cumulative_vs_reference_fixture(gpu_lib):
+    from mma_gb300 import hankel as H
+
+    g = np.load(os.path.join(GOLDEN, "hankel_config3_slice.npz"))
+    H.XUV_index.set_constant_index(complex(g["n_xuv"][0], g["n_xuv"][1]))
+    target = H.FSources_provider(g["zgrid"], g["rgrid"], g["ogrid"], data_source="static", FSource=g["S"])
+    gas = g["gas"].item().decode() if isinstance(g["gas"].item(), bytes) else str(g["gas"])
+    h = H.Hankel_long(target, float(g["distance"]), g["rho"], preset_gas=gas, pressure=1.0,
+                      near_field_factor=bool(g["near_field"]), store_cumulative_result=True, form="fast")
+    assert h.fast_plan["planes_via"] == "tc"
+    ref = g["cumulative"]
+    for k in range(ref.shape[0]):
+        assert per_harmonic(h.cumulative_field[k], ref[k]) < TOL, k
+    assert per_harmonic(h.entry_plane_transform, g["entry"]) < TOL
+    assert per_harmonic(h.exit_plane_transform, g["exit"]) < TOL

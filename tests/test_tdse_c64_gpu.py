@@ -36,3 +36,68 @@ def test_c64_against_oracle(gpu_lib, oracle_built):
     for num_r, errs in report.items():
         for k, b in BOUNDS.items():
             assert errs[k] < b, (num_r, k, errs[k])
+
+
+@pytest.mark.parametrize("threads", [512, 1024])
+def test_c64_cta_sizes_against_oracle(gpu_lib, oracle_built, threads):
+    """The wider CTA shapes of the complex64 kernel (same tables rounded the same way, wider
+    scans): same bounds against the oracle, and close to the 256-thread result."""
+    import oracle.tdse as ot
+    from mma_gb300.tdse_batch import TDSEGrids, run_batch
+
+    t, E = sin2_pulse(2, skip_first=True)
+    dtf = t[1] - t[0]
+    for num_r, dx in [(600, 0.4), (8000, 0.1)]:
+        g_w = TDSEGrids([dict(num_r=num_r, dx=dx, trg_a=A_CONFIG)], dt=dtf, c64=True, c64_threads=threads)
+        g_n = TDSEGrids([dict(num_r=num_r, dx=dx, trg_a=A_CONFIG)], dt=dtf, c64=True)
+        assert int(g_w.c64_threads[0]) == threads and int(g_w.m32[0]) * threads >= num_r + 1
+        f = torch.tensor(np.stack([E, 0.8 * E]), device="cuda")
+        rw = run_batch(g_w, f, dt_field=dtf, tmax=t[-1] - t[0], precision="c64")
+        rn = run_batch(g_n, f, dt_field=dtf, tmax=t[-1] - t[0], precision="c64")
+        torch.cuda.synchronize()
+        x, psi0, e, _ = ot.ground_state(num_r, dx, A_CONFIG, -1.0, 1e-15)
+        o = ot.propagate(x, psi0, t, E, dx, A_CONFIG)
+        for k in ("sourceterm", "PopTot", "PopInt", "expval"):
+            assert rel_l2(rw[k][0].cpu().numpy(), o[k]) < BOUNDS[k], (threads, num_r, k)
+            assert rel_l2(rw[k][1].cpu().numpy(), rn[k][1].cpu().numpy()) < BOUNDS[k], (threads, num_r, k)
+        assert plateau_error(rw["Fsourceterm"][0].cpu().numpy(), o["Fsourceterm"], o["omegagrid"]) < BOUNDS["plateau"]
+
+
+def test_c64_mixed_cta_sizes_in_one_plan(gpu_lib):
+    """Grids with different CTA sizes in one batch: the plan groups launches by shape."""
+    from mma_gb300.tdse_batch import TDSEGrids, run_batch
+
+    t, E = sin2_pulse(1, skip_first=True)
+    dtf = t[1] - t[0]
+    params = [dict(num_r=2000, dx=0.2, trg_a=A_CONFIG), dict(num_r=10000, dx=0.1, trg_a=A_CONFIG)]
+    g_mix = TDSEGrids(params, dt=dtf, c64=True, c64_threads=[512, 512])
+    assert list(g_mix.c64_threads) == [512, 256]  # 10001 sites do not fit the 512-thread kernel
+    g_ref = TDSEGrids(params, dt=dtf, c64=True)
+    f = torch.tensor(np.stack([E, E, 0.7 * E]), device="cuda")
+    ids = [0, 1, 0]
+    rm = run_batch(g_mix, f, dt_field=dtf, grid_ids=ids, precision="c64", tmax=t[-1] - t[0])
+    rr = run_batch(g_ref, f, dt_field=dtf, grid_ids=ids, precision="c64", tmax=t[-1] - t[0])
+    torch.cuda.synchronize()
+    assert torch.isfinite(rm["sourceterm"]).all()
+    for i in range(3):
+        assert rel_l2(rm["PopTot"][i].cpu().numpy(), rr["PopTot"][i].cpu().numpy()) < 2e-4
+
+
+def test_autotuner_picks_and_caches(gpu_lib, tmp_path, monkeypatch):
+    from mma_gb300 import autotune
+    from mma_gb300.tdse_batch import TDSEGrids
+
+    monkeypatch.setenv("MMA_TUNE_CACHE", str(tmp_path / "tune.json"))
+    p = dict(num_r=4000, dx=0.1, trg_a=A_CONFIG)
+    t = autotune.choose_c64_threads(4001, 0.25, p, retune=True)
+    assert t in (256, 512, 1024)
+    rep = autotune.last_report()
+    key = autotune._key(4001, 0.25, "c64", "cuda")
+    assert key in rep and all(v > 0 for v in rep[key].values())
+    best = min(rep[key], key=rep[key].get)
+    assert t == best or (t == autotune.DEFAULT and rep[key][best] > (1 - autotune.MARGIN) * rep[key][t])
+    assert (tmp_path / "tune.json").exists()
+    autotune._MEM.clear()
+    assert autotune.choose_c64_threads(4001, 0.25, p) == t  # from the file, no timing
+    g = TDSEGrids([p], dt=0.25, c64=True, c64_threads="auto")
+    assert int(g.c64_threads[0]) == t
