@@ -532,7 +532,8 @@ def run_ours(args, rank, world, precision):
     n_inst = fields_np.shape[0]
     fields = torch.tensor(fields_np, device=dev)
     grids = TDSEGrids([dict(num_r=8000, dx=0.1, trg_a=A_CONFIG)], dt=dtf, c64=(precision == "c64"),
-                      c64_threads="auto" if precision == "c64" else None)
+                      c64_threads=(args.c64_threads if args.c64_threads == "auto" else int(args.c64_threads))
+                      if precision == "c64" else None)
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
     stream = torch.cuda.current_stream()
     plan = TDSEBatchPlan(grids, [fields.shape[1]] * n_inst, dtf, tmax=tmax, precision=precision)
@@ -667,6 +668,8 @@ def main():
     ap.add_argument("--no-hankel", action="store_true")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config1")
     ap.add_argument("--forms", choices=["both", "fp64", "c64"], default="both")
+    ap.add_argument("--c64-threads", default="auto",
+                    help="CTA size of the complex64 kernel: auto (the autotuner) or 256, 512, 1024")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

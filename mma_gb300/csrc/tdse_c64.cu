@@ -460,22 +460,29 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
 // next to the tables (24 bytes per site), which leaves registers for the chunk products F and
 // G, so each sweep runs once (three passes per step); the population window is summed from
 // shared memory by the threads whose chunk meets it; the observables use blocked two-sum
-// accumulation (8 sites in FP32, then an error-free update of a float-float pair).  The CTA
+// accumulation (16 sites in FP32, then an error-free update of a float-float pair).  The CTA
 // size T is chosen per grid (the tables are laid out for it); more threads per instance hide
 // more latency at the price of wider scans.
+//
+// In shared memory the four tables are interleaved per site (one float4: 1/beta re, im, V,
+// psi0), so each pass reads one vector per site; the neighbour's V for the off-diagonal factor
+// is carried from the previous iteration.  Rows beyond n-1 have zero tables, which makes y and u
+// exactly 0 there: the last row's super-diagonal then multiplies u_n = 0 and the first row's
+// sub-diagonal an incoming carry of 0, so the sweeps need no boundary tests.  The phase of site
+// i is advanced by a recurrence ph_{i+1} = ph_i e^{i F dt dx} from the thread's first site.
 template <int M, int T>
 __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
 {
     constexpr int NW = T / 32;
-    extern __shared__ float tab[];  // T_SLOTS * L floats, then psi [L] complex float
+    extern __shared__ float4 tab4[];  // L sites x (1/beta re, im, V, psi0), then psi [L] complex float
     __shared__ cf sc[2 * NW], sb[2 * NW];
     __shared__ float red_hi[NW * 4], red_lo[NW * 4], red_pi[NW];
-    __shared__ cf wtab[M];
+    __shared__ cf s_w1;
     __shared__ float s_ahi, s_alo;
     __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     constexpr int L = T * M;
-    cf* psi = reinterpret_cast<cf*>(tab + T_SLOTS * L);
+    cf* psi = reinterpret_cast<cf*>(tab4 + L);
     if (t == 0) s_grid = -1;
 
     for (;;) {
@@ -492,7 +499,9 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
             continue;
         }
         if (s_grid != I.grid)
-            for (int q = t; q < T_SLOTS * L; q += T) tab[q] = G.c64_tab[q];
+            for (int q = t; q < L; q += T)
+                tab4[q] = make_float4(G.c64_tab[T_IBRE * L + q], G.c64_tab[T_IBIM * L + q], G.c64_tab[T_V * L + q],
+                                      G.c64_tab[T_PSI0 * L + q]);
         __syncthreads();
         if (t == 0) {
             s_grid = I.grid;
@@ -514,13 +523,9 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
             s_lo = lo < 0 ? 0 : lo;
             s_hi = hi > num_r ? num_r : hi;
         }
-        const float* ibre = tab + T_IBRE * L;
-        const float* ibim = tab + T_IBIM * L;
-        const float* vv = tab + T_V * L;
-        const float* p0 = tab + T_PSI0 * L;
         const int64_t s0 = (int64_t)t * M;
 #pragma unroll
-        for (int i = 0; i < M; i++) psi[i * T + t] = cf{p0[i * T + t], 0.f};
+        for (int i = 0; i < M; i++) psi[i * T + t] = cf{tab4[i * T + t].w, 0.f};
         const double xs_d = (s0 < n) ? G.x[s0] : 0.0;
         const float xs_hi = (float)xs_d, xs_lo = (float)(xs_d - (double)xs_hi);
         const float dxf = (float)G.dx;
@@ -592,53 +597,51 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
                 o_t[k + 1] = tt;
                 o_e[k + 1] = Fk;
             }
-            if (w == NW - 1) {
-                for (int i = lane; i < M; i += 32) {
-                    float sn, cs;
-                    sincosf((float)(Fk * dt * G.dx) * (float)i, &sn, &cs);
-                    wtab[i] = cf{cs, sn};
-                }
-                if (lane == 31) {
-                    const double fdt = Fk * dt;
-                    const float a_hi = (float)fdt;
-                    s_ahi = a_hi;
-                    s_alo = (float)(fdt - (double)a_hi);
-                }
+            if (w == NW - 1 && lane == 31) {
+                const double fdt = Fk * dt;
+                const float a_hi = (float)fdt;
+                s_ahi = a_hi;
+                s_alo = (float)(fdt - (double)a_hi);
+                float sn, cs;
+                sincosf((float)(fdt * G.dx), &sn, &cs);
+                s_w1 = cf{cs, sn};
             }
             // ---- pass 1: right-hand side 2 M2 psi, local forward sweep, forward products F
             cf pm = (t == 0) ? cf{0.f, 0.f} : psi[(M - 1) * T + t - 1];
             cf pc = psi[t];
+            float vl = (t == 0) ? 0.f : tab4[(M - 1) * T + t - 1].z;  // V of the site to the left
             cf yprev{0.f, 0.f}, Fp{1.f, 0.f};
 #pragma unroll
             for (int i = 0; i < M; i++) {
                 const int q = i * T + t;
                 const cf pn = (i + 1 < M) ? psi[q + T] : ((t + 1 < T) ? psi[t + 1] : cf{0.f, 0.f});
                 const cf r{fmaf(10.f, pc.re, pm.re + pn.re), fmaf(10.f, pc.im, pm.im + pn.im)};
-                const float vl = (i == 0) ? ((t == 0) ? 0.f : vv[(M - 1) * T + t - 1]) : vv[q - T];
-                const cf ib{ibre[q], ibim[q]};
-                cf h = off_diag(vl, ib.re, ib.im);
-                if (s0 + i == 0) h = cf{0.f, 0.f};
+                const float4 tb = tab4[q];
+                const cf ib{tb.x, tb.y};
+                const cf h = off_diag(vl, ib.re, ib.im);
                 yprev = cfms(h, yprev, cmul(ib, r));
                 yl[i] = yprev;
                 Fp = cmul(Fp, cf{-h.re, -h.im});
                 fg[i] = Fp;
+                vl = tb.z;
                 pm = pc;
                 pc = pn;
             }
             const cf yin = scan_fwd<NW>(fg[M - 1], yprev, sc, sb);
             // ---- pass 2: forward correction, local backward sweep, backward products G
             cf unext{0.f, 0.f}, Gp{1.f, 0.f};
+            float vr = (t == T - 1) ? 0.f : tab4[t + 1].z;  // V of the site to the right
 #pragma unroll
             for (int i = M - 1; i >= 0; i--) {
                 const int q = i * T + t;
                 const cf y = cfma(fg[i], yin, yl[i]);
-                const float vr = (i == M - 1) ? ((t == T - 1) ? 0.f : vv[t + 1]) : vv[q + T];
-                cf g = off_diag(vr, ibre[q], ibim[q]);
-                if (s0 + i >= n - 1) g = cf{0.f, 0.f};
+                const float4 tb = tab4[q];
+                const cf g = off_diag(vr, tb.x, tb.y);
                 unext = cfms(g, unext, y);
                 yl[i] = unext;
                 Gp = cmul(Gp, cf{-g.re, -g.im});
                 fg[i] = Gp;
+                vr = tb.z;
             }
             const cf uin = scan_bwd<NW>(fg[0], unext, sc + NW, sb + NW);
             // ---- pass 3: backward correction, CN update, phase, observables
@@ -651,23 +654,26 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
             red = fmaf(-kk, 3.0199159819370158e-07f, red) + th_lo;
             float sn, cs;
             sincosf(red, &sn, &cs);
-            const cf phs{cs, sn};
+            const cf w1 = s_w1;
+            cf ph{cs, sn};
             float ahi[4] = {0.f, 0.f, 0.f, 0.f}, alo[4] = {0.f, 0.f, 0.f, 0.f}, part[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int i = 0; i < M; i++) {
                 const int q = i * T + t;
                 const cf u = cfma(fg[i], uin, yl[i]);
                 const cf d = u - psi[q];
-                const cf pn = cmul(cmul(phs, wtab[i]), d);
+                const cf pn = cmul(ph, d);
+                ph = cmul(ph, w1);
                 psi[q] = pn;
                 const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
                 const float xj = fmaf(dxf, (float)i, xs_hi);
-                const float vj = vv[q], pj = p0[q];
+                const float4 tb = tab4[q];
+                const float vj = tb.z, pj = tb.w;
                 part[0] = fmaf(n2, -xj * vj * vj * vj, part[0]);  // -V' = -x V^3
                 part[1] = fmaf(n2, xj, part[1]);
                 part[2] = fmaf(pn.re, pj, part[2]);
                 part[3] = fmaf(-pn.im, pj, part[3]);
-                if ((i & 7) == 7 || i == M - 1) {
+                if ((i & 15) == 15 || i == M - 1) {
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
                         float s2, e2;
