@@ -153,6 +153,19 @@ void inputs_destructor(inputs_def *in);
 void free_arr(double *buf);
 void free_mtrx(double **buf, int n_rows);
 
+/* Replace window_analysis (tools.c:206-316; PythonTDSE.py:80-109): photoelectron spectrum of
+ * psi (2(num_r+1) doubles, interleaved) by the resolvent window method on num_E energies
+ * E_start + i Estep with window dE; returns a malloc'ed [num_E] array (free_arr).  The inputs
+ * record is passed by value as in the reference; uses num_r, dx and trg.a.  Computed on the GPU
+ * (mma_tdse_pes); NULL with the status set on failure. */
+double *window_analysis(inputs_def inputs, double *psi, int num_E, double dE, double Estep, double E_start);
+
+/* Replace GaborTransform (tools_fftw3.c:158-213; PythonTDSE.py:111-150): |Gabor transform| of
+ * N samples at dt for N_G window centres t_min + i (t_max - t_min)/N_G with width a, the first
+ * N_freq DFT bins; returns malloc'ed rows [N_G][N_freq] (free_mtrx).  Computed on the GPU
+ * (mma_gabor). */
+double **GaborTransform(double *signal, double dt, int N, int N_freq, int N_G, double t_min, double t_max, double a);
+
 /* Status of the last legacy call on this thread (no reference counterpart). */
 int mma_last_error(void);
 const char *mma_last_error_message(void);
@@ -256,6 +269,20 @@ int mma_tdse_propagate_ex(const mma_tdse_instance *insts, int n_inst, const mma_
 
 /* 1 if the complex64 form has a kernel for CTA size cta_threads (0 = 256) and m32 sites per thread. */
 int mma_tdse_c64_shape_ok(int cta_threads, int m32);
+
+/* Photoelectron spectra on the GPU (window_analysis's algorithm, device pointers): one thread
+ * per energy, two FP64 Numerov-tridiagonal solves each.  psi [2(num_r+1)] interleaved, pes
+ * [num_E].  Scratch: the energies run in chunks of as many as the scratch holds;
+ * mma_tdse_pes_scratch_bytes(num_r, chunk) is the size for `chunk` energies at a time. */
+size_t mma_tdse_pes_scratch_bytes(int num_r, int chunk);
+int mma_tdse_pes(const double *psi, int num_r, double dx, double trg_a, int num_E, double dE, double Estep,
+                 double E_start, double *pes, void *scratch, size_t scratch_bytes, void *stream);
+
+/* Gabor transforms of n_sig signals (GaborTransform's algorithm, device pointers): signal s
+ * starts at signals + s * stride (N samples at dt); gabor [n_sig][N_G][N_freq]. */
+size_t mma_gabor_scratch_bytes(int n_sig, int N, int N_G);
+int mma_gabor(const double *signals, int64_t stride, int n_sig, double dt, int N, int N_freq, int N_G, double t_min,
+              double t_max, double a, double *gabor, void *scratch, size_t scratch_bytes, void *stream);
 
 /* Scratch bytes mma_tdse_propagate needs for these arguments. */
 size_t mma_tdse_scratch_bytes(int max_m, int grid_ctas, int precision);

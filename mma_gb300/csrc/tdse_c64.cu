@@ -138,12 +138,12 @@ constexpr double kInvTwoPi = 0.15915494309189533576888376337251;
 template <int M>
 __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
 {
-    extern __shared__ float tab[];  // T_SLOTS * 256 * M floats
+    extern __shared__ float4 tab4[];  // 256 * M sites x (1/beta re, im, V, psi0)
     __shared__ cf sc[2 * kWarps], sb[2 * kWarps];
     __shared__ float red_hi[kWarps * 4], red_lo[kWarps * 4];
     __shared__ cf bfirst[kWarps], blast[kWarps];
-    __shared__ cf wtab[M];
-    __shared__ float s_ahi, s_alo;  // F_k dt as a float-float pair (phase angle of pass 3)
+    __shared__ cf wtab[M];          // e^{i F_k dt dx i}, i < M: phase of site i relative to site 0
+    __shared__ float s_ahi, s_alo;  // F_k dt as a float-float pair (phase angle of pass 5)
     __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     constexpr int L = kThreads * M;
@@ -165,7 +165,9 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
         }
         // ---- tables into shared memory when the grid changes
         if (s_grid != I.grid) {
-            for (int q = t; q < T_SLOTS * L; q += kThreads) tab[q] = G.c64_tab[q];
+            for (int q = t; q < L; q += kThreads)
+                tab4[q] = make_float4(G.c64_tab[T_IBRE * L + q], G.c64_tab[T_IBIM * L + q], G.c64_tab[T_V * L + q],
+                                      G.c64_tab[T_PSI0 * L + q]);
         }
         __syncthreads();
         if (t == 0) {
@@ -188,15 +190,11 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             s_lo = lo < 0 ? 0 : lo;
             s_hi = hi > num_r ? num_r : hi;
         }
-        const float* ibre = tab + T_IBRE * L;
-        const float* ibim = tab + T_IBIM * L;
-        const float* vv = tab + T_V * L;
-        const float* p0 = tab + T_PSI0 * L;
         // ---- state: psi in registers, initialised from the ground state
         cf psi[M], yy[M];
         const int64_t s0 = (int64_t)t * M;
 #pragma unroll
-        for (int i = 0; i < M; i++) psi[i] = cf{p0[i * kThreads + t], 0.f};
+        for (int i = 0; i < M; i++) psi[i] = cf{tab4[i * kThreads + t].w, 0.f};
         // chunk start x as a float-float pair (phase angle) and as a float (<x>, -V')
         const double xs_d = (s0 < n) ? G.x[s0] : 0.0;
         const float xs_hi = (float)xs_d, xs_lo = (float)(xs_d - (double)xs_hi);
@@ -211,6 +209,8 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
         if (lane == 31) blast[w] = psi[M - 1];
         __syncthreads();
         const int64_t lo = s_lo, hi = s_hi, gate = s_gate;
+        // this thread's part of the population window [lo, hi], as chunk indices
+        const int win_a = (int)max((int64_t)0, lo - s0), win_b = (int)min((int64_t)M - 1, hi - s0);
         const double* f = P.fields + I.field_off;
         double* out = P.outputs + I.out_off;
         double *o_t = out, *o_e = out + (S + 1), *o_src = out + 2 * (S + 1), *o_ptot = out + 3 * (S + 1),
@@ -230,24 +230,16 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             }
         }
         double tt = I.tmin;
-        // h_j and g_j of site (i, t): 6 a_j /beta_j and 6 c_j /beta_j (zero at the grid ends)
-        // (1/2 + i 6 w) * ib with 6 w = c_hi + (c_lo + c1 V) kept unsummed
+        // h_j and g_j of site (i, t): 6 a_j /beta_j and 6 c_j /beta_j from the neighbour's V,
+        // (1/2 + i 6 w) * ib with 6 w = c_hi + (c_lo + c1 V) kept unsummed.  No boundary tests:
+        // rows beyond n-1 have zero tables (y = u = 0 there), the first row's h multiplies an
+        // incoming carry of 0 and the last row's g multiplies u_n = 0.
         auto off_diag = [&](float v, float ir, float ii) -> cf {
             const float t1 = fmaf(c1, v, c_lo);
             return cf{fmaf(-t1, ii, fmaf(-c_hi, ii, 0.5f * ir)), fmaf(t1, ir, fmaf(c_hi, ir, 0.5f * ii))};
         };
-        auto h_at = [&](int i) -> cf {
-            const int q = i * kThreads + t;
-            const float vl = (i == 0) ? ((t == 0) ? 0.f : vv[(M - 1) * kThreads + t - 1]) : vv[q - kThreads];
-            const cf r = off_diag(vl, ibre[q], ibim[q]);
-            return (s0 + i == 0) ? cf{0.f, 0.f} : r;
-        };
-        auto g_at = [&](int i) -> cf {
-            const int q = i * kThreads + t;
-            const float vr = (i == M - 1) ? ((t == kThreads - 1) ? 0.f : vv[t + 1]) : vv[q + kThreads];
-            const cf r = off_diag(vr, ibre[q], ibim[q]);
-            return (s0 + i >= n - 1) ? cf{0.f, 0.f} : r;
-        };
+        const float v_left = (t == 0) ? 0.f : tab4[(M - 1) * kThreads + t - 1].z;   // V left of site 0
+        const float v_right = (t == kThreads - 1) ? 0.f : tab4[t + 1].z;            // V right of site M-1
 
         for (int64_t k = 0; k < S; k++) {
             // FP64 work of a step is spread over three warps so that no single warp holds the
@@ -280,7 +272,10 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
                 o_e[k + 1] = Fk;
             }
             if (w == kWarps - 1) {
-                for (int i = lane; i < M; i += 32) {  // per-site phase factors e^{i F dt dx i}, i < M
+                // per-site phase factors, each from its own angle: a recurrence in i would carry
+                // the FP32 rounding of |e^{i F dt dx}| (1 +- 6e-8) as a bias growing with i, and it
+                // would compound over the steps into a drift of the norm along each chunk
+                for (int i = lane; i < M; i += 32) {
                     float sn, cs;
                     sincosf((float)(Fk * dt * G.dx) * (float)i, &sn, &cs);
                     wtab[i] = cf{cs, sn};
@@ -298,41 +293,51 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             if (lane == 31) right = (w == kWarps - 1) ? cf{0.f, 0.f} : bfirst[w + 1];
             // ---- pass 1: local forward sweep from zero: chunk-end value and product of (-h)
             cf yprev{0.f, 0.f}, Fp{1.f, 0.f};
+            float vl = v_left;
 #pragma unroll
             for (int i = 0; i < M; i++) {
-                const int q = i * kThreads + t;
+                const float4 tb = tab4[i * kThreads + t];
                 const cf pm = (i == 0) ? left : psi[i - 1];
                 const cf pn = (i == M - 1) ? right : psi[i + 1];
                 const cf r{fmaf(10.f, psi[i].re, pm.re + pn.re), fmaf(10.f, psi[i].im, pm.im + pn.im)};
-                const cf h = h_at(i);
-                yprev = cfms(h, yprev, cmul(cf{ibre[q], ibim[q]}, r));
+                const cf h = off_diag(vl, tb.x, tb.y);
+                yprev = cfms(h, yprev, cmul(cf{tb.x, tb.y}, r));
                 Fp = cmul(Fp, cf{-h.re, -h.im});
+                vl = tb.z;
             }
             cf yc = scan_fwd(Fp, yprev, sc, sb);  // exact y at the end of the previous chunk
             // ---- pass 2: forward sweep again from the exact carry, kept in registers
+            vl = v_left;
 #pragma unroll
             for (int i = 0; i < M; i++) {
-                const int q = i * kThreads + t;
+                const float4 tb = tab4[i * kThreads + t];
                 const cf pm = (i == 0) ? left : psi[i - 1];
                 const cf pn = (i == M - 1) ? right : psi[i + 1];
                 const cf r{fmaf(10.f, psi[i].re, pm.re + pn.re), fmaf(10.f, psi[i].im, pm.im + pn.im)};
-                yc = cfms(h_at(i), yc, cmul(cf{ibre[q], ibim[q]}, r));
+                yc = cfms(off_diag(vl, tb.x, tb.y), yc, cmul(cf{tb.x, tb.y}, r));
                 yy[i] = yc;
+                vl = tb.z;
             }
             // ---- pass 3: local backward sweep from zero: chunk-start value and product of (-g)
             cf unext{0.f, 0.f}, Gp{1.f, 0.f};
+            float vr = v_right;
 #pragma unroll
             for (int i = M - 1; i >= 0; i--) {
-                const cf g = g_at(i);
+                const float4 tb = tab4[i * kThreads + t];
+                const cf g = off_diag(vr, tb.x, tb.y);
                 unext = cfms(g, unext, yy[i]);
                 Gp = cmul(Gp, cf{-g.re, -g.im});
+                vr = tb.z;
             }
             cf uc = scan_bwd(Gp, unext, sc + kWarps, sb + kWarps);  // exact u at the start of the next chunk
             // ---- pass 4: backward sweep again from the exact carry
+            vr = v_right;
 #pragma unroll
             for (int i = M - 1; i >= 0; i--) {
-                uc = cfms(g_at(i), uc, yy[i]);
+                const float4 tb = tab4[i * kThreads + t];
+                uc = cfms(off_diag(vr, tb.x, tb.y), uc, yy[i]);
                 yy[i] = uc;
+                vr = tb.z;
             }
             // ---- pass 5: CN update, phase, observables
             // chunk-start angle F dt x_s in float-float, reduced mod 2 pi
@@ -348,29 +353,33 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             float sn, cs;
             sincosf(red, &sn, &cs);
             const cf phs{cs, sn};
-            float acc_hi[4] = {0.f, 0.f, 0.f, 0.f}, acc_c[4] = {0.f, 0.f, 0.f, 0.f};
+            // compensated sums: FP32 blocks of 16 sites, then an error-free update of (hi, lo)
+            float acc_hi[4] = {0.f, 0.f, 0.f, 0.f}, acc_lo[4] = {0.f, 0.f, 0.f, 0.f}, part[4] = {0.f, 0.f, 0.f, 0.f};
             float pint = 0.f;
 #pragma unroll
             for (int i = 0; i < M; i++) {
-                const int q = i * kThreads + t;
-                const int64_t j = s0 + i;
+                const float4 tb = tab4[i * kThreads + t];
                 const cf d = yy[i] - psi[i];
-                const cf ph = cmul(phs, wtab[i]);
-                const cf pn = cmul(ph, d);
+                const cf pn = cmul(cmul(phs, wtab[i]), d);
                 psi[i] = pn;
                 const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
                 const float xj = fmaf(dxf, (float)i, xs_hi);
-                const float vj = vv[q];
-                const float gvj = -xj * vj * vj * vj;  // -V' = x (a^2+x^2)^-3/2 = -x V^3
-                const float terms[4] = {n2 * gvj, n2 * xj, pn.re * p0[q], -pn.im * p0[q]};
+                const float vj = tb.z, pj = tb.w;
+                part[0] = fmaf(n2, -xj * vj * vj * vj, part[0]);  // -V' = x (a^2+x^2)^-3/2 = -x V^3
+                part[1] = fmaf(n2, xj, part[1]);
+                part[2] = fmaf(pn.re, pj, part[2]);
+                part[3] = fmaf(-pn.im, pj, part[3]);
+                if ((i & 15) == 15 || i == M - 1) {
 #pragma unroll
-                for (int c = 0; c < 4; c++) {  // Kahan
-                    const float y = terms[c] - acc_c[c];
-                    const float s = acc_hi[c] + y;
-                    acc_c[c] = (s - acc_hi[c]) - y;
-                    acc_hi[c] = s;
+                    for (int c = 0; c < 4; c++) {
+                        float s2, e2;
+                        two_sum(acc_hi[c], part[c], s2, e2);
+                        acc_hi[c] = s2;
+                        acc_lo[c] += e2;
+                        part[c] = 0.f;
+                    }
                 }
-                if (j >= lo && j <= hi) pint += n2;
+                if (i >= win_a && i <= win_b) pint += n2;
             }
             if (lane == 0) bfirst[w] = psi[0];
             if (lane == 31) blast[w] = psi[M - 1];
@@ -379,7 +388,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 hs[c] = acc_hi[c];
-                ls[c] = -acc_c[c];
+                ls[c] = acc_lo[c];
             }
 #pragma unroll
             for (int d = 16; d >= 1; d >>= 1)
@@ -468,8 +477,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
 // psi0), so each pass reads one vector per site; the neighbour's V for the off-diagonal factor
 // is carried from the previous iteration.  Rows beyond n-1 have zero tables, which makes y and u
 // exactly 0 there: the last row's super-diagonal then multiplies u_n = 0 and the first row's
-// sub-diagonal an incoming carry of 0, so the sweeps need no boundary tests.  The phase of site
-// i is advanced by a recurrence ph_{i+1} = ph_i e^{i F dt dx} from the thread's first site.
+// sub-diagonal an incoming carry of 0, so the sweeps need no boundary tests.
 template <int M, int T>
 __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
 {
@@ -477,7 +485,7 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
     extern __shared__ float4 tab4[];  // L sites x (1/beta re, im, V, psi0), then psi [L] complex float
     __shared__ cf sc[2 * NW], sb[2 * NW];
     __shared__ float red_hi[NW * 4], red_lo[NW * 4], red_pi[NW];
-    __shared__ cf s_w1;
+    __shared__ cf wtab[M];
     __shared__ float s_ahi, s_alo;
     __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -597,14 +605,21 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
                 o_t[k + 1] = tt;
                 o_e[k + 1] = Fk;
             }
-            if (w == NW - 1 && lane == 31) {
-                const double fdt = Fk * dt;
-                const float a_hi = (float)fdt;
-                s_ahi = a_hi;
-                s_alo = (float)(fdt - (double)a_hi);
-                float sn, cs;
-                sincosf((float)(fdt * G.dx), &sn, &cs);
-                s_w1 = cf{cs, sn};
+            if (w == NW - 1) {
+                // per-site phase factors, each from its own angle: a recurrence in i would carry
+                // the FP32 rounding of |e^{i F dt dx}| (1 +- 6e-8) as a bias growing with i, and it
+                // would compound over the steps into a drift of the norm along each chunk
+                for (int i = lane; i < M; i += 32) {
+                    float sn, cs;
+                    sincosf((float)(Fk * dt * G.dx) * (float)i, &sn, &cs);
+                    wtab[i] = cf{cs, sn};
+                }
+                if (lane == 31) {
+                    const double fdt = Fk * dt;
+                    const float a_hi = (float)fdt;
+                    s_ahi = a_hi;
+                    s_alo = (float)(fdt - (double)a_hi);
+                }
             }
             // ---- pass 1: right-hand side 2 M2 psi, local forward sweep, forward products F
             cf pm = (t == 0) ? cf{0.f, 0.f} : psi[(M - 1) * T + t - 1];
@@ -654,16 +669,14 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
             red = fmaf(-kk, 3.0199159819370158e-07f, red) + th_lo;
             float sn, cs;
             sincosf(red, &sn, &cs);
-            const cf w1 = s_w1;
-            cf ph{cs, sn};
+            const cf phs{cs, sn};
             float ahi[4] = {0.f, 0.f, 0.f, 0.f}, alo[4] = {0.f, 0.f, 0.f, 0.f}, part[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int i = 0; i < M; i++) {
                 const int q = i * T + t;
                 const cf u = cfma(fg[i], uin, yl[i]);
                 const cf d = u - psi[q];
-                const cf pn = cmul(ph, d);
-                ph = cmul(ph, w1);
+                const cf pn = cmul(cmul(phs, wtab[i]), d);
                 psi[q] = pn;
                 const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
                 const float xj = fmaf(dxf, (float)i, xs_hi);

@@ -87,6 +87,12 @@ int grid_for(long long total) { return (int)((total + 255) / 256 < 4096 ? (total
 
 }  // namespace
 
+// the plan cache, for the other FFT users of the library (tdse_analysis.cu)
+int mma_fft_get_plan_d2z(int n, long long idist, long long odist, int batch, cufftHandle* out)
+{
+    return get_plan(CUFFT_D2Z, n, idist, odist, batch, out);
+}
+
 extern "C" int mma_tdse_prepare_fields(const double* raw, int n_batch, int n_raw, int k1, double* interp,
                                        void* stream)
 {

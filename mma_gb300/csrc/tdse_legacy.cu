@@ -400,3 +400,92 @@ extern "C" void free_mtrx(double** buf, int n_rows)
     for (int i = 0; i < n_rows; i++) free(buf[i]);
     free(buf);
 }
+
+// ------------------------------------------------------------------------------------------
+// Analysis exports of the reference DLL (bound in PythonTDSE.py:80-150): host buffers in,
+// malloc'd host results out (freed by free_arr / free_mtrx), computed on the GPU.
+
+// tools.c:206-316 -- the inputs record is passed by value, as in the reference
+extern "C" double* window_analysis(inputs_def inputs, double* psi, int num_E, double dE, double Estep, double E_start)
+{
+    clear_status();
+    if (!psi || num_E < 1 || inputs.num_r < 1 || !(inputs.dx > 0.0)) {
+        set_status(MMA_ERR_ARG, "window_analysis: invalid arguments");
+        return nullptr;
+    }
+    if (!have_device()) return nullptr;
+    const size_t n = (size_t)inputs.num_r + 1;
+    int chunk = num_E < 8192 ? num_E : 8192;
+    const size_t sb = mma_tdse_pes_scratch_bytes(inputs.num_r, chunk);
+    double *d_psi = nullptr, *d_pes = nullptr;
+    void* d_sc = nullptr;
+    double* out = nullptr;
+    int rc;
+    CK(cudaMalloc(&d_psi, sizeof(double) * 2 * n));
+    CK(cudaMalloc(&d_pes, sizeof(double) * num_E));
+    CK(cudaMalloc(&d_sc, sb));
+    CK(cudaMemcpy(d_psi, psi, sizeof(double) * 2 * n, cudaMemcpyHostToDevice));
+    rc = mma_tdse_pes(d_psi, inputs.num_r, inputs.dx, inputs.trg.a, num_E, dE, Estep, E_start, d_pes, d_sc, sb,
+                      nullptr);
+    if (rc != MMA_OK) {
+        set_status(rc, "mma_tdse_pes failed (status %d)", rc);
+        goto fail;
+    }
+    out = static_cast<double*>(malloc(sizeof(double) * num_E));
+    CK(cudaMemcpy(out, d_pes, sizeof(double) * num_E, cudaMemcpyDeviceToHost));
+    cudaFree(d_psi);
+    cudaFree(d_pes);
+    cudaFree(d_sc);
+    return out;
+fail:
+    free(out);
+    if (d_psi) cudaFree(d_psi);
+    if (d_pes) cudaFree(d_pes);
+    if (d_sc) cudaFree(d_sc);
+    return nullptr;
+}
+
+// tools_fftw3.c:158-213 -- rows [N_G][N_freq]
+extern "C" double** GaborTransform(double* signal, double dt, int N, int N_freq, int N_G, double t_min, double t_max,
+                                   double a)
+{
+    clear_status();
+    if (!signal || N < 2 || N_freq < 1 || N_freq > N / 2 + 1 || N_G < 1) {
+        set_status(MMA_ERR_ARG, "GaborTransform: invalid arguments");
+        return nullptr;
+    }
+    if (!have_device()) return nullptr;
+    const size_t sb = mma_gabor_scratch_bytes(1, N, N_G);
+    double *d_sig = nullptr, *d_g = nullptr;
+    void* d_sc = nullptr;
+    double** rows = nullptr;
+    double* h = nullptr;
+    int rc;
+    CK(cudaMalloc(&d_sig, sizeof(double) * N));
+    CK(cudaMalloc(&d_g, sizeof(double) * (size_t)N_G * N_freq));
+    CK(cudaMalloc(&d_sc, sb));
+    CK(cudaMemcpy(d_sig, signal, sizeof(double) * N, cudaMemcpyHostToDevice));
+    rc = mma_gabor(d_sig, N, 1, dt, N, N_freq, N_G, t_min, t_max, a, d_g, d_sc, sb, nullptr);
+    if (rc != MMA_OK) {
+        set_status(rc, "mma_gabor failed (status %d)", rc);
+        goto fail;
+    }
+    h = static_cast<double*>(malloc(sizeof(double) * (size_t)N_G * N_freq));
+    CK(cudaMemcpy(h, d_g, sizeof(double) * (size_t)N_G * N_freq, cudaMemcpyDeviceToHost));
+    rows = static_cast<double**>(malloc(sizeof(double*) * N_G));
+    for (int i = 0; i < N_G; i++) {
+        rows[i] = static_cast<double*>(malloc(sizeof(double) * N_freq));
+        memcpy(rows[i], h + (size_t)i * N_freq, sizeof(double) * N_freq);
+    }
+    free(h);
+    cudaFree(d_sig);
+    cudaFree(d_g);
+    cudaFree(d_sc);
+    return rows;
+fail:
+    free(h);
+    if (d_sig) cudaFree(d_sig);
+    if (d_g) cudaFree(d_g);
+    if (d_sc) cudaFree(d_sc);
+    return nullptr;
+}

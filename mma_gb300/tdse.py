@@ -3,7 +3,8 @@
 ``TDSE_DLL(path)`` binds a shared library that exports the reference DLL's
 legacy symbols -- ``Initialise_grid_and_ground_state``, ``call1DTDSE``,
 ``set_time_and_field``, ``Set_all_prints``, ``inputs_destructor``,
-``outputs_destructor``, ``free_arr``, ``free_mtrx`` -- with the record layouts of
+``outputs_destructor``, ``free_arr``, ``free_mtrx``, ``window_analysis``,
+``GaborTransform`` -- with the record layouts of
 ``mma_gb300.structures``.  With no path it binds this package's GPU library,
 whose legacy symbols run the CUDA kernels.  The same class drives the reference
 DLL built from its own sources, which is how the parity tests and the CPU
@@ -83,6 +84,49 @@ class TDSE_DLL:
 
     def init_prints(self, inputs):
         inputs.Print = self.DLL.Set_all_prints()
+
+    def compute_PES(self, inputs, psi, E_start=-0.6, num_E=10000, epsilon=5e-4, Estep=5e-4):
+        """Photoelectron spectrum of ``psi`` by the resolvent window method
+        (window_analysis, tools.c:206-316; PythonTDSE.py:80-109): returns (E_grid, PES).
+        ``psi``: complex numpy array of num_r + 1 values or a ctypes pointer to interleaved
+        doubles.  ``inputs`` supplies num_r, dx and trg.a (passed by value)."""
+        f = self.DLL.window_analysis
+        f.restype = POINTER(c_double)
+        f.argtypes = [inputs_def, POINTER(c_double), c_int, c_double, c_double, c_double]
+        if isinstance(psi, np.ndarray):
+            il = np.empty(2 * len(psi))
+            il[0::2] = np.real(psi)
+            il[1::2] = np.imag(psi)
+            ptr = il.ctypes.data_as(POINTER(c_double))
+        else:
+            il, ptr = None, psi
+        res = f(inputs, ptr, int(num_E), float(epsilon), float(Estep), float(E_start))
+        self._check("window_analysis")
+        if not res:
+            raise MMAError("window_analysis returned no result")
+        out = np.ctypeslib.as_array(res, shape=(int(num_E),)).copy()
+        self.free_arr(res)
+        return np.linspace(E_start, E_start + (num_E - 1) * Estep, num_E), out
+
+    def gabor_transform(self, signal, dt, N, omega_max, t_min, t_max, N_G, a=8.0):
+        """|Gabor transform| of ``signal`` (GaborTransform, tools_fftw3.c:158-213;
+        PythonTDSE.py:111-150): returns (t grid [N_G], omegas [N_freq], |G| [N_freq, N_G]),
+        with the frequencies 2 pi fftfreq(N, dt) up to omega_max."""
+        f = self.DLL.GaborTransform
+        f.restype = POINTER(POINTER(c_double))
+        f.argtypes = [POINTER(c_double), c_double, c_int, c_int, c_int, c_double, c_double, c_double]
+        omegas = 2 * np.pi * np.fft.fftfreq(int(N), dt)[0:int(N) // 2]
+        sel = omegas <= omega_max
+        n_freq = int(np.count_nonzero(sel))
+        sig = np.ascontiguousarray(signal, dtype=np.float64)
+        res = f(sig.ctypes.data_as(POINTER(c_double)), float(dt), int(N), n_freq, int(N_G), float(t_min),
+                float(t_max), float(a))
+        self._check("GaborTransform")
+        if not res:
+            raise MMAError("GaborTransform returned no result")
+        g = np.stack([np.ctypeslib.as_array(res[i], shape=(n_freq,)).copy() for i in range(int(N_G))])
+        self.free_mtrx(res, int(N_G))
+        return np.linspace(t_min, t_max, int(N_G)), omegas[sel], g.T
 
     def free_mtrx(self, buffer_ptr, N_rows):
         self.DLL.free_mtrx(buffer_ptr, int(N_rows))

@@ -10,6 +10,9 @@ replaced in sys.modules: h5py (file I/O only) and XUV_refractive_index, whose
 dispersion_function/beta_factor_ref return the constant complex index of the
 synthetic medium (n = 1 - 1e-5 + 1e-7 i by default), and `gases`.
 
+Analysis fixtures: the same reference DLL's window_analysis and GaborTransform exports,
+driven by TDSE_DLL.compute_PES / gabor_transform.
+
 Run from the repository root where the reference checkout exists:
     python tests/golden/make_golden.py [--ref /root/reference]
 """
@@ -63,6 +66,44 @@ def make_tdse(ref_src):
             out["tprint"] = kw["tprint"]
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, "Nt", r["Nt"], "Einit", r["Einit"])
+
+
+def analysis_inputs(seed=0):
+    """A synthetic wavefunction (ground-state-like core plus a boosted wavepacket, seeded) for
+    the photoelectron spectrum and a chirped sin^2 pulse for the Gabor transform."""
+    rng = np.random.default_rng(seed)
+    num_r, dx = 800, 0.2
+    x = np.arange(num_r + 1) * dx - 0.5 * num_r * dx
+    psi = (np.exp(-np.abs(x)) + 0.3 * np.exp(-((x - 20.0) / 6.0) ** 2) * np.exp(1j * 0.9 * x)
+           + 0.05 * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size)) * np.exp(-(x / 30.0) ** 2))
+    dt, N = 0.25, 1500
+    t = dt * np.arange(N)
+    sig = np.sin(np.pi * t / (N * dt)) ** 2 * np.cos(0.057 * t + 2e-4 * t ** 2) + 0.02 * rng.standard_normal(N)
+    return num_r, dx, psi, dt, N, sig
+
+
+def make_analysis(ref_src):
+    """PES (window_analysis) and Gabor (GaborTransform) through the reference DLL's own exports."""
+    import oracle
+    from mma_gb300.structures import inputs_def
+    from mma_gb300.tdse import TDSE_DLL
+
+    os.environ["MMA_REF_SRC"] = ref_src
+    oracle.build(ref=True)
+    dll = TDSE_DLL(oracle.ref_dll_path())
+    num_r, dx, psi, dt, N, sig = analysis_inputs()
+    inp = inputs_def()
+    inp.init_default_inputs(num_r=num_r, dx=dx, trg_a=A_CONFIG)
+    pes_kw = dict(E_start=-0.7, num_E=300, epsilon=5e-3, Estep=5e-3)
+    E, P = dll.compute_PES(inp, psi, **pes_kw)
+    gab_kw = dict(omega_max=1.5, t_min=0.0, t_max=N * dt, N_G=64, a=8.0)
+    tg, om, G = dll.gabor_transform(sig, dt, N, **gab_kw)
+    np.savez_compressed(os.path.join(HERE, "analysis.npz"), num_r=num_r, dx=dx, trg_a=A_CONFIG, psi=psi,
+                        E=E, PES=P, dt=dt, N=N, signal=sig, t_gabor=tg, omegas=om, gabor=G,
+                        pes_kw=np.array([pes_kw["E_start"], pes_kw["num_E"], pes_kw["epsilon"], pes_kw["Estep"]]),
+                        gab_kw=np.array([gab_kw["omega_max"], gab_kw["t_min"], gab_kw["t_max"], gab_kw["N_G"],
+                                         gab_kw["a"]]))
+    print("analysis: PES", P.shape, "max", P.max(), "Gabor", G.shape)
 
 
 def import_reference_hankel(ref_root, n_xuv=complex(1 - 1e-5, 1e-7)):
@@ -134,9 +175,11 @@ def make_hankel(ref_root):
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["tdse", "hankel"], default=None)
+    ap.add_argument("--only", choices=["tdse", "hankel", "analysis"], default=None)
     a = ap.parse_args()
     if a.only in (None, "tdse"):
         make_tdse(os.path.join(a.ref, "1DTDSE", "sources"))
     if a.only in (None, "hankel"):
         make_hankel(a.ref)
+    if a.only in (None, "analysis"):
+        make_analysis(os.path.join(a.ref, "1DTDSE", "sources"))
