@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
                                                        __half* Bh, __half* Bl, float* alpha, int64_t rpad,
                                                        int64_t zpad)
 {
-    __shared__ float wmax[2][PREP_THREADS / 32];
+    __shared__ float wmax[2][4][PREP_THREADS / 32];
     const int64_t o = blockIdx.x, Nr = P.n_r, No = P.n_omega;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     float kh, kl;
@@ -380,19 +380,33 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
             wr[i] = (float)(trap_w(rg, r, Nr) * rr);
         }
     }
-    for (int64_t kz = 0; kz < zpad; kz++) {
-        float2 a[2 * PREP_PAIRS];
-        float mx = 0.f;
-        const bool live = kz < P.n_z;
-        const double2 pf = (live && pre) ? pre[kz * No + o] : make_double2(1.0, 0.0);
-        const float2 pr = make_float2((float)pf.x, (float)pf.y);
-        const float2 di = live ? dinv[kz] : make_float2(0.f, 0.f);
+    constexpr int PB = 4;  // planes per iteration: their loads are in flight together, one barrier for all
+    for (int64_t kz0 = 0; kz0 < zpad; kz0 += PB) {
+        float2 a[PB][2 * PREP_PAIRS];
+        float mx[PB];
 #pragma unroll
-        for (int i = 0; i < 2 * PREP_PAIRS; i++) {
-            const int64_t r = 2 * (t + (int64_t)PREP_THREADS * (i / 2)) + (i & 1);
-            a[i] = make_float2(0.f, 0.f);
-            if (live && r < Nr) {
-                const float2 sv = load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r, P.source_c128);
+        for (int u = 0; u < PB; u++) {
+            const int64_t kz = kz0 + u;
+            const bool live = kz < P.n_z;
+#pragma unroll
+            for (int i = 0; i < 2 * PREP_PAIRS; i++) {
+                const int64_t r = 2 * (t + (int64_t)PREP_THREADS * (i / 2)) + (i & 1);
+                a[u][i] = (live && r < Nr) ? load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r,
+                                                        P.source_c128)
+                                           : make_float2(0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < PB; u++) {
+            const int64_t kz = kz0 + u;
+            const bool live = kz < P.n_z;
+            const double2 pf = (live && pre) ? pre[kz * No + o] : make_double2(1.0, 0.0);
+            const float2 pr = make_float2((float)pf.x, (float)pf.y);
+            const float2 di = live ? dinv[kz] : make_float2(0.f, 0.f);
+            mx[u] = 0.f;
+#pragma unroll
+            for (int i = 0; i < 2 * PREP_PAIRS; i++) {
+                const float2 sv = a[u][i];
                 float2 v = make_float2(fmaf(pr.x, sv.x, -pr.y * sv.y), fmaf(pr.x, sv.y, pr.y * sv.x));
                 if (P.near_field) {
                     const float th = kr2h[i] * di.x;
@@ -401,33 +415,39 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
                     sincosf(reduce_2pi(th, te), &sn, &cs);  // e^{-i theta}
                     v = make_float2(fmaf(v.x, cs, v.y * sn), fmaf(v.y, cs, -v.x * sn));
                 }
-                a[i] = make_float2(v.x * wr[i], v.y * wr[i]);
-                mx = fmaxf(mx, fmaxf(fabsf(a[i].x), fabsf(a[i].y)));
+                a[u][i] = make_float2(v.x * wr[i], v.y * wr[i]);  // zero beyond n_r (wr = 0, source 0)
+                mx[u] = fmaxf(mx[u], fmaxf(fabsf(a[u][i].x), fabsf(a[u][i].y)));
             }
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) mx[u] = fmaxf(mx[u], __shfl_xor_sync(0xffffffffu, mx[u], d));
         }
+        const int par = (int)((kz0 / PB) & 1);
+        if (lane == 0)
 #pragma unroll
-        for (int d = 16; d >= 1; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
-        const int par = (int)(kz & 1);
-        if (lane == 0) wmax[par][w] = mx;
+            for (int u = 0; u < PB; u++) wmax[par][u][w] = mx[u];
         __syncthreads();
-        float al = 0.f;
 #pragma unroll
-        for (int q = 0; q < PREP_THREADS / 32; q++) al = fmaxf(al, wmax[par][q]);
-        const float sc = al > 0.f ? 1.0f / al : 0.f;
-        if (t == 0) alpha[o * zpad + kz] = al;
+        for (int u = 0; u < PB; u++) {
+            const int64_t kz = kz0 + u;
+            float al = 0.f;
 #pragma unroll
-        for (int p = 0; p < PREP_PAIRS; p++) {
-            const int64_t r0 = 2 * (t + (int64_t)PREP_THREADS * p);
-            if (r0 >= rpad) continue;
+            for (int q = 0; q < PREP_THREADS / 32; q++) al = fmaxf(al, wmax[par][u][q]);
+            const float sc = al > 0.f ? 1.0f / al : 0.f;
+            if (t == 0) alpha[o * zpad + kz] = al;
 #pragma unroll
-            for (int c = 0; c < 2; c++) {
-                const float x0 = (c ? a[2 * p].y : a[2 * p].x) * sc;
-                const float x1 = (c ? a[2 * p + 1].y : a[2 * p + 1].x) * sc;
-                const __half h0 = __float2half_rn(x0), h1 = __float2half_rn(x1);
-                const __half l0 = __float2half_rn(x0 - __half2float(h0)), l1 = __float2half_rn(x1 - __half2float(h1));
-                const int64_t idx = ((o * 2 * zpad + 2 * kz + c) * rpad + r0) / 2;
-                reinterpret_cast<__half2*>(Bh)[idx] = __halves2half2(h0, h1);
-                reinterpret_cast<__half2*>(Bl)[idx] = __halves2half2(l0, l1);
+            for (int pp = 0; pp < PREP_PAIRS; pp++) {
+                const int64_t r0 = 2 * (t + (int64_t)PREP_THREADS * pp);
+                if (r0 >= rpad) continue;
+#pragma unroll
+                for (int c = 0; c < 2; c++) {
+                    const float x0 = (c ? a[u][2 * pp].y : a[u][2 * pp].x) * sc;
+                    const float x1 = (c ? a[u][2 * pp + 1].y : a[u][2 * pp + 1].x) * sc;
+                    const __half h0 = __float2half_rn(x0), h1 = __float2half_rn(x1);
+                    const __half l0 = __float2half_rn(x0 - __half2float(h0)), l1 = __float2half_rn(x1 - __half2float(h1));
+                    const int64_t idx = ((o * 2 * zpad + 2 * kz + c) * rpad + r0) / 2;
+                    reinterpret_cast<__half2*>(Bh)[idx] = __halves2half2(h0, h1);
+                    reinterpret_cast<__half2*>(Bl)[idx] = __halves2half2(l0, l1);
+                }
             }
         }
     }
