@@ -19,9 +19,12 @@ Same names, arguments and results as the reference module:
 
 Refractive index: the reference reads f1/f2 tables through XUV_refractive_index
 (HDF5).  Here ``XUV_index`` is a provider with the same two functions; by default it
-models a constant complex XUV index (``XUV_index.set_constant_index``).
+models a constant complex XUV index (``XUV_index.set_constant_index``);
+``XUV_index.load_tables(directory)`` reads the CXRO/NIST text tables those HDF5 tables are
+made from.
 """
 import ctypes
+import os
 from ctypes import POINTER, Structure, c_double, c_int, c_int64, c_size_t, c_void_p
 
 import numpy as np
@@ -90,23 +93,123 @@ def _check(rc, what):
 
 
 # ------------------------------------------------------------------------------ refractive index
+# physical constants of shared_python/units.py:3-7,16-19 (the reference's values)
+_HBAR, _INV_ALPHA, _ELCHARGE, _ELMASS = 1.0545718e-34, 137.035999139, 1.602176565e-19, 9.10938356e-31
+_ALPHA = 1.0 / _INV_ALPHA
+_R_BOHR = _HBAR * _INV_ALPHA / (C_LIGHT * _ELMASS)
+_R_ELECTRON = _R_BOHR * _ALPHA ** 2
+_TIME_AU = _ELMASS * _R_BOHR ** 2 / _HBAR
+N_REF_DEFAULT = 2.7e25  # XUV_refractive_index.py:122
+
+# tabulated scattering factors: gas -> files, in the directory layout of shared_python/XUV_tables
+TABLE_FILES = {
+    "He_Henke": ("he.nff",), "Ne_Henke": ("ne.nff",), "Ar_Henke": ("ar.nff",), "Kr_Henke": ("kr.nff",),
+    "Xe_Henke": ("xe.nff",),
+    "He_NIST": ("he_f1_NIST.txt", "he_f2_NIST.txt"), "Ne_NIST": ("ne_f1_NIST.txt", "ne_f2_NIST.txt"),
+    "Ar_NIST": ("ar_f1_NIST.txt", "ar_f2_NIST.txt"), "Kr_NIST": ("kr_f1_NIST.txt", "kr_f2_NIST.txt"),
+    "Xe_NIST": ("xe_f1_NIST.txt", "xe_f2_NIST.txt"),
+}
+
+
+def _omega_si_to_ev(omega):
+    """mynumerics.ConvertPhoton(omega, 'omegaSI', 'eV') (mynumerics.py:313,325)."""
+    return np.asarray(omega, dtype=float) * _TIME_AU / (_ELCHARGE / (_ELMASS * _ALPHA ** 2 * C_LIGHT ** 2))
+
+
+def _omega_si_to_lambda(omega):
+    """mynumerics.ConvertPhoton(omega, 'omegaSI', 'lambdaSI') (mynumerics.py:313,322)."""
+    w_au = np.asarray(omega, dtype=float) * _TIME_AU
+    return 2.0 * np.pi * _HBAR / (w_au * _ELMASS * C_LIGHT * _ALPHA ** 2)
+
+
+def _read_columns(path, skip, cols):
+    """Rows of whitespace-separated numbers after `skip` header lines, blank lines ignored (the
+    parsing of shared_python/make_table.py)."""
+    out = []
+    with open(path) as f:
+        for k, line in enumerate(f):
+            parts = line.split()
+            if k < skip or not parts:
+                continue
+            out.append([float(parts[c]) for c in cols])
+    return np.asarray(out, dtype=float)
+
+
 class _XUVIndex:
-    """Stand-in for XUV_refractive_index (dispersion_function :125, beta_factor_ref :164) with
-    a constant complex index n = n0 + i beta per reference density; the dispersion term
-    scales with pressure like the tabulated one."""
+    """XUV refractive index provider with the interface of the reference's XUV_refractive_index
+    (gases, dispersion_function :125-161, beta_factor_ref :164-194).
+
+    Two sources:
+    * ``set_constant_index(n)``: a constant complex index n = n0 + i beta per reference density
+      (the dispersion term scales with pressure like the tabulated one) -- the default;
+    * ``load_tables(directory)``: the tabulated scattering factors f1, f2 of the CXRO (Henke,
+      ``*.nff``: E [eV], f1, f2 after one header line) and NIST (``*_f1_NIST.txt``,
+      ``*_f2_NIST.txt``: E [keV], f after three header lines) tables in the directory layout of
+      shared_python/XUV_tables, linearly interpolated in photon energy (ValueError outside the
+      table), with n_XUV = 1 - p N_ref r_e lambda^2 f1/(2 pi) and beta = N_ref r_e lambda^2 f2/(2 pi).
+    """
 
     def __init__(self):
         self.set_constant_index(complex(1 - 1e-5, 1e-7))
 
     def set_constant_index(self, n, gases=("Ar_Henke", "Ar_NIST", "Ne_Henke", "He_Henke", "Kr_Henke", "Xe_Henke")):
+        self.mode = "constant"
         self.n = complex(n)
         self.gases = list(gases)
+        self.tables = {}
 
-    def dispersion_function(self, omega, pressure, gas, n_IR=1.0):
-        return pressure * (n_IR - self.n.real) / C_LIGHT * np.ones_like(np.asarray(omega, dtype=float))
+    def load_tables(self, directory, gases=None):
+        tables = {}
+        for gas, files in TABLE_FILES.items():
+            if gases is not None and gas not in gases:
+                continue
+            paths = [os.path.join(directory, f) for f in files]
+            if not all(os.path.exists(p) for p in paths):
+                continue
+            if len(files) == 1:
+                t = _read_columns(paths[0], 1, (0, 1, 2))
+                tables[gas] = (t[:, 0], t[:, 1], t[:, 0], t[:, 2])
+            else:
+                t1 = _read_columns(paths[0], 3, (0, 1))
+                t2 = _read_columns(paths[1], 3, (0, 1))
+                tables[gas] = (1e3 * t1[:, 0], t1[:, 1], 1e3 * t2[:, 0], t2[:, 1])
+        if not tables:
+            raise FileNotFoundError("no scattering-factor tables found in %s" % directory)
+        self.mode = "tables"
+        self.tables = tables
+        self.gases = sorted(tables)
 
-    def beta_factor_ref(self, omega, gas):
-        return self.n.imag * np.ones_like(np.asarray(omega, dtype=float))
+    @staticmethod
+    def _interp(E, x, y):
+        E = np.asarray(E, dtype=float)
+        if np.any(E < x[0]) or np.any(E > x[-1]):
+            raise ValueError("photon energy outside the scattering-factor table")
+        return np.interp(E, x, y)
+
+    def getf1(self, gas, E):
+        x1, f1, _, _ = self.tables[gas]
+        return self._interp(E, x1, f1)
+
+    def getf2(self, gas, E):
+        _, _, x2, f2 = self.tables[gas]
+        return self._interp(E, x2, f2)
+
+    def dispersion_function(self, omega, pressure, gas, n_IR=1.0, N_ref=N_REF_DEFAULT):
+        if self.mode == "constant":
+            return pressure * (n_IR - self.n.real) / C_LIGHT * np.ones_like(np.asarray(omega, dtype=float))
+        f1 = self.getf1(gas, _omega_si_to_ev(omega))
+        if np.any(f1 < -9998.0):
+            raise ValueError("f1-scattering coefficient not listed for this frequency.")
+        lam = _omega_si_to_lambda(omega)
+        n_xuv = 1.0 - pressure * N_ref * _R_ELECTRON * (lam ** 2 * f1 / (2.0 * np.pi))
+        return 1.0 / (C_LIGHT / n_IR) - 1.0 / (C_LIGHT / n_xuv)
+
+    def beta_factor_ref(self, omega, gas, N_ref=N_REF_DEFAULT):
+        if self.mode == "constant":
+            return self.n.imag * np.ones_like(np.asarray(omega, dtype=float))
+        f2 = self.getf2(gas, _omega_si_to_ev(omega))
+        lam = _omega_si_to_lambda(omega)
+        return N_ref * _R_ELECTRON * (lam ** 2 * f2 / (2.0 * np.pi))
 
 
 XUV_index = _XUVIndex()

@@ -13,6 +13,10 @@ synthetic medium (n = 1 - 1e-5 + 1e-7 i by default), and `gases`.
 Analysis fixtures: the same reference DLL's window_analysis and GaborTransform exports,
 driven by TDSE_DLL.compute_PES / gabor_transform.
 
+Refractive-index fixture: the reference's shared_python/make_table.py and
+XUV_refractive_index.py run unchanged on synthetic tables (xuv_tables/, written here) with an
+in-memory stand-in for h5py.
+
 Run from the repository root where the reference checkout exists:
     python tests/golden/make_golden.py [--ref /root/reference]
 """
@@ -106,6 +110,110 @@ def make_analysis(ref_src):
     print("analysis: PES", P.shape, "max", P.max(), "Gabor", G.shape)
 
 
+XUV_GASES = {"he": 2.0, "ne": 10.0, "ar": 18.0, "kr": 36.0, "xe": 54.0}
+
+
+def write_xuv_tables(directory):
+    """Synthetic scattering-factor tables (smooth functions of the photon energy, this file's
+    own numbers) in the two text formats of the reference's table directory: Henke ``*.nff``
+    (one header line; E [eV], f1, f2; f1 = -9999 where not listed) and NIST ``*_f1_NIST.txt`` /
+    ``*_f2_NIST.txt`` (three header lines and a blank one; E [keV], f)."""
+    os.makedirs(directory, exist_ok=True)
+    E = np.geomspace(10.0, 200.0, 48)
+    for g, Z in XUV_GASES.items():
+        f1 = Z * (1.0 - np.exp(-E / 50.0)) + 0.3 * np.sin(E / 7.0)
+        f1[E < 18.0] = -9999.0
+        f2 = Z * np.exp(-E / 40.0) * (E / 30.0)
+        with open(os.path.join(directory, g + ".nff"), "w") as f:
+            f.write("E(eV)\tf1\tf2\n")
+            for e, a, b in zip(E, f1, f2):
+                f.write("%.4f\t%.6g\t%.6E\n" % (e, a, b))
+        for which, val in (("f1", Z * (1.0 - np.exp(-E / 45.0)) - 0.2 * np.cos(E / 9.0)), ("f2", 1.1 * f2)):
+            with open(os.path.join(directory, "%s_%s_NIST.txt" % (g, which)), "w") as f:
+                f.write("synthetic table\n    E              %s\n   keV           e atom-1\n\n" % which)
+                for e, v in zip(E, val):
+                    f.write("%.6E  %.5E\n" % (1e-3 * e, v))
+
+
+class _MemH5:
+    """In-memory stand-in for the two h5py calls of the reference's table scripts: File(...) in
+    write mode (create_group, create_dataset, attrs) records the archive, read mode serves it."""
+    store = {}
+
+    class Dataset:
+        def __init__(self, data):
+            self.data = np.asarray(data)
+            self.attrs = {}
+
+        def __getitem__(self, k):
+            return self.data[k]
+
+    class Group(dict):
+        def create_dataset(self, name, data=None):
+            d = _MemH5.Dataset(data)
+            self[name] = d
+            return d
+
+    class File:
+        def __init__(self, path, mode="r"):
+            key = os.path.basename(path)
+            if mode == "w":
+                _MemH5.store[key] = {}
+            self.data = _MemH5.store[key]
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            return False
+
+        def create_group(self, name):
+            g = _MemH5.Group()
+            self.data[name] = g
+            return g
+
+        def keys(self):
+            return self.data.keys()
+
+        def __getitem__(self, k):
+            return self.data[k]
+
+
+def make_xuv(ref_root):
+    """Tabulated refractive index: the reference's make_table.py (text tables -> archive) and
+    XUV_refractive_index.py (archive -> dispersion_function, beta_factor_ref), run unchanged on
+    the synthetic tables committed in xuv_tables/ with the in-memory h5py stand-in."""
+    import runpy
+    import shutil
+    import tempfile
+
+    tables = os.path.join(HERE, "xuv_tables")
+    write_xuv_tables(tables)
+    mod = types.ModuleType("h5py")
+    mod.File = _MemH5.File
+    sys.modules["h5py"] = mod
+    sp = os.path.join(ref_root, "shared_python")
+    sys.path.insert(0, sp)
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        shutil.copytree(tables, os.path.join(d, "XUV_tables"))
+        os.chdir(d)
+        try:
+            runpy.run_path(os.path.join(sp, "make_table.py"), run_name="__main__")
+        finally:
+            os.chdir(cwd)
+    sys.modules.pop("XUV_refractive_index", None)
+    import XUV_refractive_index as XR
+
+    omega = np.geomspace(20.0, 190.0, 9) * 1.602176565e-19 / 1.0545718e-34  # photon energies 20..190 eV
+    out = dict(omega=omega, gases=np.array(sorted(XR.gases)))
+    for g in sorted(XR.gases):
+        out["disp_" + g] = np.array([XR.dispersion_function(w, 0.7, g, n_IR=1.0003) for w in omega])
+        out["beta_" + g] = np.array([XR.beta_factor_ref(w, g) for w in omega])
+    np.savez_compressed(os.path.join(HERE, "xuv_index.npz"), **out)
+    print("xuv index:", sorted(XR.gases))
+
+
 def import_reference_hankel(ref_root, n_xuv=complex(1 - 1e-5, 1e-7)):
     """Import Hankel_transform.py from the reference with the two stubs described above."""
     sys.modules["h5py"] = types.ModuleType("h5py")
@@ -175,7 +283,7 @@ def make_hankel(ref_root):
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["tdse", "hankel", "analysis"], default=None)
+    ap.add_argument("--only", choices=["tdse", "hankel", "analysis", "xuv"], default=None)
     a = ap.parse_args()
     if a.only in (None, "tdse"):
         make_tdse(os.path.join(a.ref, "1DTDSE", "sources"))
@@ -183,3 +291,5 @@ if __name__ == "__main__":
         make_hankel(a.ref)
     if a.only in (None, "analysis"):
         make_analysis(os.path.join(a.ref, "1DTDSE", "sources"))
+    if a.only in (None, "xuv"):
+        make_xuv(a.ref)
