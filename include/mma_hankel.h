@@ -27,12 +27,15 @@ typedef struct mma_hankel_problem {
     int64_t source_c128;              /* 0 = complex64 source, 1 = complex128 */
     int64_t plane_stride;             /* source elements between planes k */
     int64_t omega_stride;             /* source elements between frequencies; r is contiguous */
+    int64_t pre_radial;               /* 0: pre [n_z][n_omega]; 1: pre [n_z][n_omega][n_r] (radially modulated
+                                         medium, Hankel_transform.py:244-399, applied per radius as in :505-512) */
 } mma_hankel_problem;
 
 /* Inputs common to both forms:
  *   ogrid [n_omega], rgrid [n_r], zgrid [n_z], rho [n_rho]    float64 grids
  *   source                                                    S[k][w][r] with the strides above
- *   pre     [n_z][n_omega] complex128 pre-factor, or NULL for 1 (get_propagation_pre_factor_function)
+ *   pre     [n_z][n_omega] complex128 pre-factor, or NULL for 1 (get_propagation_pre_factor_function);
+ *           with pre_radial = 1, [n_z][n_omega][n_r]
  * Outputs:
  *   ff      [n_rho][n_omega] complex128                        FF_integrated
  *   plane_slot [n_z] int64 (or NULL): slot of plane k in `planes`, -1 = not stored;

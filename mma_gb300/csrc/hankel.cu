@@ -38,12 +38,11 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(mma_hankel_problem P, c
     for (int64_t kz = 0; kz < Nz; kz++) {
         const double D = P.distance - zg[kz];
         const double tau = trap_w(zg, kz, Nz);
-        const double2 pf = pre ? pre[kz * No + o] : make_double2(1.0, 0.0);
         __syncthreads();
         for (int64_t r = threadIdx.x; r < Nr; r += blockDim.x) {
             const double rr = rg[r];
             const double2 s = load_src_d(src, kz * P.plane_stride + o * P.omega_stride + r, P.source_c128);
-            double2 a = pf;
+            double2 a = pre_at(P, pre, kz, o, r);  // the radial factor first, as in :505-512
             if (P.near_field) {  // exp(-1j k r^2 / (2 D)), Hankel_transform.py:506
                 double sn, cs;
                 sincos(-((k * (rr * rr)) / (2.0 * D)), &sn, &cs);
@@ -117,7 +116,7 @@ __global__ void __launch_bounds__(kThreads) fast_stage1(mma_hankel_problem P, co
     float2* pr = reinterpret_cast<float2*>(smem + ((Nz * RW + 1) / 2) * 2);  // Nz: pre-factor
     for (int64_t q = threadIdx.x; q < Nz * RW; q += blockDim.x) tabs[q] = ptab[q];
     for (int64_t q = threadIdx.x; q < Nz; q += blockDim.x) {
-        const double2 pf = pre ? pre[q * No + o] : make_double2(1.0, 0.0);
+        const double2 pf = (pre && !P.pre_radial) ? pre[q * No + o] : make_double2(1.0, 0.0);
         pr[q] = make_float2((float)pf.x, (float)pf.y);
     }
     __syncthreads();
@@ -147,7 +146,11 @@ __global__ void __launch_bounds__(kThreads) fast_stage1(mma_hankel_problem P, co
             const int64_t kz = k0 + u;
             if (kz >= Nz) break;
             const float* row = tabs + kz * RW;
-            const float2 pf = pr[kz];
+            float2 pf = pr[kz];
+            if (P.pre_radial) {
+                const double2 pd = pre_at(P, pre, kz, o, r);
+                pf = make_float2((float)pd.x, (float)pd.y);
+            }
             float2 a = make_float2(fmaf(pf.x, sv[u].x, -pf.y * sv[u].y), fmaf(pf.x, sv[u].y, pf.y * sv[u].x));
             if (P.near_field) {
                 const float ih = row[MM], il = row[MM + 1];
@@ -269,7 +272,6 @@ __global__ void __launch_bounds__(kThreads) fast_planes(mma_hankel_problem P, co
         if (slot[q] == want) kz = q;
     if (kz < 0) return;  // uniform over the CTA
     const double k = og[o] / kC, D = P.distance - zg[kz];
-    const double2 pf = pre ? pre[kz * No + o] : make_double2(1.0, 0.0);
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float rh = 0.f, rl = 0.f;
     if (j < Nrho) split_d(rho[j], rh, rl);
@@ -282,7 +284,7 @@ __global__ void __launch_bounds__(kThreads) fast_planes(mma_hankel_problem P, co
             const int64_t r = r0 + q;
             const double rr = rg[r];
             const double2 sd = load_src_d(src, kz * P.plane_stride + o * P.omega_stride + r, P.source_c128);
-            double2 a = pf;
+            double2 a = pre_at(P, pre, kz, o, r);
             if (P.near_field) {
                 double sn, cs;
                 sincos(-((k * (rr * rr)) / (2.0 * D)), &sn, &cs);

@@ -101,6 +101,15 @@ __device__ __forceinline__ void ff_acc(float& hi, float& lo, float part)
     lo += e;
 }
 
+// pre-factor of plane kz, frequency o, radius r: per (plane, frequency) or, for a radially
+// modulated medium, per (plane, frequency, radius); NULL means 1
+__device__ __forceinline__ double2 pre_at(const mma_hankel_problem& P, const double2* pre, int64_t kz, int64_t o,
+                                          int64_t r)
+{
+    if (!pre) return make_double2(1.0, 0.0);
+    return P.pre_radial ? pre[(kz * P.n_omega + o) * P.n_r + r] : pre[kz * P.n_omega + o];
+}
+
 inline bool valid(const mma_hankel_problem* p)
 {
     return p && p->n_omega > 0 && p->n_r > 1 && p->n_z > 0 && p->n_rho > 0 && p->distance == p->distance &&

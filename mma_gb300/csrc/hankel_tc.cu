@@ -400,13 +400,21 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
         for (int u = 0; u < PB; u++) {
             const int64_t kz = kz0 + u;
             const bool live = kz < P.n_z;
-            const double2 pf = (live && pre) ? pre[kz * No + o] : make_double2(1.0, 0.0);
-            const float2 pr = make_float2((float)pf.x, (float)pf.y);
+            const double2 pf = (live && pre && !P.pre_radial) ? pre[kz * No + o] : make_double2(1.0, 0.0);
+            const float2 pr0 = make_float2((float)pf.x, (float)pf.y);
             const float2 di = live ? dinv[kz] : make_float2(0.f, 0.f);
             mx[u] = 0.f;
 #pragma unroll
             for (int i = 0; i < 2 * PREP_PAIRS; i++) {
                 const float2 sv = a[u][i];
+                float2 pr = pr0;
+                if (P.pre_radial && live) {
+                    const int64_t r = 2 * (t + (int64_t)PREP_THREADS * (i / 2)) + (i & 1);
+                    if (r < Nr) {
+                        const double2 pd = pre_at(P, pre, kz, o, r);
+                        pr = make_float2((float)pd.x, (float)pd.y);
+                    }
+                }
                 float2 v = make_float2(fmaf(pr.x, sv.x, -pr.y * sv.y), fmaf(pr.x, sv.y, pr.y * sv.x));
                 if (P.near_field) {
                     const float th = kr2h[i] * di.x;

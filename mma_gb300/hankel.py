@@ -39,7 +39,7 @@ C_LIGHT = 299792458.0  # shared_python/units.py:3
 class HankelProblem(Structure):
     _fields_ = [("n_omega", c_int64), ("n_r", c_int64), ("n_z", c_int64), ("n_rho", c_int64), ("distance", c_double),
                 ("near_field", c_int64), ("source_c128", c_int64), ("plane_stride", c_int64),
-                ("omega_stride", c_int64)]
+                ("omega_stride", c_int64), ("pre_radial", c_int64)]
 
 
 class FastPlan(Structure):
@@ -262,13 +262,23 @@ def get_propagation_pre_factor_function(zgrid, rgrid, ogrid, preset_gas="vacuum"
                                         absorption_tables="Henke", include_absorption=True, dispersion_tables="Henke",
                                         include_dispersion=True, effective_IR_refrective_index=1.0):
     """(pre_factor, exp_renorm) as in Hankel_transform.py:85-448 (no-modulation :405-448,
-    z-modulation :146-239).  Returns numpy closures; ``pre_table`` gives [Nz, No]."""
+    z-modulation :146-239, radially modulated :242-399).  Returns numpy closures; pre_factor(kz)
+    is [Nr, No] (the orientation HankelTransform reads, :505-512); ``pre_table`` gives [Nz, No]
+    or [Nz, No, Nr].  A radially modulated medium has no renormalisation (None), as in the
+    reference."""
     pre_tab, renorm_tab = pre_factor_table(zgrid, ogrid, preset_gas, pressure, absorption_tables, include_absorption,
-                                           dispersion_tables, include_dispersion, effective_IR_refrective_index)
+                                           dispersion_tables, include_dispersion, effective_IR_refrective_index,
+                                           rgrid=rgrid)
     Nr = len(rgrid)
 
     def pre_factor(kz):
+        if pre_tab.ndim == 3:
+            return pre_tab[kz].T
         return np.outer(np.ones(Nr), pre_tab[kz])
+
+    pre_factor.pre_table = pre_tab
+    if renorm_tab is None:
+        return pre_factor, None
 
     def exp_renorm(kz):
         return renorm_tab[kz]
@@ -278,16 +288,84 @@ def get_propagation_pre_factor_function(zgrid, rgrid, ogrid, preset_gas="vacuum"
     return pre_factor, exp_renorm
 
 
+def _radial_pre_factor(z, r, w, gas, pressure, absorption_tables, include_absorption, dispersion_tables,
+                       include_dispersion, n_ir):
+    """[Nz, No, Nr] pre-factor of a radially modulated medium (Hankel_transform.py:242-399).
+
+    * zr branch (pressure with 'zgrid', 'rgrid', 'value'[Nz_table, Nr_table], :302-399): the
+      pressure rows interpolated in r onto the computational radii (edge values outside), then per
+      radius the pressure interpolated onto the planes and, per frequency, the cumulative
+      trapezoid along the table's z of the dispersion function and of the pressure (absorption,
+      with beta of the *dispersion* tables as in :366-370), interpolated onto the planes:
+          pre[z, w, r] = p(z, r) exp(w (i int disp dz + (1/c) beta int p dz)).
+    * r branch (pressure with 'rgrid', 'value'[Nr_table], :242-299): a radial profile constant
+      along z.  The reference's branch does not run (it indexes with k1 before defining it, :250,
+      and uses an undefined dispersion_factor, :295); this implements its evident intent, the
+      no-modulation formula (:405-448) with the local pressure p(r).
+    The reference returns the zr table per plane as [omega, r] while HankelTransform reads it as
+    [r, omega] (:505-512); here the factor of (plane, frequency, radius) multiplies that radius's
+    integrand, which is what both functions describe."""
+    from scipy import integrate, interpolate
+
+    pr_r = np.asarray(pressure["rgrid"], dtype=np.float64)
+    val = np.asarray(pressure["value"], dtype=np.float64)
+    Nz, No, Nr = len(z), len(w), len(r)
+    pre = np.empty((Nz, No, Nr), dtype=np.complex128)
+
+    def on_r(row):  # :247-254, :316-323
+        return interpolate.interp1d(pr_r, row, bounds_error=False, fill_value=(row[0], row[-1]), copy=False)(r)
+
+    if "zgrid" not in pressure:
+        p_r = on_r(val if val.ndim == 1 else val[0])
+        beta = XUV_index.beta_factor_ref(w, gas + "_" + absorption_tables) if include_absorption else None
+        for kr in range(Nr):
+            if include_dispersion:
+                disp = 1j * XUV_index.dispersion_function(w, p_r[kr], gas + "_" + dispersion_tables, n_IR=n_ir)
+            else:
+                disp = 1j * (n_ir - 1.0) / C_LIGHT * np.ones_like(w)
+            absorb = (p_r[kr] / C_LIGHT) * beta if include_absorption else np.zeros_like(w)
+            pre[:, :, kr] = p_r[kr] * np.exp(w[None, :] * (z[:, None] * disp[None, :] +
+                                                          (z[:, None] - z[-1]) * absorb[None, :]))
+        return pre
+    pz = np.asarray(pressure["zgrid"], dtype=np.float64)
+    p_rg = np.stack([on_r(val[k]) for k in range(len(pz))])  # [Nz_table, Nr]
+    beta_d = XUV_index.beta_factor_ref(w, gas + "_" + dispersion_tables) if include_absorption else None
+    for kr in range(Nr):
+        col = p_rg[:, kr]
+        p_loc = interpolate.interp1d(pz, col, bounds_error=False, fill_value=(col[0], col[-1]), copy=False)(z)
+        if include_dispersion:
+            dfun = XUV_index.dispersion_function(w[:, None], col[None, :], gas + "_" + dispersion_tables, n_IR=n_ir)
+            integ = integrate.cumulative_trapezoid(np.broadcast_to(dfun, (No, len(pz))), x=pz, initial=0.0, axis=1)
+            disp = 1j * interpolate.interp1d(pz, integ, axis=1, bounds_error=False,
+                                             fill_value=(integ[:, 0], integ[:, -1]), copy=False)(z)
+        else:
+            disp = 1j * (n_ir - 1.0) / C_LIGHT * np.ones((No, Nz))
+        if include_absorption:
+            ib = beta_d[:, None] * integrate.cumulative_trapezoid(col, x=pz, initial=0.0)[None, :]
+            absf = (1.0 / C_LIGHT) * interpolate.interp1d(pz, ib, axis=1, bounds_error=False,
+                                                          fill_value=(ib[:, 0], ib[:, -1]), copy=False)(z)
+        else:
+            absf = 0.0
+        pre[:, :, kr] = (p_loc[None, :] * np.exp(w[:, None] * (disp + absf))).T
+    return pre
+
+
 def pre_factor_table(zgrid, ogrid, preset_gas="vacuum", pressure=1.0, absorption_tables="Henke",
                      include_absorption=True, dispersion_tables="Henke", include_dispersion=True,
-                     effective_IR_refrective_index=1.0):
-    """[Nz, No] pre-factor and renormalisation tables (the reference's closures evaluated)."""
+                     effective_IR_refrective_index=1.0, rgrid=None):
+    """Pre-factor and renormalisation tables (the reference's closures evaluated): [Nz, No], or
+    [Nz, No, Nr] for a radially modulated medium (pressure with 'rgrid'; needs `rgrid`; no
+    renormalisation, as in the reference)."""
     z = np.asarray(zgrid, dtype=np.float64)
     w = np.asarray(ogrid, dtype=np.float64)
     n_ir = effective_IR_refrective_index
     if isinstance(pressure, dict):
         if "rgrid" in pressure:
-            raise NotImplementedError("radially modulated density (r and zr branches) is not implemented")
+            if rgrid is None:
+                raise ValueError("a radially modulated medium needs the radial grid")
+            return _radial_pre_factor(z, np.asarray(rgrid, dtype=np.float64), w, preset_gas, pressure,
+                                      absorption_tables, include_absorption, dispersion_tables, include_dispersion,
+                                      n_ir), None
         from scipy import integrate, interpolate
 
         pz, pv = np.asarray(pressure["zgrid"]), np.asarray(pressure["value"])
@@ -349,8 +427,11 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
     if len(zgrid) != Nz or len(ogrid) != No or len(rgrid) != Nr:
         raise ValueError("source shape does not match the grids")
     S = source.contiguous()
+    radial = pre_table is not None and np.ndim(pre_table) == 3
+    if pre_table is not None and tuple(np.shape(pre_table)) not in ((Nz, No), (Nz, No, Nr)):
+        raise ValueError("pre-factor must be [Nz, No] or [Nz, No, Nr]")
     prob = HankelProblem(No, Nr, Nz, len(rho), float(distance), int(bool(near_field)),
-                         int(S.dtype == torch.complex128), No * Nr, Nr)
+                         int(S.dtype == torch.complex128), No * Nr, Nr, int(radial))
     og, rg, zg, rh = (_dev(a, dev) for a in (ogrid, rgrid, zgrid, rho))
     pre = None
     if pre_table is not None:
@@ -421,10 +502,8 @@ def HankelTransform(ogrid, rgrid, FField, distance, rgrid_FF, integrator=trapezo
         raise NotImplementedError("only the trapezoidal radial integrator is implemented")
     pre = None
     pf = np.asarray(pre_factor)
-    if pf.ndim == 2:
-        if not np.allclose(pf, pf[:1, :]):
-            raise NotImplementedError("radially varying pre-factors are not implemented")
-        pre = pf[0][None, :]
+    if pf.ndim == 2:  # pre_factor[r, omega] (:505-512)
+        pre = pf[0][None, :] if np.all(pf == pf[:1, :]) else np.ascontiguousarray(pf.T)[None, :, :]
     elif pf.ndim == 0 and pf != 1.0:
         pre = np.full((1, len(ogrid)), complex(pf))
     src = FField if torch.is_tensor(FField) else torch.from_numpy(np.ascontiguousarray(FField))
@@ -472,7 +551,7 @@ class Hankel_long:
             raise NotImplementedError("Renormalisation of the signal is not implemented for radially modulated density.")
         pre, renorm = pre_factor_table(target.zgrid, target.ogrid, preset_gas, pressure, absorption_tables,
                                        include_absorption, dispersion_tables, include_dispersion,
-                                       effective_IR_refrective_index)
+                                       effective_IR_refrective_index, rgrid=target.rgrid)
         z = np.asarray(target.zgrid, dtype=np.float64)
         Nz = len(z)
         if Nz < 2:

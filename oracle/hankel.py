@@ -65,8 +65,9 @@ def hankel_plane(ogrid, rgrid, S_plane, distance, rho, pre_row=None, near_field=
     A = np.asarray(S_plane, dtype=np.complex128) * r[None, :]
     if near_field:
         A = A * np.exp(-1j * k[:, None] * r[None, :] ** 2 / (2.0 * distance))
-    if pre_row is not None:
-        A = A * np.asarray(pre_row)[:, None]
+    if pre_row is not None:  # [No], or [No, Nr] for a radially modulated medium (factor per radius, :505-512)
+        pr = np.asarray(pre_row)
+        A = A * (pr if pr.ndim == 2 else pr[:, None])
     A = A * trapz_weights(r)[None, :]
     out = np.empty((len(w), len(rho)), dtype=np.complex128)
     for i in range(len(w)):
@@ -76,14 +77,17 @@ def hankel_plane(ogrid, rgrid, S_plane, distance, rho, pre_row=None, near_field=
 
 
 def hankel_long(zgrid_full, rgrid, ogrid, S, distance, rho, pressure=1.0, disp=None, absorb=None, near_field=True,
-                cumulative=False):
+                cumulative=False, pre=None):
     """Hankel_long on a static source S[kz, omega, r]; zgrid_full is the grid the source was
     given on (its last plane is dropped as FSources_provider does).
 
     Returns dict(FF_integrated [Nrho, No], entry, exit, planes [Nz, Nrho, No] and, when
-    asked, cumulative [Nz-1, Nrho, No])."""
+    asked, cumulative [Nz-1, Nrho, No]).  ``pre`` overrides the no-modulation pre-factor."""
     z = np.asarray(zgrid_full, dtype=np.float64)[0:-1]
-    pre, renorm = pre_factor_table(z, ogrid, pressure, disp, absorb)
+    if pre is None:
+        pre, renorm = pre_factor_table(z, ogrid, pressure, disp, absorb)
+    else:  # a given table: [Nz, No] or [Nz, No, Nr] (radially modulated medium, no renormalisation)
+        renorm = np.ones((len(z), len(ogrid)))
     planes = np.stack([hankel_plane(ogrid, rgrid, S[k], distance - z[k], rho, pre[k], near_field).T
                        for k in range(len(z))])
     ff = np.zeros_like(planes[0])

@@ -243,6 +243,33 @@ HANKEL_CASES = {
 }
 
 
+def radial_pressure():
+    """A medium modulated in z and r (a jet narrowing downstream): the pressure table of the
+    reference's zr branch."""
+    pz = np.linspace(-6e-3, 6e-3, 13)
+    pr = np.linspace(0.0, 300e-6, 11)
+    val = np.exp(-(pr[None, :] / (150e-6 * (1.0 + 40.0 * (pz[:, None] + 6e-3)))) ** 2) * (1.0 - 0.3 * pz[:, None] / 6e-3)
+    return dict(zgrid=pz, rgrid=pr, value=val)
+
+
+def make_hankel_radial(ref_root):
+    """The reference's zr-branch pre-factor (Hankel_transform.py:302-399) on the
+    hankel_config3_slice grids, for each plane: get_propagation_pre_factor_function(...)[0](kz)."""
+    HT, units = import_reference_hankel(ref_root)
+    No, Nr, Nz, Nrho = HANKEL_CASES["hankel_config3_slice"][:4]
+    zgrid, rgrid, ogrid, rho, S = hankel_inputs(No, Nr, Nz, Nrho)
+    press = radial_pressure()
+    target = HT.FSources_provider(zgrid, rgrid, ogrid, data_source="static", FSource=S)
+    pf, renorm = HT.get_propagation_pre_factor_function(target.zgrid, target.rgrid, target.ogrid, preset_gas="Ar",
+                                                        pressure=press)
+    pre = np.stack([pf(k) for k in range(len(target.zgrid))])  # [Nz, No, Nr] as the reference returns it
+    np.savez_compressed(os.path.join(HERE, "prefactor_radial.npz"), zgrid=target.zgrid, rgrid=target.rgrid,
+                        ogrid=target.ogrid, pressure_zgrid=press["zgrid"], pressure_rgrid=press["rgrid"],
+                        pressure_value=press["value"], pre=pre, renorm_is_none=renorm is None,
+                        n_xuv=np.array([1 - 1e-5, 1e-7]))
+    print("hankel radial pre-factor", pre.shape)
+
+
 def hankel_inputs(No, Nr, Nz, Nrho, seed=0):
     """Seeded synthetic source with config-3 structure at small size: Gaussian radial
     profile (50 um) times a comb of odd harmonics (11..41 of 800 nm, Lorentzian width
@@ -283,7 +310,7 @@ def make_hankel(ref_root):
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["tdse", "hankel", "analysis", "xuv"], default=None)
+    ap.add_argument("--only", choices=["tdse", "hankel", "analysis", "xuv", "radial"], default=None)
     a = ap.parse_args()
     if a.only in (None, "tdse"):
         make_tdse(os.path.join(a.ref, "1DTDSE", "sources"))
@@ -293,3 +320,5 @@ if __name__ == "__main__":
         make_analysis(os.path.join(a.ref, "1DTDSE", "sources"))
     if a.only in (None, "xuv"):
         make_xuv(a.ref)
+    if a.only in (None, "radial"):
+        make_hankel_radial(a.ref)

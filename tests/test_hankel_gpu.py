@@ -91,3 +91,32 @@ def test_hankel_transform_single_plane(gpu_lib):
     got = H.HankelTransform(og, rg, F, 0.9, rho, pre_factor=pre)
     ref = oh.hankel_plane(og, rg, F, 0.9, rho, pre_row=pre[0])
     assert np.abs(got - ref).max() < 1e-11 * np.abs(ref).max()
+
+
+def test_radially_modulated_medium(gpu_lib):
+    """zr-modulated medium (pre-factor per plane, frequency and radius): plain FP64, the fast form
+    and its tensor-core planes against the numpy restatement with the same pre-factor table
+    (integrated far field, entry plane, non-normalised cumulative field)."""
+    import oracle.hankel as oh
+    from mma_gb300 import hankel as H
+
+    g = np.load(os.path.join(GOLDEN, "hankel_config3_slice.npz"))
+    p = np.load(os.path.join(GOLDEN, "prefactor_radial.npz"))
+    H.XUV_index.set_constant_index(complex(g["n_xuv"][0], g["n_xuv"][1]))
+    press = dict(zgrid=p["pressure_zgrid"], rgrid=p["pressure_rgrid"], value=p["pressure_value"])
+    target = H.FSources_provider(g["zgrid"], g["rgrid"], g["ogrid"], data_source="static", FSource=g["S"])
+    ref = oh.hankel_long(g["zgrid"], g["rgrid"], g["ogrid"], g["S"][:-1].astype(np.complex128), float(g["distance"]),
+                         g["rho"], cumulative=True, pre=p["pre"])
+    for form in ("plain", "fast"):
+        h = H.Hankel_long(target, float(g["distance"]), g["rho"], preset_gas="Ar", pressure=press,
+                          store_non_normalised_cumulative_result=True, form=form)
+        if form == "plain":
+            scale = np.abs(ref["FF_integrated"]).max()
+            assert np.abs(h.FF_integrated - ref["FF_integrated"]).max() < 1e-10 * scale
+            assert np.abs(h.cumulative_field_no_norm - ref["cumulative"]).max() < 1e-10 * scale
+        else:
+            assert h.fast_plan["planes_via"] == "tc"
+            assert per_harmonic(h.FF_integrated, ref["FF_integrated"]) < FAST_TOL
+            assert per_harmonic(h.entry_plane_transform, ref["entry"]) < FAST_TOL
+            for k in range(ref["cumulative"].shape[0]):
+                assert per_harmonic(h.cumulative_field_no_norm[k], ref["cumulative"][k]) < FAST_TOL, k

@@ -42,3 +42,32 @@ def test_trapz_weights():
     x = np.sort(np.random.default_rng(0).uniform(0, 1, 17))
     y = np.random.default_rng(1).standard_normal(17)
     assert abs(np.sum(oh.trapz_weights(x) * y) - integrate.trapezoid(y, x=x)) < 1e-14
+
+
+def test_radial_prefactor_matches_reference():
+    """zr-modulated medium: the pre-factor table against the reference's own zr branch
+    (Hankel_transform.py:302-399, fixture made by tests/golden/make_golden.py)."""
+    from mma_gb300 import hankel as H
+
+    g = np.load(os.path.join(GOLDEN, "prefactor_radial.npz"))
+    H.XUV_index.set_constant_index(complex(g["n_xuv"][0], g["n_xuv"][1]))
+    press = dict(zgrid=g["pressure_zgrid"], rgrid=g["pressure_rgrid"], value=g["pressure_value"])
+    pre, renorm = H.pre_factor_table(g["zgrid"], g["ogrid"], "Ar", press, rgrid=g["rgrid"])
+    assert renorm is None and bool(g["renorm_is_none"])
+    assert pre.shape == g["pre"].shape
+    assert np.abs(pre - g["pre"]).max() < 1e-12 * np.abs(g["pre"]).max()
+
+
+def test_radial_profile_constant_in_r_is_the_plain_medium():
+    """r branch: a radially constant profile gives the no-modulation pre-factor at every radius."""
+    from mma_gb300 import hankel as H
+
+    H.XUV_index.set_constant_index(complex(1 - 1e-5, 1e-7))
+    z = np.linspace(-1e-3, 1e-3, 5)
+    w = np.linspace(1e16, 3e16, 4)
+    r = np.linspace(0.0, 1e-4, 6)
+    pre_r, ren = H.pre_factor_table(z, w, "Ar", dict(rgrid=np.array([0.0, 2e-4]), value=np.array([0.8, 0.8])), rgrid=r)
+    pre0, _ = H.pre_factor_table(z, w, "Ar", 0.8)
+    assert ren is None
+    for k in range(len(r)):
+        assert np.allclose(pre_r[:, :, k], pre0, rtol=1e-14, atol=0)
