@@ -279,6 +279,35 @@ def run_hankel(args, device):
     return out
 
 
+def run_profile_case(args, device):
+    """Small cases for kernel captures (one untimed pass each): ``small_wide`` propagates 152
+    instances on grids of 9001-12001 sites (the register-resident complex64 kernel, 40 and 48
+    sites per thread) with 2-cycle pulses; ``small_adjoint`` runs the adjoint gradient of 16
+    config-1-grid instances with 2-cycle pulses."""
+    import torch
+
+    from mma_gb300.tdse_batch import TDSEGrids, run_batch
+
+    if args.workload == "small_wide":
+        sizes = [9000, 10000, 11000, 12000]
+        t, fields = focus_fields(n_r=8, n_z=19, n_cycles=2)
+        grids = TDSEGrids([dict(num_r=n, dx=0.1, trg_a=A_CONFIG) for n in sizes], dt=float(t[1] - t[0]), c64=True)
+        ids = np.arange(fields.shape[0]) % len(sizes)
+        res = run_batch(grids, torch.tensor(fields, device=device), float(t[1] - t[0]), grid_ids=ids,
+                        precision="c64", tmax=float(t[-1] - t[0]))
+        torch.cuda.synchronize()
+        return {"instances": int(fields.shape[0]), "sites_per_thread": sorted(set(int(m) for m in grids.m32)),
+                "finite": bool(torch.isfinite(res["sourceterm"]).all())}
+    from mma_gb300.tdse_adjoint import yield_and_grad
+
+    t, fields = focus_fields(n_r=4, n_z=4, n_cycles=2)
+    dtf = float(t[1] - t[0])
+    grids = TDSEGrids([dict(num_r=8000, dx=0.1, trg_a=A_CONFIG)], dt=dtf, adjoint=True)
+    L, g = yield_and_grad(grids, torch.tensor(fields, device=device), dtf, (11 * OMEGA0, 21 * OMEGA0), ckpt_every=256)
+    torch.cuda.synchronize()
+    return {"instances": int(fields.shape[0]), "finite": bool(torch.isfinite(g).all())}
+
+
 def run_analysis(args, device):
     """Analysis functions of the TDSE library on config-1 sizes: the photoelectron spectrum of
     an 8001-site wavefunction on the reference's default energy grid (10000 energies, window
@@ -576,6 +605,8 @@ WORKLOADS = {
     "config3": (64, 32, 10, 2048),  # the far field alone (run_hankel), reported on its own line
     "analysis": (64, 32, 10, 2048),  # photoelectron spectra and Gabor transforms (run_analysis)
     "small": (8, 19, 2, 128),  # profiling case: same grids, fewer instances, shorter pulses
+    "small_wide": (8, 19, 2, 128),  # profiling case: grids of 9001-12001 sites (run_profile_case)
+    "small_adjoint": (8, 19, 2, 128),  # profiling case: the adjoint on 16 short pulses (run_profile_case)
 }
 
 
@@ -762,13 +793,14 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
-    if args.workload in ("config2", "config3", "config4", "analysis"):
+    if args.workload in ("config2", "config3", "config4", "analysis", "small_wide", "small_adjoint"):
         import torch
 
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
         torch.cuda.set_device(dev)
         fn = {"config2": run_config2, "config3": run_hankel, "config4": run_config4,
-              "analysis": run_analysis}[args.workload]
+              "analysis": run_analysis, "small_wide": run_profile_case,
+              "small_adjoint": run_profile_case}[args.workload]
         print(json.dumps({"workload": args.workload, "result": fn(args, dev)}))
         return
     r64 = run_ours(args, rank, world, "fp64") if args.forms in ("both", "fp64") else None

@@ -34,7 +34,7 @@ def _sig():
     return lib
 
 
-def pes(psi, num_r, dx, trg_a, E_start=-0.6, num_E=10000, epsilon=5e-4, Estep=5e-4, chunk=8192, stream=None):
+def pes(psi, num_r, dx, trg_a, E_start=-0.6, num_E=10000, epsilon=5e-4, Estep=5e-4, chunk=16384, stream=None):
     """Photoelectron spectrum of one wavefunction (complex cuda tensor of num_r + 1 values):
     returns (E grid numpy, PES float64 cuda tensor [num_E]).  Energies run `chunk` at a time."""
     lib = _sig()

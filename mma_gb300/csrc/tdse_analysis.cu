@@ -24,15 +24,23 @@ namespace an {
 
 constexpr double kPi = 3.14159265358979323846;
 
-// x_k = k dx - xmax with xmax = 0.5 num_r dx (tools.c:231, 246) and V(x_k) = -1/sqrt(a^2 + x^2)
-// (tools.c:91-95); V has n + 1 entries (the reference reads x[num_r + 1] for an unused
-// super-diagonal of the last row; here it is defined and equally unused).
-__global__ void pes_potential(int64_t n, int num_r, double dx, double a, double* V)
+// Energy-independent tables of the photoelectron spectrum: x_k = k dx - xmax with
+// xmax = 0.5 num_r dx (tools.c:231, 246), V(x_k) = -1/sqrt(a^2 + x^2) (tools.c:91-95) kept as
+// V/12 (n + 1 entries: the reference reads x[num_r + 1] for an unused super-diagonal of the
+// last row), and the right-hand side of the first solve, M2 psi = (10 psi_j + psi_{j-1} +
+// psi_{j+1})/12 (tridiag.c:261-268), which is the same for every energy.
+__global__ void pes_tables(int64_t n, int num_r, double dx, double a, const double* psi, double* V12, cd* rhs0)
 {
     const double xmax = __dmul_rn(__dmul_rn(0.5, (double)num_r), dx);
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k <= n; k += (int64_t)gridDim.x * blockDim.x) {
         const double x = __dsub_rn(__dmul_rn((double)k, dx), xmax);
-        V[k] = -1.0 / sqrt(a * a + x * x);
+        V12[k] = (-1.0 / sqrt(a * a + x * x)) / 12.;
+        if (k < n) {
+            const cd pc{psi[2 * k], psi[2 * k + 1]};
+            const cd pm = k > 0 ? cd{psi[2 * k - 2], psi[2 * k - 1]} : cd{0.0, 0.0};
+            const cd pn = k + 1 < n ? cd{psi[2 * k + 2], psi[2 * k + 3]} : cd{0.0, 0.0};
+            rhs0[k] = cd{10 * pc.re / 12. + (pn.re + pm.re) / 12., 10 * pc.im / 12. + (pn.im + pm.im) / 12.};
+        }
     }
 }
 
@@ -40,60 +48,68 @@ struct PesArgs {
     int64_t n;        // rows = num_r + 1
     double dx, dE, Estep, E_start;
     int num_E, e0, chunk;
-    const double* V;    // [n + 1]
-    const double* psi;  // [2n] interleaved
+    const double* V12;  // [n + 1]  V / 12
+    const cd* rhs0;     // [n]      M2 psi
     cd* gam;            // [n][chunk]
     cd* u;              // [n][chunk]
     double* pes;        // [num_E]
 };
 
-// one Numerov-tridiagonal solve for the energy of this thread (sg = -1: first window, +1: second)
-// rhs from `src` (the input wavefunction, shared by all energies) or from u itself (the first
-// solve's result, overwritten row by row as the sweep passes it).
+// One Numerov-tridiagonal solve for the energy of this thread (sg = -1: first window, +1:
+// second).  Rows of (M2 (Es -/+ i dE - V) - K): diagonal 10 (Es - V_j)/12 - 1/dx^2 -/+ i 10 dE/12,
+// sub-diagonal of row j (Es - V_{j-1})/12 + 0.5/dx^2 -/+ i dE/12, super-diagonal of row j-1
+// (Es - V_j)/12 + 0.5/dx^2 -/+ i dE/12 (tools.c:257-275).  The right-hand side is M2 psi (first
+// solve) or M2 u1 formed from the first solve's result, which the sweep overwrites row by row
+// after reading it.  The Thomas recurrence is that of tridiag.c:26-70 with one reciprocal of
+// |beta|^2 per row; Es/12 and V/12 are formed once, so the rows need no divisions.
 __device__ __forceinline__ void pes_solve(const PesArgs& A, int e, double E, double sg, bool rhs_from_u,
                                           double* norm_out)
 {
     const int64_t n = A.n, C = A.chunk;
     const double Es = E + sg * A.dE;  // E_start + Estep i -/+ dE
+    const double e12 = Es / 12., e10 = 10 * Es / 12.;
     const double diag = 1. / (A.dx * A.dx), off = -0.5 / (A.dx * A.dx);
     const double im_d = (sg < 0 ? -1.0 : 1.0) * (10 * A.dE / 12), im_o = (sg < 0 ? -1.0 : 1.0) * (A.dE / 12);
-    auto p_at = [&](int64_t j) -> cd {
-        if (rhs_from_u) return A.u[j * C + e];
-        return cd{A.psi[2 * j], A.psi[2 * j + 1]};
-    };
-    // psi_inter (tridiag.c:261-268)
-    cd pm{0.0, 0.0}, pc = p_at(0), pn = (n > 1) ? p_at(1) : cd{0.0, 0.0};
+    constexpr double k12 = 1.0 / 12.;
+    cd pm{0.0, 0.0}, pc{0.0, 0.0}, pn{0.0, 0.0};
+    if (rhs_from_u) {
+        pc = A.u[e];
+        pn = (n > 1) ? A.u[C + e] : cd{0.0, 0.0};
+    }
     auto rhs = [&](int64_t j) -> cd {
-        if (j == 0) return cd{10 * pc.re / 12. + pn.re / 12., 10 * pc.im / 12. + pn.im / 12.};
-        if (j == n - 1) return cd{10 * pc.re / 12. + pm.re / 12., 10 * pc.im / 12. + pm.im / 12.};
-        return cd{10 * pc.re / 12. + (pn.re + pm.re) / 12., 10 * pc.im / 12. + (pn.im + pm.im) / 12.};
+        if (!rhs_from_u) return A.rhs0[j];
+        return cd{(10 * pc.re + (pn.re + pm.re)) * k12, (10 * pc.im + (pn.im + pm.im)) * k12};
     };
     // row 0
     cd r = rhs(0);
-    double b_re = 10 * (Es - A.V[0]) / 12. - diag, b_im = -0.0 + im_d;
-    double bet_re = b_re, bet_im = b_im, bet_norm = bet_re * bet_re + bet_im * bet_im;
-    cd uprev{(r.re * b_re + r.im * b_im) / bet_norm, (r.im * b_re - r.re * b_im) / bet_norm};
-    A.u[0 * C + e] = uprev;
+    double v12 = A.V12[0];
+    double b_re = (e10 - 10 * v12) - diag, b_im = im_d;
+    double bet_re = b_re, bet_im = b_im;
+    double inv = 1.0 / (bet_re * bet_re + bet_im * bet_im);
+    cd uprev{(r.re * b_re + r.im * b_im) * inv, (r.im * b_re - r.re * b_im) * inv};
+    A.u[e] = uprev;
     for (int64_t j = 1; j < n; j++) {
-        pm = pc;
-        pc = pn;
-        pn = (j + 1 < n) ? p_at(j + 1) : cd{0.0, 0.0};
+        if (rhs_from_u) {
+            pm = pc;
+            pc = pn;
+            pn = (j + 1 < n) ? A.u[(j + 1) * C + e] : cd{0.0, 0.0};
+        }
         r = rhs(j);
-        // sub-diagonal of row j = dinf[j-1], super-diagonal of row j-1 = dsup[j-1]
-        const double a_re = (Es - A.V[j - 1]) / 12. - off, a_im = -0.0 + im_o;
-        const double c_re = (Es - A.V[j]) / 12. - off, c_im = -0.0 + im_o;
-        const double g_re = (c_re * bet_re + c_im * bet_im) / bet_norm;
-        const double g_im = (c_im * bet_re - c_re * bet_im) / bet_norm;
+        const double v12j = A.V12[j];
+        const double a_re = (e12 - v12) - off, a_im = im_o;   // dinf[j-1]
+        const double c_re = (e12 - v12j) - off, c_im = im_o;  // dsup[j-1]
+        const double g_re = (c_re * bet_re + c_im * bet_im) * inv;
+        const double g_im = (c_im * bet_re - c_re * bet_im) * inv;
         A.gam[j * C + e] = cd{g_re, g_im};
-        b_re = 10 * (Es - A.V[j]) / 12. - diag;
-        b_im = -0.0 + im_d;
+        b_re = (e10 - 10 * v12j) - diag;
         bet_re = b_re - (a_re * g_re - a_im * g_im);
         bet_im = b_im - (a_im * g_re + a_re * g_im);
-        bet_norm = bet_re * bet_re + bet_im * bet_im;
+        inv = 1.0 / (bet_re * bet_re + bet_im * bet_im);
         const double t_re = r.re - a_re * uprev.re + a_im * uprev.im;
         const double t_im = r.im - a_re * uprev.im - a_im * uprev.re;
-        uprev = cd{(t_re * bet_re + t_im * bet_im) / bet_norm, (-t_re * bet_im + t_im * bet_re) / bet_norm};
-        A.u[j * C + e] = uprev;  // the rhs of row j+1 already holds p_j (pc) and p_{j+1} (pn)
+        uprev = cd{(t_re * bet_re + t_im * bet_im) * inv, (-t_re * bet_im + t_im * bet_re) * inv};
+        A.u[j * C + e] = uprev;  // the rhs of row j+1 already holds u1_j (pc) and u1_{j+1} (pn)
+        v12 = v12j;
     }
     // back substitution (tridiag.c:62-66)
     cd unext = uprev;
@@ -110,7 +126,7 @@ __device__ __forceinline__ void pes_solve(const PesArgs& A, int e, double E, dou
     *norm_out = nrm;
 }
 
-__global__ void __launch_bounds__(128) pes_kernel(PesArgs A)
+__global__ void __launch_bounds__(64) pes_kernel(PesArgs A)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int ie = A.e0 + e;
@@ -122,16 +138,26 @@ __global__ void __launch_bounds__(128) pes_kernel(PesArgs A)
     A.pes[ie] = nrm * A.dx * pow(A.dE, 4.);
 }
 
-// Gabor windows: in[(s N_G + w) N + j] = exp(-(ia (j dt - (t_min + w dt_G)))^2) signal_s[j]
-// (tools_fftw3.c:180-196, ia = 1/a)
-__global__ void gabor_window(const double* sig, int64_t stride, int n_sig, int N, int N_G, double dt, double t_min,
-                             double dt_G, double ia, double* in)
+// Gabor windows exp(-(ia (j dt - (t_min + w dt_G)))^2) (tools_fftw3.c:180-196, ia = 1/a), the
+// same for every signal: tabulated once per call, [N_G][N]
+__global__ void gabor_table(int N, int N_G, double dt, double t_min, double dt_G, double ia, double* win)
+{
+    const int64_t total = (int64_t)N_G * N;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = q % N, w = q / N;
+        const double arg = ia * (((double)j) * dt - (t_min + ((double)w) * dt_G));
+        win[q] = exp(-(arg * arg));  // arg * arg: the correctly rounded square, as pow(arg, 2.)
+    }
+}
+
+// windowed signals in[(s N_G + w) N + j] = win[w][j] signal_s[j]
+__global__ void gabor_window(const double* sig, int64_t stride, int n_sig, int N, int N_G, const double* win,
+                             double* in)
 {
     const int64_t total = (int64_t)n_sig * N_G * N;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = q % N, b = q / N, w = b % N_G, s = b / N_G;
-        const double arg = ia * (((double)j) * dt - (t_min + ((double)w) * dt_G));
-        in[q] = exp(-pow(arg, 2.)) * sig[s * stride + j];
+        in[q] = win[w * N + j] * sig[s * stride + j];
     }
 }
 
@@ -156,11 +182,16 @@ using namespace mma;
 // cuFFT plans are cached by tdse_fft.cu (shape and batch)
 int mma_fft_get_plan_d2z(int n, long long idist, long long odist, int batch, cufftHandle* out);
 
+namespace {
+// scratch: V/12 [n + 1] | M2 psi [n] | gam [n][chunk] | u [n][chunk]
+size_t pes_fixed(size_t n) { return (sizeof(double) * (n + 1) + 255) / 256 * 256 + (sizeof(cd) * n + 255) / 256 * 256; }
+}  // namespace
+
 extern "C" size_t mma_tdse_pes_scratch_bytes(int num_r, int chunk)
 {
     if (num_r < 1 || chunk < 1) return 0;
     const size_t n = (size_t)num_r + 1;
-    return sizeof(double) * (n + 1) + 2 * sizeof(cd) * n * (size_t)chunk + 256;
+    return pes_fixed(n) + 2 * sizeof(cd) * n * (size_t)chunk;
 }
 
 extern "C" int mma_tdse_pes(const double* psi, int num_r, double dx, double trg_a, int num_E, double dE, double Estep,
@@ -168,20 +199,21 @@ extern "C" int mma_tdse_pes(const double* psi, int num_r, double dx, double trg_
 {
     if (!psi || !pes || !scratch || num_r < 1 || num_E < 1 || !(dx > 0.0)) return MMA_ERR_ARG;
     const int64_t n = (int64_t)num_r + 1;
-    const size_t fixed = sizeof(double) * (size_t)(n + 1) + 256;
+    const size_t fixed = pes_fixed((size_t)n);
     if (scratch_bytes < fixed + 2 * sizeof(cd) * (size_t)n) return MMA_ERR_ARG;
     int64_t chunk = (int64_t)((scratch_bytes - fixed) / (2 * sizeof(cd) * (size_t)n));
     if (chunk > num_E) chunk = num_E;
     cudaStream_t st = (cudaStream_t)stream;
     char* sc = static_cast<char*>(scratch);
-    double* V = reinterpret_cast<double*>(sc);
-    cd* gam = reinterpret_cast<cd*>(sc + (sizeof(double) * (size_t)(n + 1) + 255) / 256 * 256);  // after V
+    double* V12 = reinterpret_cast<double*>(sc);
+    cd* rhs0 = reinterpret_cast<cd*>(sc + (sizeof(double) * (size_t)(n + 1) + 255) / 256 * 256);
+    cd* gam = reinterpret_cast<cd*>(sc + fixed);
     cd* u = gam + (size_t)n * chunk;
-    an::pes_potential<<<an::grid_for(n + 1), 256, 0, st>>>(n, num_r, dx, trg_a, V);
+    an::pes_tables<<<an::grid_for(n + 1), 256, 0, st>>>(n, num_r, dx, trg_a, psi, V12, rhs0);
     for (int e0 = 0; e0 < num_E; e0 += (int)chunk) {
-        an::PesArgs A{n, dx, dE, Estep, E_start, num_E, e0, (int)chunk, V, psi, gam, u, pes};
+        an::PesArgs A{n, dx, dE, Estep, E_start, num_E, e0, (int)chunk, V12, rhs0, gam, u, pes};
         const int cnt = (int)((num_E - e0 < chunk) ? num_E - e0 : chunk);
-        an::pes_kernel<<<(cnt + 127) / 128, 128, 0, st>>>(A);
+        an::pes_kernel<<<(cnt + 63) / 64, 64, 0, st>>>(A);  // small blocks: few energies still reach every SM
     }
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }
@@ -207,7 +239,10 @@ extern "C" int mma_gabor(const double* signals, int64_t stride, int n_sig, doubl
     double* in = static_cast<double*>(scratch);
     double2* out = reinterpret_cast<double2*>(static_cast<char*>(scratch) + (sizeof(double) * nb * N + 255) / 256 * 256);
     const double ia = 1.0 / a, dt_G = (t_max - t_min) / N_G;
-    an::gabor_window<<<an::grid_for(nb * N), 256, 0, st>>>(signals, stride, n_sig, N, N_G, dt, t_min, dt_G, ia, in);
+    // the window table sits at the front of the DFT output buffer: it is read before the DFT writes there
+    double* win = reinterpret_cast<double*>(out);
+    an::gabor_table<<<an::grid_for((int64_t)N_G * N), 256, 0, st>>>(N, N_G, dt, t_min, dt_G, ia, win);
+    an::gabor_window<<<an::grid_for(nb * N), 256, 0, st>>>(signals, stride, n_sig, N, N_G, win, in);
     cufftHandle p;
     int rc = mma_fft_get_plan_d2z(N, N, Nc, (int)nb, &p);
     if (rc != MMA_OK) return rc;

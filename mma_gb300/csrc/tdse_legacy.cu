@@ -415,7 +415,7 @@ extern "C" double* window_analysis(inputs_def inputs, double* psi, int num_E, do
     }
     if (!have_device()) return nullptr;
     const size_t n = (size_t)inputs.num_r + 1;
-    int chunk = num_E < 8192 ? num_E : 8192;
+    int chunk = num_E < 16384 ? num_E : 16384;
     const size_t sb = mma_tdse_pes_scratch_bytes(inputs.num_r, chunk);
     double *d_psi = nullptr, *d_pes = nullptr;
     void* d_sc = nullptr;
