@@ -246,7 +246,13 @@ class FSources_provider:
                 S = S.to(torch.complex128)
             self.source = S.to(device).contiguous()
         elif data_source == "dynamic":
-            raise NotImplementedError("HDF5 ('dynamic') sources need h5py, which this build does not use")
+            # h5_handle[h5_path] = FSourceTerm [kz, kr, omega, re/im] (Hankel_transform.py:71-77),
+            # read once through mma_gb300.h5io (or any handle whose dataset gives numpy arrays)
+            from .archive import read_fsource
+
+            S = read_fsource(h5_handle[h5_path], len(self.zgrid), kz_step=kz_step, kr_max=kr_max, kr_step=kr_step,
+                             ko_min=ko_min, ko_max=ko_max, ko_step=ko_step)
+            self.source = torch.from_numpy(S).to(device).contiguous()
         else:
             raise ValueError("Wrongly specified input of the class.")
 

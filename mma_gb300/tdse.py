@@ -176,7 +176,7 @@ def run_single(dll, t, E, num_r=8000, dx=0.1, trg_a=np.sqrt(1.68), dt=0.25, Egue
             Nt=out.Nt, Nomega=out.Nomega, dt=inp.Efield.dt, num_t=inp.num_t, Ntinterp=inp.Ntinterp,
         )
         if writewft:
-            res["snapshots"] = out.get_wavefunction(inp)
+            res["snapshots"] = out.get_wavefunction(inp, grids=False)
             steps = int(np.floor(tprint / (res["tgrid"][1] - res["tgrid"][0])))
             n_snap = int(out.Nt // steps)
             if n_snap and out.psi:

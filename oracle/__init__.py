@@ -25,6 +25,14 @@ def build(ref=None):
         subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref", "REF_SRC=" + src], check=True)
 
 
+def ref_file(*parts):
+    """Path of a file of the reference checkout (the parent of the 1DTDSE/sources directory
+    named by MMA_REF_SRC), or None where the checkout is absent."""
+    src = os.environ.get("MMA_REF_SRC", "/root/reference/1DTDSE/sources")
+    p = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(src))), *parts)
+    return p if os.path.exists(p) else None
+
+
 def oracle_lib_path():
     return os.path.join(ORACLE_DIR, "_build", "libmma_oracle.so")
 

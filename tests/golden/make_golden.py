@@ -17,6 +17,11 @@ Refractive-index fixture: the reference's shared_python/make_table.py and
 XUV_refractive_index.py run unchanged on synthetic tables (xuv_tables/, written here) with an
 in-memory stand-in for h5py.
 
+Stored-result fixture: the reference's own regression archive 1DTDSE/ionization.h5 (written by
+its save_to_hdf5, read by 1DTDSE/tests.py:50-88), read with mma_gb300.h5io and kept as
+ionization_h5.npz: every dataset as stored (float32 / int32), the wavefunction snapshots
+subsampled to every 7th.
+
 Run from the repository root where the reference checkout exists:
     python tests/golden/make_golden.py [--ref /root/reference]
 """
@@ -307,10 +312,31 @@ def make_hankel(ref_root):
         print(name, res.FF_integrated.shape)
 
 
+IONIZATION_SNAPSHOTS = slice(0, None, 7)
+
+
+def make_ionization(ref_root):
+    """Every dataset of 1DTDSE/ionization.h5 (TDSE_inputs/*, TDSE_outputs/*) as stored; keys are
+    the archive paths with '/' replaced by '__'."""
+    from mma_gb300 import h5io
+
+    f = h5io.File(os.path.join(ref_root, "1DTDSE", "ionization.h5"))
+    out = {}
+    for grp in ("TDSE_inputs", "TDSE_outputs"):
+        for k in f[grp].keys():
+            v = f[grp + "/" + k][()]
+            if k in ("psi_re", "psi_im"):
+                out["snapshot_index"] = np.arange(v.shape[0])[IONIZATION_SNAPSHOTS]
+                v = v[IONIZATION_SNAPSHOTS]
+            out[grp + "__" + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, "ionization_h5.npz"), **out)
+    print("ionization_h5", len(out), "arrays")
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["tdse", "hankel", "analysis", "xuv", "radial"], default=None)
+    ap.add_argument("--only", choices=["tdse", "hankel", "analysis", "xuv", "radial", "ionization"], default=None)
     a = ap.parse_args()
     if a.only in (None, "tdse"):
         make_tdse(os.path.join(a.ref, "1DTDSE", "sources"))
@@ -322,3 +348,5 @@ if __name__ == "__main__":
         make_xuv(a.ref)
     if a.only in (None, "radial"):
         make_hankel_radial(a.ref)
+    if a.only in (None, "ionization"):
+        make_ionization(a.ref)
