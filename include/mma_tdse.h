@@ -242,9 +242,9 @@ int mma_tdse_build_grids(const mma_tdse_grid *grids_dev, const mma_tdse_grid *gr
                          void *stream);
 
 /* Build the complex64-form tables of n_grids grids from their FP64 data (after
- * mma_tdse_build_grids): 1/beta of the FP64 factorisation, the off-diagonal factor
- * w_j = dt/2 (-1/(2dx^2) + V_j/12), -V' and the (real) ground state, rounded once to
- * FP32 and laid out for m32 sites per thread.  Needs m32 <= 32 (n <= 8192). */
+ * mma_tdse_build_grids): 1/(2 beta) of the FP64 factorisation (half of 1/beta, an exact
+ * scaling), V_j and the (real) ground state, rounded once to FP32 and laid out for
+ * c64_threads threads x m32 sites per thread (m32 <= 48). */
 int mma_tdse_build_c64_tables(const mma_tdse_grid *grids_dev, const mma_tdse_grid *grids_host, int n_grids,
                               void *stream);
 

@@ -8,10 +8,14 @@
 //     storing the chunk products of the partitioned solve, each sweep is run twice: once
 //     from zero to get the chunk-boundary carry for the CTA scan, once from the exact carry
 //     (five passes per step, registers 4M floats);
-//   * the per-site tables in shared memory, 16 bytes per site: 1/beta (complex), V_j and the
+//   * the per-site tables in shared memory, 16 bytes per site: 1/(2 beta) (complex), V_j and the
 //     (real) ground state.  h_j = 6 a_j/beta_j and g_j = 6 c_j/beta_j are re-derived from
-//     1/beta and w_q = dt/2 (-1/(2dx^2) + V_q/12) (a_j = 1/12 + i w_{j-1}, c_j = 1/12 + i w_{j+1}),
-//     and -V'_j = -x_j V_j^3 -- nothing per step goes to L2 but the four observables;
+//     1/(2 beta) and w_q = dt/2 (-1/(2dx^2) + V_q/12) (a_j = 1/12 + i w_{j-1}, c_j = 1/12 + i w_{j+1}),
+//     and -V'_j = -x_j V_j^3 -- nothing per step goes to L2 but the four observables.  Storing
+//     half of 1/beta (a power of two, so no rounding changes) halves y and u throughout the
+//     solve and saves the multiplications by 1/2 in h and g; the update takes 2u - psi;
+//   * the field sample of the next step is copied global -> shared (cp.async) one step ahead,
+//     so no warp waits on a global load before the step's first barrier;
 //   * the phase e^{+i E dt x}: the chunk-start angle is formed and reduced mod 2 pi in
 //     float-float arithmetic, then e^{i E dt dx i} per site from a 32-entry table;
 //   * the observables summed per thread with Kahan compensation, across the warp with
@@ -102,6 +106,14 @@ __device__ __forceinline__ cf scan_bwd(cf c, cf b, cf* sc, cf* sb)
     return lane == 31 ? uw : cfma(cp, uw, bp);
 }
 
+// 8-byte global -> shared copy that holds no register while in flight; completed by cp_async_wait
+__device__ __forceinline__ void cp_async8(double* dst_smem, const double* src)
+{
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // error-free sum (Knuth two-sum)
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 {
@@ -144,6 +156,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
     __shared__ cf bfirst[kWarps], blast[kWarps];
     __shared__ cf wtab[M];          // e^{i F_k dt dx i}, i < M: phase of site i relative to site 0
     __shared__ float s_ahi, s_alo;  // F_k dt as a float-float pair (phase angle of pass 5)
+    __shared__ double s_fbuf[3];    // field samples k-1, k, k+1 (slot k mod 3), k+1 copied ahead
     __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     constexpr int L = kThreads * M;
@@ -189,6 +202,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             }
             s_lo = lo < 0 ? 0 : lo;
             s_hi = hi > num_r ? num_r : hi;
+            s_fbuf[0] = I.n_field > 0 ? P.fields[I.field_off] : 0.0;
         }
         // ---- state: psi in registers, initialised from the ground state
         cf psi[M], yy[M];
@@ -231,12 +245,14 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
         }
         double tt = I.tmin;
         // h_j and g_j of site (i, t): 6 a_j /beta_j and 6 c_j /beta_j from the neighbour's V,
-        // (1/2 + i 6 w) * ib with 6 w = c_hi + (c_lo + c1 V) kept unsummed.  No boundary tests:
-        // rows beyond n-1 have zero tables (y = u = 0 there), the first row's h multiplies an
-        // incoming carry of 0 and the last row's g multiplies u_n = 0.
+        // (1 + i 12 w) * ib2 with ib2 = 1/(2 beta) (the table) and 12 w = c_hi2 + (c_lo2 + c12 V)
+        // kept unsummed -- bit for bit (1/2 + i 6 w) / beta, every factor being scaled by 2.  No
+        // boundary tests: rows beyond n-1 have zero tables (y = u = 0 there), the first row's h
+        // multiplies an incoming carry of 0 and the last row's g multiplies u_n = 0.
+        const float c_hi2 = 2.f * c_hi, c_lo2 = 2.f * c_lo, c12 = 2.f * c1;
         auto off_diag = [&](float v, float ir, float ii) -> cf {
-            const float t1 = fmaf(c1, v, c_lo);
-            return cf{fmaf(-t1, ii, fmaf(-c_hi, ii, 0.5f * ir)), fmaf(t1, ir, fmaf(c_hi, ir, 0.5f * ii))};
+            const float t1 = fmaf(c12, v, c_lo2);
+            return cf{fmaf(-t1, ii, fmaf(-c_hi2, ii, ir)), fmaf(t1, ir, fmaf(c_hi2, ir, ii))};
         };
         const float v_left = (t == 0) ? 0.f : tab4[(M - 1) * kThreads + t - 1].z;   // V left of site 0
         const float v_right = (t == kThreads - 1) ? 0.f : tab4[t + 1].z;            // V right of site M-1
@@ -261,11 +277,16 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
                 }
                 const double v = (double)hs + (double)ls;  // FP64 finish
                 const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
-                if (lane == 0) o_src[k] = -v + o_e[k];
+                if (lane == 0) {  // o_e[k] = F_{k-1}, still in its shared slot
+                    const int64_t kp = k - 1;
+                    o_src[k] = -v + ((kp <= gate || kp >= I.n_field) ? 0.0 : s_fbuf[kp % 3]);
+                }
                 if (lane == 8) o_x[k] = v;
                 if (lane == 16) o_ptot[k] = fma(pr, pr, pim * pim);
             }
-            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : f[k];
+            const int fs = (int)(k % 3);
+            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : s_fbuf[fs];
+            if (w == 1 && lane == 0 && k + 1 < I.n_field) cp_async8(&s_fbuf[fs == 2 ? 0 : fs + 1], f + k + 1);
             if (w == 1 && lane == 0) {
                 tt += dt;
                 o_t[k + 1] = tt;
@@ -359,7 +380,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
 #pragma unroll
             for (int i = 0; i < M; i++) {
                 const float4 tb = tab4[i * kThreads + t];
-                const cf d = yy[i] - psi[i];
+                const cf d{fmaf(2.f, yy[i].re, -psi[i].re), fmaf(2.f, yy[i].im, -psi[i].im)};  // u = 2 yy
                 const cf pn = cmul(cmul(phs, wtab[i]), d);
                 psi[i] = pn;
                 const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
@@ -426,6 +447,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
                         }
                 }
             }
+            if (w == 1 && lane == 0) cp_async_wait();  // the next step's field sample has landed
             __syncthreads();
             if (w == 2 && lane == 0) {
                 float pi_sum = 0.f;
@@ -447,7 +469,10 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             }
             const double v = (double)hs + (double)ls;
             const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
-            if (lane == 0) o_src[S] = -v + o_e[S];
+            if (lane == 0) {
+                const int64_t kp = S - 1;
+                o_src[S] = -v + ((kp <= gate || kp >= I.n_field) ? 0.0 : s_fbuf[kp % 3]);
+            }
             if (lane == 8) o_x[S] = v;
             if (lane == 16) o_ptot[S] = fma(pr, pr, pim * pim);
         }
@@ -487,6 +512,7 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
     __shared__ float red_hi[NW * 4], red_lo[NW * 4], red_pi[NW];
     __shared__ cf wtab[M];
     __shared__ float s_ahi, s_alo;
+    __shared__ double s_fbuf[3];  // field samples k-1, k, k+1 (slot k mod 3), k+1 copied ahead
     __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     constexpr int L = T * M;
@@ -530,6 +556,7 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
             }
             s_lo = lo < 0 ? 0 : lo;
             s_hi = hi > num_r ? num_r : hi;
+            s_fbuf[0] = I.n_field > 0 ? P.fields[I.field_off] : 0.0;
         }
         const int64_t s0 = (int64_t)t * M;
 #pragma unroll
@@ -563,9 +590,10 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
             }
         }
         double tt = I.tmin;
+        const float c_hi2 = 2.f * c_hi, c_lo2 = 2.f * c_lo, c12 = 2.f * c1;  // as in propagate_c64_kernel
         auto off_diag = [&](float v, float ir, float ii) -> cf {
-            const float t1 = fmaf(c1, v, c_lo);
-            return cf{fmaf(-t1, ii, fmaf(-c_hi, ii, 0.5f * ir)), fmaf(t1, ir, fmaf(c_hi, ir, 0.5f * ii))};
+            const float t1 = fmaf(c12, v, c_lo2);
+            return cf{fmaf(-t1, ii, fmaf(-c_hi2, ii, ir)), fmaf(t1, ir, fmaf(c_hi2, ir, ii))};
         };
         cf yl[M], fg[M];
 
@@ -590,7 +618,10 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
                 }
                 const double v = (double)hs + (double)ls;
                 const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
-                if (lane == 0) o_src[k] = -v + o_e[k];
+                if (lane == 0) {  // o_e[k] = F_{k-1}, still in its shared slot
+                    const int64_t kp = k - 1;
+                    o_src[k] = -v + ((kp <= gate || kp >= I.n_field) ? 0.0 : s_fbuf[kp % 3]);
+                }
                 if (lane == 8) o_x[k] = v;
                 if (lane == 16) o_ptot[k] = fma(pr, pr, pim * pim);
                 if (lane == 24) {
@@ -599,7 +630,9 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
                     o_pint[k] = (double)pi_sum;
                 }
             }
-            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : f[k];
+            const int fs = (int)(k % 3);
+            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : s_fbuf[fs];
+            if (w == 1 && lane == 0 && k + 1 < I.n_field) cp_async8(&s_fbuf[fs == 2 ? 0 : fs + 1], f + k + 1);
             if (w == 1 && lane == 0) {
                 tt += dt;
                 o_t[k + 1] = tt;
@@ -674,8 +707,9 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
 #pragma unroll
             for (int i = 0; i < M; i++) {
                 const int q = i * T + t;
-                const cf u = cfma(fg[i], uin, yl[i]);
-                const cf d = u - psi[q];
+                const cf u = cfma(fg[i], uin, yl[i]);  // u / 2
+                const cf p0 = psi[q];
+                const cf d{fmaf(2.f, u.re, -p0.re), fmaf(2.f, u.im, -p0.im)};
                 const cf pn = cmul(cmul(phs, wtab[i]), d);
                 psi[q] = pn;
                 const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
@@ -736,6 +770,7 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
                         }
                 }
             }
+            if (w == 1 && lane == 0) cp_async_wait();  // the next step's field sample has landed
             __syncthreads();
         }
         if (w == 0) {  // observables of the last step
@@ -758,7 +793,10 @@ __global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
             }
             const double v = (double)hs + (double)ls;
             const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
-            if (lane == 0) o_src[S] = -v + o_e[S];
+            if (lane == 0) {
+                const int64_t kp = S - 1;
+                o_src[S] = -v + ((kp <= gate || kp >= I.n_field) ? 0.0 : s_fbuf[kp % 3]);
+            }
             if (lane == 8) o_x[S] = v;
             if (lane == 16) o_ptot[S] = fma(pr, pr, pim * pim);
             if (lane == 24) {
@@ -793,8 +831,8 @@ __global__ void __launch_bounds__(kThreads) build_c64_kernel(const mma_tdse_grid
             const int64_t q64 = (j % m) * kThreads + j / m;  // FP64 table layout
             const cd ib6 = ctab[0 * Lm + q64];
             const double vj = -1.0 / sqrt(G.trg_a * G.trg_a + G.x[j] * G.x[j]);
-            v[T_IBRE] = (float)ib6.re;
-            v[T_IBIM] = (float)ib6.im;
+            v[T_IBRE] = (float)(0.5 * ib6.re);  // half of 1/beta: exact scaling of the rounded value
+            v[T_IBIM] = (float)(0.5 * ib6.im);
             v[T_V] = (float)vj;
             v[T_PSI0] = (float)G.psi0[2 * j];
         }
