@@ -15,8 +15,10 @@ reading
     floating-point, fixed-length string and compound of those; layouts compact, contiguous and
     chunked (B-tree v1 chunk index) with the deflate and shuffle filters; attributes.
 writing (mode "w", or "a" which first reads an existing file's tree; written on close)
-    superblock 0, groups as symbol tables, contiguous datasets of fixed-point, floating-point and
-    fixed-length string types, scalar and simple dataspaces, attributes of the same types.
+    superblock 0, groups as symbol tables, datasets of fixed-point, floating-point and
+    fixed-length string types -- contiguous, or chunked (B-tree v1 chunk index) with optional
+    deflate and shuffle filters (h5py's ``chunks=``, ``compression="gzip"``, ``shuffle=``) --
+    scalar and simple dataspaces, attributes of the same types.
 
 Dense (fractal-heap) groups, variable-length types and the version 4 layouts raise
 ``NotImplementedError`` when they are reached.  The writer lays its files out with the
@@ -585,9 +587,10 @@ def _attribute_message(name, value) -> bytes:
 
 
 class _WDataset:
-    def __init__(self, data):
+    def __init__(self, data, chunks=None, gzip=None, shuffle=False):
         self.attrs = Attributes()
         self.data = np.array(data, order="C")  # keeps 0-d (scalar) datasets 0-d
+        self.chunks, self.gzip, self.shuffle = chunks, gzip, shuffle
 
     @property
     def shape(self):
@@ -639,7 +642,14 @@ class _WGroup:
             raise TypeError("%s is a dataset" % path)
         return g
 
-    def create_dataset(self, path, shape=None, dtype=None, data=None):
+    def create_dataset(self, path, shape=None, dtype=None, data=None, chunks=None, compression=None,
+                       compression_opts=None, shuffle=False):
+        """h5py's create_dataset: ``chunks`` (a tuple, or True for the whole array as one chunk),
+        ``compression="gzip"`` with level ``compression_opts`` (default 4), ``shuffle``."""
+        if compression not in (None, "gzip"):
+            raise NotImplementedError("compression %r" % (compression,))
+        if (compression or shuffle) and chunks is None:
+            chunks = True
         parent, leaf = self._walk(path, True)
         if leaf in parent.children:
             raise ValueError("%s exists" % path)
@@ -651,7 +661,14 @@ class _WGroup:
                 a = a.astype(np.dtype(dtype))
             if shape is not None and tuple(shape) != a.shape:
                 a = a.reshape(shape)
-        ds = parent.children[leaf] = _WDataset(a)
+        if chunks is True:
+            chunks = tuple(max(1, s) for s in a.shape)
+        if chunks is not None:
+            chunks = tuple(int(c) for c in chunks)
+            if a.ndim == 0 or len(chunks) != a.ndim or min(chunks) < 1:
+                raise ValueError("chunks %s do not fit a dataset of shape %s" % (chunks, a.shape))
+        level = (4 if compression_opts is None else int(compression_opts)) if compression else None
+        ds = parent.children[leaf] = _WDataset(a, chunks, level, bool(shuffle))
         return ds
 
     def __getitem__(self, path):
@@ -734,11 +751,70 @@ class _Writer(_WGroup):
 
     def _emit_dataset(self, out, ds: _WDataset) -> int:
         a = ds.data
-        addr = self._alloc(out, a.tobytes()) if a.nbytes else _UNDEF
-        msgs = [_message(0x0001, _dataspace_message(a.shape)), _message(0x0003, _dtype_message(a.dtype), 1),
-                _message(0x0008, bytes([3, 1]) + struct.pack("<QQ", addr, a.nbytes))]
+        msgs = [_message(0x0001, _dataspace_message(a.shape)), _message(0x0003, _dtype_message(a.dtype), 1)]
+        if ds.chunks is None:
+            addr = self._alloc(out, a.tobytes()) if a.nbytes else _UNDEF
+            msgs.append(_message(0x0008, bytes([3, 1]) + struct.pack("<QQ", addr, a.nbytes)))
+        else:
+            filters = []
+            if ds.shuffle:
+                filters.append((2, [a.dtype.itemsize]))
+            if ds.gzip is not None:
+                filters.append((1, [ds.gzip]))
+            if filters:  # filter pipeline message, version 1
+                body = bytes([1, len(filters)]) + bytes(6)
+                for fid, vals in filters:
+                    body += struct.pack("<HHHH", fid, 0, 0, len(vals)) + b"".join(struct.pack("<I", v) for v in vals)
+                    if len(vals) % 2:
+                        body += bytes(4)
+                msgs.append(_message(0x000B, body))
+            bt = self._emit_chunks(out, a, ds.chunks, filters)
+            lay = bytes([3, 2, a.ndim + 1]) + struct.pack("<Q", bt)
+            lay += b"".join(struct.pack("<I", c) for c in ds.chunks) + struct.pack("<I", a.dtype.itemsize)
+            msgs.append(_message(0x0008, lay))
         msgs += [_message(0x000C, _attribute_message(k, v)) for k, v in ds.attrs.items()]
         return self._emit_header(out, msgs)
+
+    _CHUNK_K = 32  # libhdf5's default "indexed storage internal node K": 2K entries per node
+
+    def _emit_chunks(self, out, a, chunks, filters) -> int:
+        """Write every chunk (edge chunks zero-filled to full size, filtered) and a B-tree v1 chunk
+        index over them (node type 1, keys: stored size, filter mask, element offsets)."""
+        rank = a.ndim
+        grid = [-(-s // c) for s, c in zip(a.shape, chunks)]
+        entries = []  # (key bytes, child address)
+        for idx in np.ndindex(*grid):
+            offs = [i * c for i, c in zip(idx, chunks)]
+            blk = np.zeros(chunks, dtype=a.dtype)
+            src = a[tuple(slice(o, min(o + c, s)) for o, c, s in zip(offs, chunks, a.shape))]
+            blk[tuple(slice(0, n) for n in src.shape)] = src
+            raw = blk.tobytes()
+            for fid, vals in filters:
+                if fid == 2:  # shuffle: byte k of every element together
+                    es = vals[0]
+                    raw = np.frombuffer(raw, dtype=np.uint8).reshape(-1, es).T.tobytes()
+                elif fid == 1:
+                    raw = zlib.compress(raw, vals[0])
+            addr = self._alloc(out, raw)
+            entries.append((struct.pack("<II", len(raw), 0) + b"".join(struct.pack("<Q", o) for o in offs + [0]), addr))
+        end_key = struct.pack("<II", 0, 0) + b"".join(struct.pack("<Q", g * c) for g, c in zip(grid, chunks)) + bytes(8)
+        ksize = 8 + 8 * (rank + 1)
+        cap = 2 * self._CHUNK_K
+        level = 0
+        while True:
+            nodes = []
+            for i in range(0, len(entries), cap):
+                part = entries[i:i + cap]
+                last = entries[i + cap][0] if i + cap < len(entries) else end_key
+                blob = b"TREE" + bytes([1, level]) + struct.pack("<HQQ", len(part), _UNDEF, _UNDEF)
+                for key, child in part:
+                    blob += key + struct.pack("<Q", child)
+                blob += last
+                blob += bytes(24 + cap * 8 + (cap + 1) * ksize - len(blob))
+                nodes.append((part[0][0], self._alloc(out, blob)))
+            if len(nodes) == 1:
+                return nodes[0][1]
+            entries, level = nodes, level + 1
 
     def _emit_group(self, out, g: _WGroup):
         names = sorted(g.children.keys(), key=lambda s: s.encode())  # symbol nodes are searched by name

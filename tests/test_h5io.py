@@ -137,6 +137,28 @@ def test_writer_round_trip(tmp_path):
         assert fh.read(24) == bytes.fromhex("894844460d0a1a0a00000000000808000400100000000000")
 
 
+def test_chunked_and_filtered_round_trip(tmp_path):
+    """Chunked datasets (B-tree v1 chunk index, as CUPRAD's unlimited datasets are stored), edge
+    chunks, a multi-level index and the deflate and shuffle filters."""
+    from mma_gb300 import h5io
+
+    rng = np.random.default_rng(2)
+    data = {"a": (rng.standard_normal((37, 50, 3)), dict(chunks=(8, 16, 3), compression="gzip", shuffle=True)),
+            "b": (np.arange(1000, dtype=np.int32).reshape(10, 100), dict(chunks=(3, 7))),
+            "c": (rng.standard_normal(5000).astype(np.float32), dict(chunks=(10,), compression="gzip",
+                                                                      compression_opts=9)),
+            "d": (rng.standard_normal((4, 6)), dict(compression="gzip"))}
+    p = str(tmp_path / "c.h5")
+    with h5io.File(p, "w") as f:
+        for k, (v, kw) in data.items():
+            f.create_dataset(k, data=v, **kw)
+    r = h5io.File(p)
+    for k, (v, _) in data.items():
+        assert r[k].dtype == v.dtype and np.array_equal(r[k][()], v), k
+    with pytest.raises(ValueError):
+        h5io.File(str(tmp_path / "x.h5"), "w").create_dataset("x", data=np.zeros((2, 2)), chunks=(2,))
+
+
 def test_append_keeps_existing(tmp_path):
     from mma_gb300 import h5io
 
