@@ -62,7 +62,7 @@ struct Params {
     const double* rg;
     const double* rho;
     const float* alpha;       // [n_omega][zpad]: scale of B rows (both re and im of plane k)
-    const float* ftab;        // [MM][zpad]: v_k^m / s_m
+    const float* ftab;        // [zpad][MM]: v_k^m / s_m, plane-major
     const int64_t* slot;      // [n_z]
     double* planes;           // [n_planes][n_rho][n_omega] complex128
     int* status;
@@ -286,53 +286,53 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             if (!ok) break;
             // ------------------------------------------------------------ epilogue of this tile
+            {   // while the tile's MMAs run, bring into L1 what this lane's epilogue reads: its row
+                // of per-plane factors and the group's slot and alpha entries (64 planes each), so
+                // that the epilogue's table loads hit L1 instead of waiting on L2 one store at a time
+                const int64_t kz0 = pb * NP + grp * (NP / 2);  // first plane of this group's columns
+                for (int q = lane; q < (NP / 2) * MM / 32; q += 32) prefetch_l1(P.ftab + kz0 * MM + 32 * q);
+                const int64_t ks_ = kz0 + 16 * (lane & 3);  // 64 slot entries: four 128-byte lines
+                prefetch_l1(P.slot + (ks_ < P.n_z ? ks_ : P.n_z - 1));
+                prefetch_l1(P.alpha + o * P.zpad + kz0 + 32 * (lane & 1));  // 64 floats: two lines
+            }
             if (!mbar_wait(acc_full, tt & 1u, abort_s, WAIT_NS)) {
                 fail(abort_s, P.status, 6);
                 break;
             }
             tc_fence_after();
-            // per-plane factors straight from global memory (ftab[m][plane], small and cached): no
-            // CTA-wide barrier here.  Group grp takes columns [grp * NCOL/2, (grp + 1) * NCOL/2).
+            // per-plane factors straight from global memory (ftab[plane][m], small and cached; the 16
+            // lanes of one rho row read one contiguous run per plane): no CTA-wide barrier here.
+            // Group grp takes columns [grp * NCOL/2, (grp + 1) * NCOL/2).
             const int mt = gw8 / 4, qd = warp % 4;
             const int row = qd * 32 + lane;
             const int m = row % MM;
-            const float* fm = P.ftab + (int64_t)m * P.zpad + pb * NP;
+            const float* fm = P.ftab + pb * NP * MM + m;
             const int64_t ig = rb * RC + mt * RT + row / MM;
-            for (int c0 = grp * (NCOL / 2); c0 < (grp + 1) * (NCOL / 2); c0 += CH) {
-                float v[CH];
-                {
-                    float t16[16];
-                    const uint32_t ta = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(mt * NCOL + c0);
-                    tmem_ld16(ta, t16);
+            // 32 columns per TMEM load (one wait), their CH-column groups reduced over the m lanes
+            // independently, so the groups' shuffle chains interleave
+            constexpr int CW = 32;
+            for (int c0 = grp * (NCOL / 2); c0 < (grp + 1) * (NCOL / 2); c0 += CW) {
+                float f[CW / 2];  // factors of the 16 planes of these columns, requested first
 #pragma unroll
-                    for (int j = 0; j < 16; j++) v[j] = t16[j];
-                    if constexpr (CH > 16) {
-                        tmem_ld16(ta + 16, t16);
+                for (int q = 0; q < CW / 2; q++) f[q] = __ldg(fm + ((c0 >> 1) + q) * MM);
+                float v[CW];
+                tmem_ld32(tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(mt * NCOL + c0), v);
 #pragma unroll
-                        for (int j = 0; j < 16; j++) v[(16 + j) % CH] = t16[j];
-                    }
-                }
-                float f[CH / 2];  // factors of the CH / 2 planes of these columns
+                for (int h = 0; h < CW / CH; h++) {
+                    float u[CH];
 #pragma unroll
-                for (int q4 = 0; q4 < CH / 8; q4++) {
-                    const float4 f4 = __ldg(reinterpret_cast<const float4*>(fm + (c0 >> 1)) + q4);
-                    f[4 * q4] = f4.x;
-                    f[4 * q4 + 1] = f4.y;
-                    f[4 * q4 + 2] = f4.z;
-                    f[4 * q4 + 3] = f4.w;
-                }
+                    for (int j = 0; j < CH; j++) u[j] = v[h * CH + j] * f[(h * CH + j) >> 1];
+                    reduce_scatter<MM, CH>(u, lane);
 #pragma unroll
-                for (int j = 0; j < CH; j++) v[j] *= f[j >> 1];
-                reduce_scatter<MM, CH>(v, lane);
-#pragma unroll
-                for (int j = 0; j < CH / MM; j++) {
-                    const int col = c0 + (lane % MM) * (CH / MM) + j;
-                    const int64_t kz = pb * NP + (col >> 1);
-                    if (kz < P.n_z && ig < P.n_rho) {
-                        const int64_t sl = __ldg(P.slot + kz);
-                        if (sl >= 0)
-                            P.planes[((sl * P.n_rho + ig) * P.n_omega + o) * 2 + (col & 1)] =
-                                (double)(v[j] * __ldg(P.alpha + o * P.zpad + kz));
+                    for (int j = 0; j < CH / MM; j++) {
+                        const int col = c0 + h * CH + (lane % MM) * (CH / MM) + j;
+                        const int64_t kz = pb * NP + (col >> 1);
+                        if (kz < P.n_z && ig < P.n_rho) {
+                            const int64_t sl = __ldg(P.slot + kz);
+                            if (sl >= 0)
+                                P.planes[((sl * P.n_rho + ig) * P.n_omega + o) * 2 + (col & 1)] =
+                                    (double)(u[j] * __ldg(P.alpha + o * P.zpad + kz));
+                        }
                     }
                 }
             }
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
     }
 }
 
-// per plane: dinv = 1/(2 D_k) as (hi, lo); ftab[m][k] = v_k^m / s_m = (v_k x)^m / m!, x = sigma y_max / 2;
+// per plane: dinv = 1/(2 D_k) as (hi, lo); ftab[k][m] = v_k^m / s_m = (v_k x)^m / m!, x = sigma y_max / 2;
 // per radius: rgf = r as float-float
 __global__ void plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, const double* zg, const double* rg,
                             int mm, int64_t zpad, int64_t rpad, float2* dinv, float* ftab, float2* rgf)
@@ -474,7 +474,7 @@ __global__ void plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, cons
     const double x = 0.5 * F.sigma * F.y_max;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < zpad; q += (int64_t)gridDim.x * blockDim.x) {
         if (q >= P.n_z) {
-            for (int m = 0; m < mm; m++) ftab[m * zpad + q] = 0.f;
+            for (int m = 0; m < mm; m++) ftab[q * mm + m] = 0.f;
             continue;
         }
         const double D = P.distance - zg[q];
@@ -482,7 +482,7 @@ __global__ void plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, cons
         const double v = (1.0 - lam * lam) / F.sigma;
         double c = 1.0;
         for (int m = 0; m < mm; m++) {
-            ftab[m * zpad + q] = (float)c;
+            ftab[q * mm + m] = (float)c;
             c *= (x > 0.0 ? v * x : v) / (double)(m + 1);
         }
         float hi, lo;
