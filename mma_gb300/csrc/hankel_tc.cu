@@ -219,72 +219,94 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int grp = gw / GWARPS, gw8 = gw % GWARPS;  // generator group (alternate K-blocks), warp in it
         const int hw = lane >> 4, k0 = 2 * (lane & 15);  // half-warp -> rho row; lane -> r pair (k0, k0+1)
         constexpr int PASSES = (RC + 2 * GWARPS - 1) / (2 * GWARPS);
-        uint32_t it = 0, tt = 0;
+        uint32_t tt = 0;
         bool ok = true;
         const float tw = P.two_over_ymax, iy = P.inv_ymax;
-        for (int64_t tile = blockIdx.x; ok && tile < P.n_tiles; tile += gridDim.x, tt++) {
-            const int64_t o = tile / (P.n_pb * P.n_rb), pb = (tile / P.n_rb) % P.n_pb, rb = tile % P.n_rb;
+        // k rho / d_ref of this half-warp's rows (float-float) for a tile
+        auto rows_of = [&](int64_t tile, float (&kh)[PASSES], float (&kl)[PASSES]) {
+            const int64_t o = tile / (P.n_pb * P.n_rb), rb = tile % P.n_rb;
             const double kap = P.og[o] * P.inv_cd;
-            float kh[PASSES], kl[PASSES];  // k rho / d_ref of this half-warp's rows (float-float)
 #pragma unroll
             for (int j = 0; j < PASSES; j++) {
                 const int q = gw8 + GWARPS * (2 * j + hw);
                 const int64_t ig = rb * RC + q;
                 split_d((q < RC && ig < P.n_rho) ? kap * P.rho[ig] : 0.0, kh[j], kl[j]);
             }
-            for (int kb = 0; kb < nkb; kb++, it++) {
-                if ((int)(it & 1u) != grp) continue;  // the other group generates this K-block
-                const uint32_t s = it % STAGES, ph = (it / STAGES) & 1u;
-                // r and r+1 as float-float (hi0, lo0, hi1, lo1), loaded before the wait
-                const float4 rv = __ldg(reinterpret_cast<const float4*>(P.rgf) + ((int64_t)kb * KB + k0) / 2);
-                if (!mbar_wait(&empty[s], ph ^ 1u, abort_s, WAIT_NS)) {
-                    fail(abort_s, P.status, 5);
-                    ok = false;
-                    break;
-                }
-                uint8_t* st = smem + s * STAGE_BYTES;
-#pragma unroll
-                for (int j = 0; j < PASSES; j++) {
-                    const int q = gw8 + GWARPS * (2 * j + hw);  // rho row within the CTA tile
-                    if (q >= RC) continue;                   // uniform per half-warp
-                    const int mt = q / RT, rloc = q % RT;
-                    uint8_t* ah = st + mt * 2 * A_BYTES;
-                    uint8_t* al = ah + A_BYTES;
-                    const float y0h = kh[j] * rv.x, y0l = fmaf(kh[j], rv.x, -y0h) + fmaf(kh[j], rv.y, kl[j] * rv.x);
-                    const float y1h = kh[j] * rv.z, y1l = fmaf(kh[j], rv.z, -y1h) + fmaf(kh[j], rv.w, kl[j] * rv.z);
-                    float J00, J10, J01, J11;
-                    bessel01<true>(y0h, y0l, J00, J10);
-                    bessel01<true>(y1h, y1l, J01, J11);
-                    // K^_m = u^m J_m(y), u = y / y_max <= 1:  K^_{m+1} = (2m / y_max) K^_m - u^2 K^_{m-1}
-                    const float u0 = (y0h + y0l) * iy, u1 = (y1h + y1l) * iy;
-                    const float w0 = u0 * u0, w1 = u1 * u1;
-                    auto put2 = [&](int m, float x0, float x1) {
-                        const __half2 h = __floats2half2_rn(x0, x1);
-                        const float2 f = __half22float2(h);
-                        const __half2 l = __floats2half2_rn(x0 - f.x, x1 - f.y);
-                        const uint32_t off = sw64_offset((uint32_t)(rloc * MM + m), (uint32_t)k0);
-                        *reinterpret_cast<__half2*>(ah + off) = h;
-                        *reinterpret_cast<__half2*>(al + off) = l;
-                    };
-                    float a0 = J00, b0 = u0 * J10, a1 = J01, b1 = u1 * J11;
-                    put2(0, a0, a1);
-                    put2(1, b0, b1);
-#pragma unroll
-                    for (int m = 1; m + 1 < MM; m++) {
-                        const float c = (float)m * tw;
-                        const float n0 = fmaf(c, b0, -w0 * a0), n1 = fmaf(c, b1, -w1 * a1);
-                        put2(m + 1, n0, n1);
-                        a0 = b0;
-                        b0 = n0;
-                        a1 = b1;
-                        b1 = n1;
-                    }
-                }
-                fence_async_smem();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&full[s]);
+        };
+        // the A operand of K-block kb (this CTA's K-block number it) into its stage; false on timeout
+        auto gen_block = [&](int kb, uint32_t it, const float (&kh)[PASSES], const float (&kl)[PASSES]) -> bool {
+            if ((int)(it & 1u) != grp) return true;  // the other group generates this K-block
+            const uint32_t s = it % STAGES, ph = (it / STAGES) & 1u;
+            // r and r+1 as float-float (hi0, lo0, hi1, lo1), loaded before the wait
+            const float4 rv = __ldg(reinterpret_cast<const float4*>(P.rgf) + ((int64_t)kb * KB + k0) / 2);
+            if (!mbar_wait(&empty[s], ph ^ 1u, abort_s, WAIT_NS)) {
+                fail(abort_s, P.status, 5);
+                return false;
             }
+            uint8_t* st = smem + s * STAGE_BYTES;
+#pragma unroll
+            for (int j = 0; j < PASSES; j++) {
+                const int q = gw8 + GWARPS * (2 * j + hw);  // rho row within the CTA tile
+                if (q >= RC) continue;                   // uniform per half-warp
+                const int mt = q / RT, rloc = q % RT;
+                uint8_t* ah = st + mt * 2 * A_BYTES;
+                uint8_t* al = ah + A_BYTES;
+                const float y0h = kh[j] * rv.x, y0l = fmaf(kh[j], rv.x, -y0h) + fmaf(kh[j], rv.y, kl[j] * rv.x);
+                const float y1h = kh[j] * rv.z, y1l = fmaf(kh[j], rv.z, -y1h) + fmaf(kh[j], rv.w, kl[j] * rv.z);
+                float J00, J10, J01, J11;
+                bessel01<true>(y0h, y0l, J00, J10);
+                bessel01<true>(y1h, y1l, J01, J11);
+                // K^_m = u^m J_m(y), u = y / y_max <= 1:  K^_{m+1} = (2m / y_max) K^_m - u^2 K^_{m-1}
+                const float u0 = (y0h + y0l) * iy, u1 = (y1h + y1l) * iy;
+                const float w0 = u0 * u0, w1 = u1 * u1;
+                auto put2 = [&](int m, float x0, float x1) {
+                    const __half2 h = __floats2half2_rn(x0, x1);
+                    const float2 f = __half22float2(h);
+                    const __half2 l = __floats2half2_rn(x0 - f.x, x1 - f.y);
+                    const uint32_t off = sw64_offset((uint32_t)(rloc * MM + m), (uint32_t)k0);
+                    *reinterpret_cast<__half2*>(ah + off) = h;
+                    *reinterpret_cast<__half2*>(al + off) = l;
+                };
+                float a0 = J00, b0 = u0 * J10, a1 = J01, b1 = u1 * J11;
+                put2(0, a0, a1);
+                put2(1, b0, b1);
+#pragma unroll
+                for (int m = 1; m + 1 < MM; m++) {
+                    const float c = (float)m * tw;
+                    const float n0 = fmaf(c, b0, -w0 * a0), n1 = fmaf(c, b1, -w1 * a1);
+                    put2(m + 1, n0, n1);
+                    a0 = b0;
+                    b0 = n0;
+                    a1 = b1;
+                    b1 = n1;
+                }
+            }
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full[s]);
+            return true;
+        };
+        // Each tile: its remaining K-blocks, then the next tile's first K-blocks (their stages free
+        // up as this tile's last MMAs complete, before its epilogue), then this tile's epilogue --
+        // so the next tile's MMAs start as soon as the accumulators are drained.
+        constexpr int AHEAD = STAGES;
+        float kh[PASSES], kl[PASSES], khn[PASSES], kln[PASSES];
+        if (blockIdx.x < P.n_tiles) rows_of(blockIdx.x, kh, kl);
+        int done_ahead = 0;
+        uint32_t it0 = 0;  // K-block number of this tile's first K-block
+        for (int64_t tile = blockIdx.x; ok && tile < P.n_tiles; tile += gridDim.x, tt++, it0 += (uint32_t)nkb) {
+            const int64_t o = tile / (P.n_pb * P.n_rb), pb = (tile / P.n_rb) % P.n_pb, rb = tile % P.n_rb;
+            for (int kb = done_ahead; ok && kb < nkb; kb++) ok = gen_block(kb, it0 + kb, kh, kl);
             if (!ok) break;
+            const int64_t next = tile + gridDim.x;
+            done_ahead = 0;
+            if (next < P.n_tiles) {
+                rows_of(next, khn, kln);
+                const int na = AHEAD < nkb ? AHEAD : nkb;
+                for (int kb = 0; ok && kb < na; kb++) ok = gen_block(kb, it0 + nkb + kb, khn, kln);
+                if (!ok) break;
+                done_ahead = na;
+            }
             // ------------------------------------------------------------ epilogue of this tile
             {   // while the tile's MMAs run, bring into L1 what this lane's epilogue reads: its row
                 // of per-plane factors and the group's slot and alpha entries (64 planes each), so
@@ -339,6 +361,11 @@ __global__ void __launch_bounds__(THREADS, 1)
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(acc_empty);
+#pragma unroll
+            for (int j = 0; j < PASSES; j++) {
+                kh[j] = khn[j];
+                kl[j] = kln[j];
+            }
         }
     }
     tc_fence_before();
