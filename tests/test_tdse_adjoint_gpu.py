@@ -82,7 +82,7 @@ def _torch_reference(grids, E, dtf, band):
         fk = E[k] if k < nf else torch.zeros((), dtype=torch.float64)
         fk1 = E[k + 1] if k + 1 < nf else torch.zeros((), dtype=torch.float64)
         if not gate_open:
-            if float(fk) * float(fk1) <= 0.0:
+            if float(fk.detach()) * float(fk1.detach()) <= 0.0:  # the gate is not differentiated
                 gate_open = True
             F = torch.zeros((), dtype=torch.float64)
         else:
