@@ -610,6 +610,25 @@ WORKLOADS = {
 }
 
 
+def max_over_ranks(x, world, device=None):
+    """The largest value of x over the ranks, on every rank: the step time of the slowest replica,
+    which sets the whole job's throughput.  NCCL reduces on the rank's GPU, other backends on CPU."""
+    if world <= 1:
+        return float(x)
+    import torch
+
+    on_gpu = device is not None and torch.distributed.get_backend() == "nccl"
+    tt = torch.tensor([float(x)], dtype=torch.float64, device=device if on_gpu else "cpu")
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_throughput(units_per_rank, seconds_slowest, world):
+    """Whole-job throughput of `world` independent replicas that each process units_per_rank,
+    timed by the slowest replica (weak scaling)."""
+    return world * units_per_rank / seconds_slowest
+
+
 def run_ours(args, rank, world, precision):
     import torch
 
@@ -658,13 +677,9 @@ def run_ours(args, rank, world, precision):
     if world > 1:
         torch.distributed.barrier()
     ms = [a.elapsed_time(b) for a, b in ev]
-    ms_step = float(np.mean(ms))
-    if world > 1:
-        tt = torch.tensor([ms_step], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(tt.item())
+    ms_step = max_over_ranks(float(np.mean(ms)), world, dev)
     site_steps = float(n_inst) * sites * S
-    value = world * site_steps / (ms_step * 1e-3)
+    value = replica_throughput(site_steps, ms_step * 1e-3, world)
 
     # propagation kernel alone: launch duration for the roofline
     kev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
