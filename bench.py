@@ -646,7 +646,7 @@ def run_ours(args, rank, world, precision):
     fields = torch.tensor(fields_np, device=dev)
     grids = TDSEGrids([dict(num_r=8000, dx=0.1, trg_a=A_CONFIG)], dt=dtf, c64=(precision == "c64"),
                       c64_threads=(args.c64_threads if args.c64_threads == "auto" else int(args.c64_threads))
-                      if precision == "c64" else None)
+                      if precision == "c64" else None, df64=(precision == "df64"))
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
     stream = torch.cuda.current_stream()
     plan = TDSEBatchPlan(grids, [fields.shape[1]] * n_inst, dtf, tmax=tmax, precision=precision)
@@ -776,7 +776,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-hankel", action="store_true")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config1")
-    ap.add_argument("--forms", choices=["both", "fp64", "c64"], default="both")
+    ap.add_argument("--forms", choices=["all", "both", "fp64", "c64", "df64"], default="all",
+                    help="all: FP64, complex64 and float-float; both: FP64 and complex64")
     ap.add_argument("--c64-threads", default="auto",
                     help="CTA size of the complex64 kernel: auto (the autotuner) or 256, 512, 1024")
     args = ap.parse_args()
@@ -818,12 +819,13 @@ def main():
               "small_adjoint": run_profile_case}[args.workload]
         print(json.dumps({"workload": args.workload, "result": fn(args, dev)}))
         return
-    r64 = run_ours(args, rank, world, "fp64") if args.forms in ("both", "fp64") else None
-    r = run_ours(args, rank, world, "c64") if args.forms in ("both", "c64") else None
+    r64 = run_ours(args, rank, world, "fp64") if args.forms in ("all", "both", "fp64") else None
+    r = run_ours(args, rank, world, "c64") if args.forms in ("all", "both", "c64") else None
+    rdf = run_ours(args, rank, world, "df64") if args.forms in ("all", "df64") else None
     if rank != 0:
         return
     if r is None or r64 is None:  # single-form run (profiling): a short line, no form comparison
-        one = r or r64
+        one = r or r64 or rdf
         print(json.dumps({"metric": METRIC, "value": one["value"], "unit": "site-steps/s", "forms": args.forms,
                           "workload": args.workload, "ms_per_step": one["ms_per_step"],
                           "kernel_ms": one["kernel_ms"]}))
@@ -851,6 +853,13 @@ def main():
                             "autotune_seconds_per_probe_batch": r["autotune"],
                             "error_vs_fp64": errs},
     }
+    if rdf is not None:  # float-float: the FP64 step in double-word FP32, bound by FP32 issue
+        a_df = FLOPS_PER_SITE_STEP * site_steps / (rdf["kernel_ms"] * 1e-3)
+        forms["tdse_float_float"] = {"site_steps_per_s": rdf["value"], "ms_per_step": rdf["ms_per_step"],
+                                     "kernel_ms": rdf["kernel_ms"], "speedup_vs_plain": rdf["value"] / r64["value"],
+                                     "algorithmic_tflops": a_df / 1e12,
+                                     "e2e_site_steps_per_s": world * site_steps / (rdf["e2e_ms"] * 1e-3),
+                                     "error_vs_fp64": form_errors(rdf, r64)}
     line = {"metric": METRIC, "value": r["value"], "unit": "site-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64 (fp32 propagation, fp64 factorisation/accumulation)",

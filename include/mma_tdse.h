@@ -194,6 +194,8 @@ const char *mma_last_error_message(void);
  *            written by mma_tdse_build_grids when not NULL)
  *   c64_threads  CTA size the c64 tables are laid out for: 0 or 256 (m32 <= 48),
  *            512 (m32 8 or 16) or 1024 (m32 8); c64_tab then holds 4 * c64_threads * m32 floats
+ *   df_tab   [28 L] floats, the cn_tab entries split into (hi, lo) float pairs for the
+ *            float-float form (precision 2); NULL when unused (written by mma_tdse_build_df_tables)
  * The record has 8-byte fields only, so its layout is the same in every ABI. */
 typedef struct mma_tdse_grid {
     int64_t n, m;
@@ -204,6 +206,7 @@ typedef struct mma_tdse_grid {
     float *c64_tab;
     double *adj_tab;
     int64_t c64_threads;
+    float *df_tab;
 } mma_tdse_grid;
 
 /* One TDSE instance of a batch (offsets are in doubles). */
@@ -255,17 +258,24 @@ int mma_tdse_build_c64_tables(const mma_tdse_grid *grids_dev, const mma_tdse_gri
  *   precision  0 = FP64, the reference's arithmetic;
  *              1 = complex64 propagation (FP32 wavefunction and sweeps) with the
  *                  factorisation computed in FP64 and the observables summed with
- *                  compensation and finished in FP64; needs c64 tables (n <= 8192) */
+ *                  compensation and finished in FP64; needs c64 tables (n <= 8192);
+ *              2 = float-float propagation: the FP64 step and tables carried in double-word
+ *                  FP32 arithmetic (about 48 significant bits); needs df tables */
 int mma_tdse_propagate(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
                        const mma_tdse_buffers *bufs, int max_m, int grid_ctas, int precision, void *stream);
 
 /* mma_tdse_propagate with the CTA size of the complex64 form chosen by the caller (0 = 256):
  * every instance's grid must carry c64 tables of shape (cta_threads, max_m), see
  * mma_tdse_grid.c64_threads; instances whose grid has another shape get NaN outputs.
- * For precision 0 cta_threads must be 0 or 256. */
+ * For precisions 0 and 2 cta_threads must be 0 or 256. */
 int mma_tdse_propagate_ex(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
                           const mma_tdse_buffers *bufs, int max_m, int cta_threads, int grid_ctas, int precision,
                           void *stream);
+
+/* Split the FP64 solve tables of n_grids grids (after mma_tdse_build_grids) into the (hi, lo)
+ * float pairs of the float-float form: every grid needs df_tab (28 L floats). */
+int mma_tdse_build_df_tables(const mma_tdse_grid *grids_dev, const mma_tdse_grid *grids_host, int n_grids,
+                             void *stream);
 
 /* 1 if the complex64 form has a kernel for CTA size cta_threads (0 = 256) and m32 sites per thread. */
 int mma_tdse_c64_shape_ok(int cta_threads, int m32);

@@ -1,0 +1,443 @@
+// tdse_df64.cu -- float-float ("df64") form of the TDSE propagation: the FP64 Crank-Nicolson-
+// Numerov step (prop.c:115-347, the same tables and partitioned solve as propagate_fp64_kernel)
+// carried out in double-word FP32 arithmetic.
+//
+// On this GPU FP32 runs at about 62x the FP64 rate, so a double-word operation of 6-25 FP32
+// instructions still outruns one FP64 operation.  A value is a pair (hi, lo) of floats with
+// |lo| <= ulp(hi)/2, about 48 significant bits; every operation below is built from two
+// error-free transformations:
+//   * TwoSum (Knuth): s + e = a + b exactly, s = fl(a + b);
+//   * TwoProduct with an FMA: p + e = a b exactly, p = fl(a b), e = fma(a, b, -p);
+// with the accurate double-word addition of Joldes, Muller and Popescu ("Tight and rigorous
+// error bounds for basic building blocks of double-word arithmetic", ACM TOMS 2017, Alg. 6):
+// relative error about 3 u^2 (u = 2^-24).  Products and sums of products fold their low-order
+// terms with FMAs before one final renormalisation.
+//
+// Layout as in the FP64 kernel: site j = t m + i at q = i T + t; psi in shared memory when it
+// fits (16 bytes per site), the sweep buffer in the caller's scratch; the tables are the FP64
+// tables split once per grid into (hi, lo) float pairs (mma_tdse_build_df_tables).
+#include <cuda_runtime.h>
+
+#include "../../include/mma_tdse.h"
+#include "common.cuh"
+#include "tdse_step.cuh"
+
+namespace mma {
+namespace dfk {
+
+struct df {
+    float hi, lo;
+};
+struct cdf {
+    df re, im;
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e)  // |a| >= |b|
+{
+    s = a + b;
+    e = b - (s - a);
+}
+__device__ __forceinline__ df renorm(float s, float e)
+{
+    df r;
+    fast_two_sum(s, e, r.hi, r.lo);
+    return r;
+}
+// x + y (Joldes, Muller, Popescu 2017, Algorithm 6)
+__device__ __forceinline__ df add(df x, df y)
+{
+    float sh, sl, th, tl;
+    two_sum(x.hi, y.hi, sh, sl);
+    two_sum(x.lo, y.lo, th, tl);
+    sl += th;
+    fast_two_sum(sh, sl, sh, sl);
+    sl += tl;
+    return renorm(sh, sl);
+}
+__device__ __forceinline__ df neg(df x) { return df{-x.hi, -x.lo}; }
+__device__ __forceinline__ df sub(df x, df y) { return add(x, neg(y)); }
+// x y
+__device__ __forceinline__ df mul(df x, df y)
+{
+    const float p = x.hi * y.hi;
+    float e = fmaf(x.hi, y.hi, -p);
+    e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e));
+    return renorm(p, e);
+}
+// a b + c d + z (products exact to first order, one accurate sum with z)
+__device__ __forceinline__ df dot2_add(df a, df b, df c, df d, df z)
+{
+    const float p = a.hi * b.hi, q = c.hi * d.hi;
+    float ep = fmaf(a.hi, b.hi, -p), eq = fmaf(c.hi, d.hi, -q);
+    ep = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, ep));
+    eq = fmaf(c.hi, d.lo, fmaf(c.lo, d.hi, eq));
+    float s1, t1, s2, t2;
+    two_sum(p, q, s1, t1);
+    two_sum(s1, z.hi, s2, t2);
+    const float e = ((t1 + t2) + (ep + eq)) + z.lo;
+    return renorm(s2, e);
+}
+__device__ __forceinline__ cdf cmul(cdf a, cdf b)
+{
+    const df z{0.f, 0.f};
+    return cdf{dot2_add(a.re, b.re, neg(a.im), b.im, z), dot2_add(a.re, b.im, a.im, b.re, z)};
+}
+// z + a b
+__device__ __forceinline__ cdf cfma(cdf a, cdf b, cdf z)
+{
+    return cdf{dot2_add(a.re, b.re, neg(a.im), b.im, z.re), dot2_add(a.re, b.im, a.im, b.re, z.im)};
+}
+// z - a b
+__device__ __forceinline__ cdf cfms(cdf a, cdf b, cdf z)
+{
+    return cdf{dot2_add(neg(a.re), b.re, a.im, b.im, z.re), dot2_add(neg(a.re), b.im, neg(a.im), b.re, z.im)};
+}
+__device__ __forceinline__ cdf cadd(cdf a, cdf b) { return cdf{add(a.re, b.re), add(a.im, b.im)}; }
+__device__ __forceinline__ cdf csub(cdf a, cdf b) { return cdf{sub(a.re, b.re), sub(a.im, b.im)}; }
+// 10 p + s, with 10 p exact to first order
+__device__ __forceinline__ df ten_plus(df p, df s)
+{
+    const float a = 10.f * p.hi;
+    float e = fmaf(10.f, p.hi, -a);
+    e = fmaf(10.f, p.lo, e);
+    float s1, t1;
+    two_sum(a, s.hi, s1, t1);
+    return renorm(s1, (t1 + e) + s.lo);
+}
+
+__device__ __forceinline__ df from_d(double v)
+{
+    const float h = (float)v;
+    return df{h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ double to_d(df v) { return (double)v.hi + (double)v.lo; }
+__device__ __forceinline__ cdf ld(const float4* p) { const float4 v = *p; return cdf{{v.x, v.y}, {v.z, v.w}}; }
+__device__ __forceinline__ void st(float4* p, cdf v) { *p = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo); }
+
+__device__ __forceinline__ df shfl_up_df(df v, int d)
+{
+    return df{__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d)};
+}
+__device__ __forceinline__ df shfl_dn_df(df v, int d)
+{
+    return df{__shfl_down_sync(0xffffffffu, v.hi, d), __shfl_down_sync(0xffffffffu, v.lo, d)};
+}
+__device__ __forceinline__ df shfl_xor_df(df v, int d)
+{
+    return df{__shfl_xor_sync(0xffffffffu, v.hi, d), __shfl_xor_sync(0xffffffffu, v.lo, d)};
+}
+__device__ __forceinline__ cdf shup(cdf v, int d) { return cdf{shfl_up_df(v.re, d), shfl_up_df(v.im, d)}; }
+__device__ __forceinline__ cdf shdn(cdf v, int d) { return cdf{shfl_dn_df(v.re, d), shfl_dn_df(v.im, d)}; }
+
+// exclusive CTA scans of the affine maps Y_t = b_t + c_t Y_{t-1} (forward) and
+// U_t = b_t + c_t U_{t+1} (backward), as scan_forward / scan_backward (tdse_solver.cuh)
+__device__ cdf scan_fwd(cdf c, cdf b, cdf* sc, cdf* sb)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const cdf cp = shup(c, d), bp = shup(b, d);
+        if (lane >= d) {
+            b = cfma(c, bp, b);
+            c = cmul(c, cp);
+        }
+    }
+    if (lane == 31) {
+        sc[w] = c;
+        sb[w] = b;
+    }
+    __syncthreads();
+    cdf yw{{0.f, 0.f}, {0.f, 0.f}};
+    for (int q = 0; q < w; q++) yw = cfma(sc[q], yw, sb[q]);
+    const cdf cp = shup(c, 1), bp = shup(b, 1);
+    return lane == 0 ? yw : cfma(cp, yw, bp);
+}
+
+__device__ cdf scan_bwd(cdf c, cdf b, cdf* sc, cdf* sb)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const cdf cp = shdn(c, d), bp = shdn(b, d);
+        if (lane + d < 32) {
+            b = cfma(c, bp, b);
+            c = cmul(c, cp);
+        }
+    }
+    if (lane == 0) {
+        sc[w] = c;
+        sb[w] = b;
+    }
+    __syncthreads();
+    cdf uw{{0.f, 0.f}, {0.f, 0.f}};
+    for (int q = kWarps - 1; q > w; q--) uw = cfma(sc[q], uw, sb[q]);
+    const cdf cp = shdn(c, 1), bp = shdn(b, 1);
+    return lane == 31 ? uw : cfma(cp, uw, bp);
+}
+
+struct Args {
+    const mma_tdse_instance* insts;
+    int n_inst;
+    const mma_tdse_grid* grids;
+    const double* fields;
+    double* outputs;
+    double* psi_final;
+    double* snapshots;
+    int* counter;
+    float4* scratch;  // per CTA: yl [L], then (when psi is not in shared memory) psi [L]
+    int64_t max_L;
+};
+
+constexpr int kPow = 8;  // e^{i F dt M dx 2^b}, b < 8: the chunk-start phases of 256 threads
+
+template <bool PSI_SMEM>
+__global__ void __launch_bounds__(kThreads, 1) propagate_df64_kernel(Args P)
+{
+    extern __shared__ float4 smem_dyn[];
+    __shared__ cdf sc[2 * kWarps], sb[2 * kWarps];
+    __shared__ double red[kWarps * 5];
+    __shared__ cdf s_pow[kPow + 2];  // e^{i F dt x_0}, e^{i F dt dx}, e^{i F dt M dx 2^b}
+    __shared__ int64_t s_inst, s_gate, s_lo, s_hi;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    float4* yl = P.scratch + blockIdx.x * P.max_L;
+    float4* psi = PSI_SMEM ? smem_dyn : P.scratch + (gridDim.x + blockIdx.x) * P.max_L;
+
+    for (;;) {
+        if (t == 0) s_inst = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int64_t inst = s_inst;
+        if (inst >= P.n_inst) break;
+        const mma_tdse_instance I = P.insts[inst];
+        const mma_tdse_grid G = P.grids[I.grid];
+        const int64_t n = G.n, m = G.m, L = m * kThreads, S = I.n_steps;
+        const float4* tab = reinterpret_cast<const float4*>(G.df_tab);
+        const float4 *IB = tab + CN_IB6 * L, *HH = tab + CN_H * L, *FF = tab + CN_F * L, *GG_ = tab + CN_G * L,
+                     *GP = tab + CN_GG * L, *P0 = tab + CN_PSI0 * L, *GVX = tab + CN_GVX * L;
+        const double* f = P.fields + I.field_off;
+        double* out = P.outputs + I.out_off;
+        double *o_t = out, *o_e = out + (S + 1), *o_src = out + 2 * (S + 1), *o_ptot = out + 3 * (S + 1),
+               *o_pint = out + 4 * (S + 1), *o_x = out + 5 * (S + 1);
+        const double dt = G.dt, dx = G.dx;
+        if (t == 0) {
+            s_gate = gate_index(f, I.n_field, S, I.gate_floor);
+            const int64_t num_r = n - 1;  // PopInt window (tools_algorithmic.c:19-43)
+            int64_t lo = -1, hi;
+            if (!(-G.x_int < G.x[0])) {
+                int64_t i = 0;
+                while (i < num_r && !(-G.x_int <= G.x[i + 1])) i++;
+                lo = i;
+            }
+            if (G.x_int < G.x[0]) {
+                hi = 0;
+            } else {
+                int64_t i = 0;
+                while (i < num_r && !(G.x_int <= G.x[i + 1])) i++;
+                hi = (i < num_r) ? i + 1 : num_r + 1;
+            }
+            s_lo = lo < 0 ? 0 : lo;
+            s_hi = hi > num_r ? num_r : hi;
+        }
+        for (int64_t i = 0; i < m; i++) psi[i * kThreads + t] = P0[i * kThreads + t];
+        __syncthreads();
+        const int64_t lo = s_lo, hi = s_hi, gate = s_gate;
+        const int64_t s0 = t * m;
+        {   // initial window population (prop.c:87-93), FP64 from the FP64 ground state
+            double v[1] = {0.0};
+            for (int64_t j = t; j < n; j += kThreads)
+                if (j >= lo && j <= hi) v[0] += G.psi0[2 * j] * G.psi0[2 * j] + G.psi0[2 * j + 1] * G.psi0[2 * j + 1];
+            block_sum<1>(v, red);
+            if (t == 0) {
+                o_t[0] = I.tmin;
+                o_e[0] = 0.0;
+                o_src[0] = 0.0;
+                o_ptot[0] = 1.0;
+                o_pint[0] = v[0];
+                o_x[0] = 0.0;
+            }
+        }
+        double tt = I.tmin;
+        const double x0 = G.x[0];
+        for (int64_t k = 0; k < S; k++) {
+            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : f[k];
+            if (t == 0) {
+                if (k > 0) {  // the previous step's observables
+                    double s[5];
+#pragma unroll
+                    for (int c = 0; c < 5; c++) {
+                        s[c] = 0.0;
+#pragma unroll
+                        for (int q = 0; q < kWarps; q++) s[c] += red[q * 5 + c];
+                    }
+                    o_src[k] = -s[0] + o_e[k];
+                    o_ptot[k] = s[2] * s[2] + s[3] * s[3];
+                    o_x[k] = s[1];
+                    o_pint[k] = s[4];
+                }
+                tt += dt;
+                o_t[k + 1] = tt;
+                o_e[k + 1] = Fk;
+            }
+            // the step's phase factors in FP64, by ten lanes of the last warp: e^{i F dt x_0},
+            // e^{i F dt dx} and e^{i F dt m dx 2^b}
+            if (w == kWarps - 1 && lane < kPow + 2) {
+                const double ang = lane == 0 ? Fk * dt * x0 : (lane == 1 ? Fk * dt * dx
+                                                                        : Fk * dt * (double)m * dx * (double)(1 << (lane - 2)));
+                double sn, cs;
+                sincos(ang, &sn, &cs);
+                s_pow[lane] = cdf{from_d(cs), from_d(sn)};
+            }
+            // ---- pass 1: local forward sweep of the right-hand side 2 M2 psi
+            cdf pm = (t == 0) ? cdf{{0.f, 0.f}, {0.f, 0.f}} : ld(psi + (m - 1) * kThreads + t - 1);
+            cdf pc = ld(psi + t);
+            cdf yprev{{0.f, 0.f}, {0.f, 0.f}};
+            for (int64_t i = 0; i < m; i++) {
+                const int64_t q = i * kThreads + t;
+                const cdf pn = (i + 1 < m) ? ld(psi + q + kThreads)
+                                           : ((t + 1 < kThreads) ? ld(psi + t + 1) : cdf{{0.f, 0.f}, {0.f, 0.f}});
+                const cdf r{ten_plus(pc.re, add(pm.re, pn.re)), ten_plus(pc.im, add(pm.im, pn.im))};
+                yprev = cfms(ld(HH + q), yprev, cmul(ld(IB + q), r));
+                st(yl + q, yprev);
+                pm = pc;
+                pc = pn;
+            }
+            const cdf yin = scan_fwd(ld(FF + (m - 1) * kThreads + t), yprev, sc, sb);
+            // ---- pass 2: forward correction, local backward sweep
+            cdf unext{{0.f, 0.f}, {0.f, 0.f}};
+            for (int64_t i = m - 1; i >= 0; i--) {
+                const int64_t q = i * kThreads + t;
+                const cdf y = cfma(ld(FF + q), yin, ld(yl + q));
+                unext = cfms(ld(GG_ + q), unext, y);
+                st(yl + q, unext);
+            }
+            const cdf uin = scan_bwd(ld(GP + t), unext, sc + kWarps, sb + kWarps);
+            // ---- pass 3: backward correction, CN update, phase e^{+i F dt x}, observables
+            cdf ph = s_pow[0];  // e^{i F dt x_0} (e^{i F dt m dx})^t = e^{i F dt x_{s0}}
+#pragma unroll
+            for (int b = 0; b < kPow; b++)
+                if (t & (1 << b)) ph = cmul(ph, s_pow[2 + b]);
+            const cdf z = s_pow[1];
+            df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+            double pint = 0.0;
+            for (int64_t i = 0; i < m; i++) {
+                const int64_t q = i * kThreads + t;
+                const cdf u = cfma(ld(GP + q), uin, ld(yl + q));
+                const cdf pn = cmul(ph, csub(u, ld(psi + q)));
+                st(psi + q, pn);
+                ph = cmul(ph, z);
+                const df n2 = dot2_add(pn.re, pn.re, pn.im, pn.im, df{0.f, 0.f});
+                const cdf gx = ld(GVX + q), p0 = ld(P0 + q);
+                acc[0] = dot2_add(n2, gx.re, df{0.f, 0.f}, df{0.f, 0.f}, acc[0]);
+                acc[1] = dot2_add(n2, gx.im, df{0.f, 0.f}, df{0.f, 0.f}, acc[1]);
+                acc[2] = dot2_add(pn.re, p0.re, pn.im, p0.im, acc[2]);
+                acc[3] = dot2_add(pn.re, p0.im, neg(pn.im), p0.re, acc[3]);
+                const int64_t j = s0 + i;
+                if (j >= lo && j <= hi) pint += to_d(n2);
+            }
+            // warp sums in double-word arithmetic, across warps in FP64
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) {
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[c] = add(acc[c], shfl_xor_df(acc[c], d));
+                pint += __shfl_xor_sync(0xffffffffu, pint, d);
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int c = 0; c < 4; c++) red[w * 5 + c] = to_d(acc[c]);
+                red[w * 5 + 4] = pint;
+            }
+            if (I.snap_off >= 0 && P.snapshots) {  // prop.c:248-263
+                int64_t slot = -1;
+                if (k % I.snap_every == 0 && k / I.snap_every < I.n_snap - 1) slot = k / I.snap_every;
+                if (k == S - 1) slot = I.n_snap - 1;
+                if (slot >= 0) {
+                    double* sp = P.snapshots + I.snap_off + slot * 2 * n;
+                    for (int64_t i = 0; i < m; i++)
+                        if (s0 + i < n) {
+                            const cdf v = ld(psi + i * kThreads + t);
+                            sp[2 * (s0 + i)] = to_d(v.re);
+                            sp[2 * (s0 + i) + 1] = to_d(v.im);
+                        }
+                }
+            }
+            __syncthreads();
+        }
+        if (t == 0) {
+            double s[5];
+#pragma unroll
+            for (int c = 0; c < 5; c++) {
+                s[c] = 0.0;
+#pragma unroll
+                for (int q = 0; q < kWarps; q++) s[c] += red[q * 5 + c];
+            }
+            o_src[S] = -s[0] + o_e[S];
+            o_ptot[S] = s[2] * s[2] + s[3] * s[3];
+            o_x[S] = s[1];
+            o_pint[S] = s[4];
+        }
+        if (P.psi_final && I.psi_off >= 0) {
+            double* pf = P.psi_final + I.psi_off;
+            for (int64_t i = 0; i < m; i++)
+                if (s0 + i < n) {
+                    const cdf v = ld(psi + i * kThreads + t);
+                    pf[2 * (s0 + i)] = to_d(v.re);
+                    pf[2 * (s0 + i) + 1] = to_d(v.im);
+                }
+        }
+        __syncthreads();
+    }
+}
+
+// the FP64 CN tables of a grid split into (hi, lo) float pairs, slot by slot in the same layout
+__global__ void __launch_bounds__(kThreads) build_df_kernel(const mma_tdse_grid* grids)
+{
+    const mma_tdse_grid G = grids[blockIdx.x];
+    const int64_t L = G.m * kThreads, cnt = (int64_t)CN_SLOTS * L;  // complex entries
+    const cd* src = reinterpret_cast<const cd*>(G.cn_tab);
+    float4* dst = reinterpret_cast<float4*>(G.df_tab);
+    for (int64_t q = threadIdx.x; q < cnt; q += blockDim.x) {
+        const cd v = src[q];
+        const df re = from_d(v.re), im = from_d(v.im);
+        dst[q] = make_float4(re.hi, re.lo, im.hi, im.lo);
+    }
+}
+
+}  // namespace dfk
+}  // namespace mma
+
+using namespace mma;
+
+extern "C" int mma_tdse_build_df_tables(const mma_tdse_grid* grids_dev, const mma_tdse_grid* grids_host, int n_grids,
+                                        void* stream)
+{
+    if (n_grids <= 0 || !grids_dev || !grids_host) return MMA_ERR_ARG;
+    for (int g = 0; g < n_grids; g++)
+        if (!grids_host[g].df_tab || !grids_host[g].cn_tab) return MMA_ERR_ARG;
+    dfk::build_df_kernel<<<n_grids, kThreads, 0, (cudaStream_t)stream>>>(grids_dev);
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
+
+// Launch of the float-float form (called by mma_tdse_propagate_ex for precision 2); scratch as
+// for precision 0.
+extern "C" int mma_tdse_propagate_df64_impl(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
+                                            const mma_tdse_buffers* bufs, int max_m, int grid_ctas, bool psi_smem,
+                                            void* stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(bufs->counter, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+    dfk::Args A{insts, n_inst, grids, bufs->fields, bufs->outputs, bufs->psi_final, bufs->snapshots, bufs->counter,
+                reinterpret_cast<float4*>(bufs->scratch), (int64_t)max_m * kThreads};
+    if (psi_smem) {
+        const size_t smem = (size_t)max_m * kThreads * 16;
+        cudaFuncSetAttribute(dfk::propagate_df64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        dfk::propagate_df64_kernel<true><<<grid_ctas, kThreads, smem, st>>>(A);
+    } else {
+        dfk::propagate_df64_kernel<false><<<grid_ctas, kThreads, 0, st>>>(A);
+    }
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}

@@ -510,6 +510,10 @@ extern "C" int mma_tdse_propagate_c64_impl(const mma_tdse_instance* insts, int n
                                            const mma_tdse_buffers* bufs, int m32, int cta_threads, int grid_ctas,
                                            void* stream);
 
+extern "C" int mma_tdse_propagate_df64_impl(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
+                                            const mma_tdse_buffers* bufs, int max_m, int grid_ctas, bool psi_smem,
+                                            void* stream);
+
 extern "C" int mma_tdse_default_ctas(int max_m, int precision)
 {
     const int sms = sm_count();
@@ -549,7 +553,7 @@ extern "C" int mma_tdse_propagate_ex(const mma_tdse_instance* insts, int n_inst,
     if (!insts || !grids || !bufs || !bufs->fields || !bufs->outputs || !bufs->counter || !bufs->scratch ||
         max_m < 1)
         return MMA_ERR_ARG;
-    if (precision != 0 && precision != 1) return MMA_ERR_UNSUPPORTED;
+    if (precision < 0 || precision > 2) return MMA_ERR_UNSUPPORTED;
     if (sm_count() <= 0) return MMA_ERR_NO_DEVICE;
     if (grid_ctas <= 0) grid_ctas = mma_tdse_default_ctas(max_m, precision);
     if (grid_ctas > n_inst) grid_ctas = n_inst;
@@ -559,6 +563,9 @@ extern "C" int mma_tdse_propagate_ex(const mma_tdse_instance* insts, int n_inst,
     }
     if (cta_threads != 0 && cta_threads != kThreads) return MMA_ERR_UNSUPPORTED;
     if (bufs->scratch_bytes < mma_tdse_scratch_bytes(max_m, grid_ctas, precision)) return MMA_ERR_ARG;
+    if (precision == 2)  // float-float form: same layout, scratch and CTA shape as FP64
+        return mma_tdse_propagate_df64_impl(insts, n_inst, grids, bufs, max_m, grid_ctas, psi_fits_smem(max_m),
+                                            stream);
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(bufs->counter, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
     PropArgs A{insts, n_inst, grids, bufs->fields, bufs->outputs, bufs->psi_final, bufs->snapshots, bufs->counter,

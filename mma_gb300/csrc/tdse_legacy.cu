@@ -103,6 +103,7 @@ int alloc_grid(DevGrid& g, int num_r, double dx, double a, double dt, double x_i
     g.h.c64_tab = nullptr;
     g.h.adj_tab = nullptr;
     g.h.c64_threads = 0;
+    g.h.df_tab = nullptr;
     if (cudaMemcpy(g.d, &g.h, sizeof(mma_tdse_grid), cudaMemcpyHostToDevice) != cudaSuccess) return MMA_ERR_CUDA;
     return MMA_OK;
 }

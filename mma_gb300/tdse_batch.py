@@ -28,7 +28,7 @@ THREADS = 256
 CN_SLOTS = 14  # doubles per padded site in the CN tables
 GS_SLOTS = 5
 
-PRECISIONS = {"fp64": 0, "c64": 1}
+PRECISIONS = {"fp64": 0, "c64": 1, "df64": 2}
 C64_SLOTS = 5  # floats per padded site in the complex64 tables
 
 
@@ -37,7 +37,7 @@ class GridRec(Structure):
                 ("x_int", c_double), ("Eguess", c_double), ("CV", c_double), ("max_iter", c_int64),
                 ("x", c_void_p), ("gv", c_void_p), ("psi0", c_void_p), ("cn_tab", c_void_p), ("gs_tab", c_void_p),
                 ("result", c_void_p), ("m32", c_int64), ("c64_tab", c_void_p), ("adj_tab", c_void_p),
-                ("c64_threads", c_int64)]
+                ("c64_threads", c_int64), ("df_tab", c_void_p)]
 
 
 class InstRec(Structure):
@@ -124,9 +124,13 @@ class TDSEGrids:
     ``c64_threads`` (complex64 form only): CTA size the complex64 tables are laid out for --
     None or 256 (every grid), 512 or 1024 (grids that fit that shape, others 256), a list (per
     grid), or "auto" (the autotuner's choice per grid size, mma_gb300.autotune).
+
+    ``df64``: also build the float-float form's tables (the FP64 solve tables split into
+    (hi, lo) float pairs) for ``precision="df64"``.
     """
 
-    def __init__(self, params, dt, device="cuda", stream=None, c64=False, adjoint=False, c64_threads=None):
+    def __init__(self, params, dt, device="cuda", stream=None, c64=False, adjoint=False, c64_threads=None,
+                 df64=False):
         lib = _sig()
         self.device = torch.device(device)
         self.dt = float(dt)
@@ -203,6 +207,13 @@ class TDSEGrids:
                 r.m32 = int(m32)
                 r.c64_threads = int(t)
                 r.c64_tab = self.c64_buf.data_ptr() + 4 * int(o)
+        self.df64 = bool(df64)
+        if self.df64:  # the FP64 solve tables as (hi, lo) float pairs: 28 L floats per grid
+            d_sizes = 2 * CN_SLOTS * THREADS * self.m  # CN_SLOTS doubles per site, each two floats
+            self.df_buf = torch.zeros(int(d_sizes.sum()), dtype=torch.float32, device=self.device)
+            d_off = np.concatenate([[0], np.cumsum(d_sizes)])[:-1]
+            for r, o in zip(recs, d_off):
+                r.df_tab = self.df_buf.data_ptr() + 4 * int(o)
         arr = (GridRec * len(recs))(*recs)
         self.host_recs = arr
         self.dev_recs = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
@@ -215,6 +226,12 @@ class TDSEGrids:
             lib.mma_tdse_build_c64_tables.restype = c_int
             _check(lib.mma_tdse_build_c64_tables(ctypes.c_void_p(self.dev_recs.data_ptr()), ctypes.addressof(arr),
                                                  len(recs), st), "mma_tdse_build_c64_tables")
+            torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
+        if self.df64:
+            lib.mma_tdse_build_df_tables.argtypes = [c_void_p, c_void_p, c_int, c_void_p]
+            lib.mma_tdse_build_df_tables.restype = c_int
+            _check(lib.mma_tdse_build_df_tables(ctypes.c_void_p(self.dev_recs.data_ptr()), ctypes.addressof(arr),
+                                                len(recs), st), "mma_tdse_build_df_tables")
             torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
         res = np.stack([self._view(g, "result").cpu().numpy() for g in range(len(recs))])
         self.Einit = res[:, 0].copy()
@@ -304,6 +321,8 @@ class TDSEBatchPlan:
         self.prec = PRECISIONS[precision]
         if self.prec == 1 and not grids.c64:
             raise ValueError("build the grids with c64=True for the complex64 form")
+        if self.prec == 2 and not getattr(grids, "df64", False):
+            raise ValueError("build the grids with df64=True for the float-float form")
         # raw and refined field buffers, grouped by raw length
         self.len_groups = []
         raw_total = 0
