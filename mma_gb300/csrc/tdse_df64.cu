@@ -83,10 +83,40 @@ __device__ __forceinline__ df dot2_add(df a, df b, df c, df d, df z)
     const float e = ((t1 + t2) + (ep + eq)) + z.lo;
     return renorm(s2, e);
 }
+// a b + c d
+__device__ __forceinline__ df dot2(df a, df b, df c, df d)
+{
+    const float p = a.hi * b.hi, q = c.hi * d.hi;
+    float ep = fmaf(a.hi, b.hi, -p), eq = fmaf(c.hi, d.hi, -q);
+    ep = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, ep));
+    eq = fmaf(c.hi, d.lo, fmaf(c.lo, d.hi, eq));
+    float s1, t1;
+    two_sum(p, q, s1, t1);
+    return renorm(s1, t1 + (ep + eq));
+}
+// a b + z
+__device__ __forceinline__ df mul_add(df a, df b, df z)
+{
+    const float p = a.hi * b.hi;
+    float ep = fmaf(a.hi, b.hi, -p);
+    ep = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, ep));
+    float s1, t1;
+    two_sum(p, z.hi, s1, t1);
+    return renorm(s1, (t1 + ep) + z.lo);
+}
+// 10 p + a + b (the Numerov right-hand side), one renormalisation
+__device__ __forceinline__ df ten_sum(df p, df a, df b)
+{
+    const float x = 10.f * p.hi;
+    const float ex = fmaf(10.f, p.lo, fmaf(10.f, p.hi, -x));
+    float s1, t1, s2, t2;
+    two_sum(a.hi, b.hi, s1, t1);
+    two_sum(x, s1, s2, t2);
+    return renorm(s2, ((t1 + t2) + ex) + (a.lo + b.lo));
+}
 __device__ __forceinline__ cdf cmul(cdf a, cdf b)
 {
-    const df z{0.f, 0.f};
-    return cdf{dot2_add(a.re, b.re, neg(a.im), b.im, z), dot2_add(a.re, b.im, a.im, b.re, z)};
+    return cdf{dot2(a.re, b.re, neg(a.im), b.im), dot2(a.re, b.im, a.im, b.re)};
 }
 // z + a b
 __device__ __forceinline__ cdf cfma(cdf a, cdf b, cdf z)
@@ -100,17 +130,6 @@ __device__ __forceinline__ cdf cfms(cdf a, cdf b, cdf z)
 }
 __device__ __forceinline__ cdf cadd(cdf a, cdf b) { return cdf{add(a.re, b.re), add(a.im, b.im)}; }
 __device__ __forceinline__ cdf csub(cdf a, cdf b) { return cdf{sub(a.re, b.re), sub(a.im, b.im)}; }
-// 10 p + s, with 10 p exact to first order
-__device__ __forceinline__ df ten_plus(df p, df s)
-{
-    const float a = 10.f * p.hi;
-    float e = fmaf(10.f, p.hi, -a);
-    e = fmaf(10.f, p.lo, e);
-    float s1, t1;
-    two_sum(a, s.hi, s1, t1);
-    return renorm(s1, (t1 + e) + s.lo);
-}
-
 __device__ __forceinline__ df from_d(double v)
 {
     const float h = (float)v;
@@ -296,11 +315,12 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_df64_kernel(Args P)
             cdf pm = (t == 0) ? cdf{{0.f, 0.f}, {0.f, 0.f}} : ld(psi + (m - 1) * kThreads + t - 1);
             cdf pc = ld(psi + t);
             cdf yprev{{0.f, 0.f}, {0.f, 0.f}};
-            for (int64_t i = 0; i < m; i++) {
-                const int64_t q = i * kThreads + t;
-                const cdf pn = (i + 1 < m) ? ld(psi + q + kThreads)
+            const int mi = (int)m;  // sites per thread: 32-bit indices in the site loops
+            for (int i = 0; i < mi; i++) {
+                const int q = i * kThreads + t;
+                const cdf pn = (i + 1 < mi) ? ld(psi + q + kThreads)
                                            : ((t + 1 < kThreads) ? ld(psi + t + 1) : cdf{{0.f, 0.f}, {0.f, 0.f}});
-                const cdf r{ten_plus(pc.re, add(pm.re, pn.re)), ten_plus(pc.im, add(pm.im, pn.im))};
+                const cdf r{ten_sum(pc.re, pm.re, pn.re), ten_sum(pc.im, pm.im, pn.im)};
                 yprev = cfms(ld(HH + q), yprev, cmul(ld(IB + q), r));
                 st(yl + q, yprev);
                 pm = pc;
@@ -309,8 +329,8 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_df64_kernel(Args P)
             const cdf yin = scan_fwd(ld(FF + (m - 1) * kThreads + t), yprev, sc, sb);
             // ---- pass 2: forward correction, local backward sweep
             cdf unext{{0.f, 0.f}, {0.f, 0.f}};
-            for (int64_t i = m - 1; i >= 0; i--) {
-                const int64_t q = i * kThreads + t;
+            for (int i = mi - 1; i >= 0; i--) {
+                const int q = i * kThreads + t;
                 const cdf y = cfma(ld(FF + q), yin, ld(yl + q));
                 unext = cfms(ld(GG_ + q), unext, y);
                 st(yl + q, unext);
@@ -323,21 +343,23 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_df64_kernel(Args P)
                 if (t & (1 << b)) ph = cmul(ph, s_pow[2 + b]);
             const cdf z = s_pow[1];
             df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-            double pint = 0.0;
-            for (int64_t i = 0; i < m; i++) {
-                const int64_t q = i * kThreads + t;
+            for (int i = 0; i < mi; i++) {
+                const int q = i * kThreads + t;
                 const cdf u = cfma(ld(GP + q), uin, ld(yl + q));
                 const cdf pn = cmul(ph, csub(u, ld(psi + q)));
                 st(psi + q, pn);
                 ph = cmul(ph, z);
-                const df n2 = dot2_add(pn.re, pn.re, pn.im, pn.im, df{0.f, 0.f});
+                const df n2 = dot2(pn.re, pn.re, pn.im, pn.im);
                 const cdf gx = ld(GVX + q), p0 = ld(P0 + q);
-                acc[0] = dot2_add(n2, gx.re, df{0.f, 0.f}, df{0.f, 0.f}, acc[0]);
-                acc[1] = dot2_add(n2, gx.im, df{0.f, 0.f}, df{0.f, 0.f}, acc[1]);
+                acc[0] = mul_add(n2, gx.re, acc[0]);
+                acc[1] = mul_add(n2, gx.im, acc[1]);
                 acc[2] = dot2_add(pn.re, p0.re, pn.im, p0.im, acc[2]);
                 acc[3] = dot2_add(pn.re, p0.im, neg(pn.im), p0.re, acc[3]);
-                const int64_t j = s0 + i;
-                if (j >= lo && j <= hi) pint += to_d(n2);
+            }
+            double pint = 0.0;  // the few sites of the population window in this chunk, in FP64
+            for (int64_t j = (lo > s0 ? lo : s0); j <= hi && j < s0 + m; j++) {
+                const cdf v = ld(psi + (j - s0) * kThreads + t);
+                pint += to_d(dot2(v.re, v.re, v.im, v.im));
             }
             // warp sums in double-word arithmetic, across warps in FP64
 #pragma unroll
