@@ -260,7 +260,8 @@ int mma_tdse_build_c64_tables(const mma_tdse_grid *grids_dev, const mma_tdse_gri
  *                  factorisation computed in FP64 and the observables summed with
  *                  compensation and finished in FP64; needs c64 tables (n <= 8192);
  *              2 = float-float propagation: the FP64 step and tables carried in double-word
- *                  FP32 arithmetic (about 48 significant bits); needs df tables */
+ *                  FP32 arithmetic (about 48 significant bits); needs df tables; psi lives in
+ *                  the scratch next to the sweep buffer (mma_tdse_scratch_bytes accounts for it) */
 int mma_tdse_propagate(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
                        const mma_tdse_buffers *bufs, int max_m, int grid_ctas, int precision, void *stream);
 

@@ -511,14 +511,16 @@ extern "C" int mma_tdse_propagate_c64_impl(const mma_tdse_instance* insts, int n
                                            void* stream);
 
 extern "C" int mma_tdse_propagate_df64_impl(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
-                                            const mma_tdse_buffers* bufs, int max_m, int grid_ctas, bool psi_smem,
-                                            void* stream);
+                                            const mma_tdse_buffers* bufs, int max_m, int grid_ctas, void* stream);
+extern "C" int mma_tdse_df64_default_ctas();
+extern "C" size_t mma_tdse_df64_scratch_bytes(int max_m, int grid_ctas);
 
 extern "C" int mma_tdse_default_ctas(int max_m, int precision)
 {
     const int sms = sm_count();
     if (sms <= 0 || max_m < 1) return 0;
     if (precision == 1) return sms;  // complex64 form: one register-resident instance per SM
+    if (precision == 2) return mma_tdse_df64_default_ctas();
     int per_sm = 1;
     if (psi_fits_smem(max_m)) {
         size_t smem = (size_t)max_m * kThreads * 16;
@@ -535,6 +537,7 @@ extern "C" size_t mma_tdse_scratch_bytes(int max_m, int grid_ctas, int precision
     if (precision == 1) return 8;  // complex64 form keeps its sweep in registers
     if (grid_ctas <= 0) grid_ctas = mma_tdse_default_ctas(max_m, precision);
     if (grid_ctas <= 0) grid_ctas = 1;
+    if (precision == 2) return mma_tdse_df64_scratch_bytes(max_m, grid_ctas);
     size_t per = (size_t)max_m * kThreads * 16;
     return per * (size_t)grid_ctas * (psi_fits_smem(max_m) ? 1 : 2);
 }
@@ -563,9 +566,8 @@ extern "C" int mma_tdse_propagate_ex(const mma_tdse_instance* insts, int n_inst,
     }
     if (cta_threads != 0 && cta_threads != kThreads) return MMA_ERR_UNSUPPORTED;
     if (bufs->scratch_bytes < mma_tdse_scratch_bytes(max_m, grid_ctas, precision)) return MMA_ERR_ARG;
-    if (precision == 2)  // float-float form: same layout, scratch and CTA shape as FP64
-        return mma_tdse_propagate_df64_impl(insts, n_inst, grids, bufs, max_m, grid_ctas, psi_fits_smem(max_m),
-                                            stream);
+    if (precision == 2)  // float-float form: the FP64 layout, psi in scratch, two CTAs per SM
+        return mma_tdse_propagate_df64_impl(insts, n_inst, grids, bufs, max_m, grid_ctas, stream);
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(bufs->counter, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
     PropArgs A{insts, n_inst, grids, bufs->fields, bufs->outputs, bufs->psi_final, bufs->snapshots, bufs->counter,
