@@ -605,6 +605,7 @@ WORKLOADS = {
     "config3": (64, 32, 10, 2048),  # the far field alone (run_hankel), reported on its own line
     "analysis": (64, 32, 10, 2048),  # photoelectron spectra and Gabor transforms (run_analysis)
     "small": (8, 19, 2, 128),  # profiling case: same grids, fewer instances, shorter pulses
+    "small_df": (16, 19, 2, 128),  # profiling case: 304 instances, two float-float CTAs per SM
     "small_wide": (8, 19, 2, 128),  # profiling case: grids of 9001-12001 sites (run_profile_case)
     "small_adjoint": (8, 19, 2, 128),  # profiling case: the adjoint on 16 short pulses (run_profile_case)
 }

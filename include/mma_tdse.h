@@ -281,6 +281,11 @@ int mma_tdse_build_df_tables(const mma_tdse_grid *grids_dev, const mma_tdse_grid
 /* 1 if the complex64 form has a kernel for CTA size cta_threads (0 = 256) and m32 sites per thread. */
 int mma_tdse_c64_shape_ok(int cta_threads, int m32);
 
+/* No counterpart in the reference.  Persistent CTAs of the complex64 form for tables of that
+ * shape: the SMs times the CTAs of that kernel resident per SM (two for 256 threads with
+ * m32 <= 16, one otherwise); 0 for a shape without a kernel. */
+int mma_tdse_c64_default_ctas(int m32, int cta_threads);
+
 /* Photoelectron spectra on the GPU (window_analysis's algorithm, device pointers): one thread
  * per energy, two FP64 Numerov-tridiagonal solves each.  psi [2(num_r+1)] interleaved, pes
  * [num_E].  Scratch: the energies run in chunks of as many as the scratch holds;

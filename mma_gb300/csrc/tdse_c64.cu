@@ -503,8 +503,8 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
 // is carried from the previous iteration.  Rows beyond n-1 have zero tables, which makes y and u
 // exactly 0 there: the last row's super-diagonal then multiplies u_n = 0 and the first row's
 // sub-diagonal an incoming carry of 0, so the sweeps need no boundary tests.
-template <int M, int T>
-__global__ void __launch_bounds__(T, 1) propagate_c64_smem_kernel(Args P)
+template <int M, int T>  // 256 threads with M <= 16 fit twice on an SM (128 registers, <= 96 KB)
+__global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c64_smem_kernel(Args P)
 {
     constexpr int NW = T / 32;
     extern __shared__ float4 tab4[];  // L sites x (1/beta re, im, V, psi0), then psi [L] complex float
@@ -890,6 +890,25 @@ int launch_c64(const c64::Args& A, int ctas, cudaStream_t st)
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }
 }  // namespace
+
+// CTAs of the complex64 form resident at once for tables laid out for (cta_threads, m32): the
+// occupancy of that kernel shape (two per SM for 256 threads with m32 <= 16: 96 KB of shared
+// memory and 128 registers per thread; one otherwise) times the SMs.
+extern "C" int mma_tdse_c64_default_ctas(int m32, int cta_threads)
+{
+    const int T = cta_threads ? cta_threads : kThreads;
+    int dev = 0, sms = 0, per_sm = 1;
+    if (!c64_shape_ok(T, m32) || cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (T == kThreads && m32 <= 16) {
+        const size_t smem = (size_t)c64::T_SLOTS * T * m32 * sizeof(float) + (size_t)T * m32 * 8;
+        const void* fn = m32 == 8 ? (const void*)c64::propagate_c64_smem_kernel<8, kThreads>
+                                  : (const void*)c64::propagate_c64_smem_kernel<16, kThreads>;
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, T, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
+    }
+    return sms * per_sm;
+}
 
 // Launch of the complex64 form (called by mma_tdse_propagate_ex for precision 1): every
 // instance's grid must have tables of shape (cta_threads, m32).

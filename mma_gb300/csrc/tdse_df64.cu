@@ -98,6 +98,46 @@ __device__ __forceinline__ df dot2(df a, df b, df c, df d)
     two_sum(p, q, s1, t1);
     return renorm(s1, t1 + (ep + eq));
 }
+// a b + c d + z + w, one renormalisation (the four leading terms by three TwoSums, every
+// low-order term folded once)
+__device__ __forceinline__ df dot2_add2(df a, df b, df c, df d, df z, df w)
+{
+    const float p = a.hi * b.hi, q = c.hi * d.hi;
+    float ep = fmaf(a.hi, b.hi, -p), eq = fmaf(c.hi, d.hi, -q);
+    ep = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, ep));
+    eq = fmaf(c.hi, d.lo, fmaf(c.lo, d.hi, eq));
+    float s1, t1, s2, t2, s3, t3;
+    two_sum(p, q, s1, t1);
+    two_sum(z.hi, w.hi, s2, t2);
+    two_sum(s1, s2, s3, t3);
+    return renorm(s3, ((t1 + t2) + t3) + ((ep + eq) + (z.lo + w.lo)));
+}
+// Accumulators of a site loop: hi takes each term's leading part by a TwoSum, lo gathers every
+// low-order part; renormalised once after the loop (lo stays far below ulp(hi) over a chunk).
+// acc += a b
+__device__ __forceinline__ void acc_mul(df& acc, df a, df b)
+{
+    const float p = a.hi * b.hi;
+    float ep = fmaf(a.hi, b.hi, -p);
+    ep = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, ep));
+    float s, e;
+    two_sum(acc.hi, p, s, e);
+    acc.hi = s;
+    acc.lo += e + ep;
+}
+// acc += a b + c d
+__device__ __forceinline__ void acc_dot2(df& acc, df a, df b, df c, df d)
+{
+    const float p = a.hi * b.hi, q = c.hi * d.hi;
+    float ep = fmaf(a.hi, b.hi, -p), eq = fmaf(c.hi, d.hi, -q);
+    ep = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, ep));
+    eq = fmaf(c.hi, d.lo, fmaf(c.lo, d.hi, eq));
+    float s1, t1, s2, t2;
+    two_sum(p, q, s1, t1);
+    two_sum(acc.hi, s1, s2, t2);
+    acc.hi = s2;
+    acc.lo += (t1 + t2) + (ep + eq);
+}
 // a b + z
 __device__ __forceinline__ df mul_add(df a, df b, df z)
 {
@@ -218,6 +258,24 @@ __device__ cdf scan_bwd(cdf c, cdf b, cdf* sc, cdf* sb)
     return lane == 31 ? uw : cfma(cp, uw, bp);
 }
 
+// The step's observables from the per-warp double-word partial sums (lane c < 5 sums column c
+// over the warps), in FP64 from there: sourceterm -<V'> + F, <x>, |<psi0|psi>|^2 and the window
+// population (prop.c:266-300, tools_algorithmic.c:19-43).  Called by one warp.
+__device__ __forceinline__ void observables_out(const df* redf, int lane, int64_t k, double F_prev, double* o_src,
+                                                double* o_x, double* o_ptot, double* o_pint)
+{
+    df s{0.f, 0.f};
+    if (lane < 5)
+#pragma unroll
+        for (int q = 0; q < kWarps; q++) s = add(s, redf[q * 5 + lane]);
+    const double v = to_d(s);
+    const double v3 = __shfl_down_sync(0xffffffffu, v, 1);  // lane 2 gets the imaginary projection
+    if (lane == 0) o_src[k] = -v + F_prev;
+    if (lane == 1) o_x[k] = v;
+    if (lane == 2) o_ptot[k] = v * v + v3 * v3;
+    if (lane == 4) o_pint[k] = v;
+}
+
 struct Args {
     const mma_tdse_instance* insts;
     int n_inst;
@@ -232,6 +290,8 @@ struct Args {
 };
 
 constexpr int kPow = 8;  // e^{i F dt M dx 2^b}, b < 8: the chunk-start phases of 256 threads
+constexpr int kPhase = kPow + 2;  // phase factors per step
+constexpr int kPhaseSteps = kThreads / kPhase;  // steps whose factors one pass of the CTA computes
 // Operand ring: each pass copies the operands of site i + kDepth - 1 into shared memory while it
 // computes site i (kSlots float4 per site at most, pass 3), so the L2 latency of psi, the sweep
 // buffer and the tables is hidden without holding registers.
@@ -242,8 +302,10 @@ __global__ void __launch_bounds__(kThreads, 2) propagate_df64_kernel(Args P)
 {
     extern __shared__ float4 ring[];  // [kDepth][kSlots][kThreads]
     __shared__ cdf sc[2 * kWarps], sb[2 * kWarps];
-    __shared__ double red[kWarps * 5];
-    __shared__ cdf s_pow[kPow + 2];  // e^{i F dt x_0}, e^{i F dt dx}, e^{i F dt M dx 2^b}
+    __shared__ double red[kWarps];
+    __shared__ df redf[kWarps * 5];  // per warp: -<V'>, <x>, <psi0|psi> (re, im), window population
+    // per step of the current block of kPhaseSteps: e^{i F dt x_0}, e^{i F dt dx}, e^{i F dt M dx 2^b}
+    __shared__ cdf s_pow[kPhaseSteps][kPhase];
     __shared__ int64_t s_inst, s_gate, s_lo, s_hi;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     float4* yl = P.scratch + blockIdx.x * P.max_L;
@@ -302,36 +364,31 @@ __global__ void __launch_bounds__(kThreads, 2) propagate_df64_kernel(Args P)
                 o_x[0] = 0.0;
             }
         }
-        double tt = I.tmin;
+        double tt = I.tmin, Fprev = 0.0;
         const double x0 = G.x[0];
         for (int64_t k = 0; k < S; k++) {
             const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : f[k];
-            if (t == 0) {
-                if (k > 0) {  // the previous step's observables
-                    double s[5];
-#pragma unroll
-                    for (int c = 0; c < 5; c++) {
-                        s[c] = 0.0;
-#pragma unroll
-                        for (int q = 0; q < kWarps; q++) s[c] += red[q * 5 + c];
-                    }
-                    o_src[k] = -s[0] + o_e[k];
-                    o_ptot[k] = s[2] * s[2] + s[3] * s[3];
-                    o_x[k] = s[1];
-                    o_pint[k] = s[4];
+            if (w == 0) {
+                if (k > 0) observables_out(redf, lane, k, Fprev, o_src, o_x, o_ptot, o_pint);
+                if (lane == 0) {
+                    tt += dt;
+                    o_t[k + 1] = tt;
+                    o_e[k + 1] = Fk;
                 }
-                tt += dt;
-                o_t[k + 1] = tt;
-                o_e[k + 1] = Fk;
             }
-            // the step's phase factors in FP64, by ten lanes of the last warp: e^{i F dt x_0},
+            Fprev = Fk;
+            // the phase factors of the next kPhaseSteps steps in FP64, one angle per thread, so
+            // that the FP64 pipe's work is spread evenly over the warps: e^{i F dt x_0},
             // e^{i F dt dx} and e^{i F dt m dx 2^b}
-            if (w == kWarps - 1 && lane < kPow + 2) {
-                const double ang = lane == 0 ? Fk * dt * x0 : (lane == 1 ? Fk * dt * dx
-                                                                        : Fk * dt * (double)m * dx * (double)(1 << (lane - 2)));
+            if (k % kPhaseSteps == 0 && t < kPhaseSteps * kPhase) {
+                const int a = t % kPhase;
+                const int64_t ks = k + t / kPhase;
+                const double Fs = (ks <= gate || ks >= I.n_field || ks >= S) ? 0.0 : f[ks];
+                const double ang = a == 0 ? Fs * dt * x0 : (a == 1 ? Fs * dt * dx
+                                                                   : Fs * dt * (double)m * dx * (double)(1 << (a - 2)));
                 double sn, cs;
                 sincos(ang, &sn, &cs);
-                s_pow[lane] = cdf{from_d(cs), from_d(sn)};
+                s_pow[t / kPhase][a] = cdf{from_d(cs), from_d(sn)};
             }
             // ---- pass 1: local forward sweep of the right-hand side 2 M2 psi
             const cdf zero{{0.f, 0.f}, {0.f, 0.f}};
@@ -395,12 +452,13 @@ __global__ void __launch_bounds__(kThreads, 2) propagate_df64_kernel(Args P)
             }
             const cdf uin = scan_bwd(ld(GP + t), unext, sc + kWarps, sb + kWarps);
             // ---- pass 3: backward correction, CN update, phase e^{+i F dt x}, observables
-            cdf ph = s_pow[0];  // e^{i F dt x_0} (e^{i F dt m dx})^t = e^{i F dt x_{s0}}
+            const cdf* pw = s_pow[k % kPhaseSteps];
+            cdf ph = pw[0];  // e^{i F dt x_0} (e^{i F dt m dx})^t = e^{i F dt x_{s0}}
 #pragma unroll
             for (int b = 0; b < kPow; b++)
-                if (t & (1 << b)) ph = cmul(ph, s_pow[2 + b]);
-            const cdf z = s_pow[1];
-            df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+                if (t & (1 << b)) ph = cmul(ph, pw[2 + b]);
+            const cdf z = pw[1];
+            df acc[5] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
             auto issue3 = [&](int i, float4* r) {  // G, u, psi, (-V', x) and psi0 of site i
                 const int q = i * kThreads + t;
                 cp16(r, GP + q);
@@ -422,34 +480,35 @@ __global__ void __launch_bounds__(kThreads, 2) propagate_df64_kernel(Args P)
                 cp_wait<kDepth - 1>();
                 su = su + 1 == kDepth ? 0 : su + 1;
                 const int q = i * kThreads + t;
-                const cdf u = cfma(ld(r), uin, ld(r + kThreads));
-                const cdf pn = cmul(ph, csub(u, ld(r + 2 * kThreads)));
+                const cdf gp = ld(r), yv = ld(r + kThreads), po = ld(r + 2 * kThreads);
+                // u - psi with u = G u_in + y, the CN update before the phase
+                const cdf d{dot2_add2(gp.re, uin.re, neg(gp.im), uin.im, yv.re, neg(po.re)),
+                            dot2_add2(gp.re, uin.im, gp.im, uin.re, yv.im, neg(po.im))};
+                const cdf pn = cmul(ph, d);
                 st(psi + q, pn);
                 ph = cmul(ph, z);
                 const df n2 = dot2(pn.re, pn.re, pn.im, pn.im);
                 const cdf gx = ld(r + 3 * kThreads), p0 = ld(r + 4 * kThreads);
-                acc[0] = mul_add(n2, gx.re, acc[0]);
-                acc[1] = mul_add(n2, gx.im, acc[1]);
-                acc[2] = dot2_add(pn.re, p0.re, pn.im, p0.im, acc[2]);
-                acc[3] = dot2_add(pn.re, p0.im, neg(pn.im), p0.re, acc[3]);
+                acc_mul(acc[0], n2, gx.re);
+                acc_mul(acc[1], n2, gx.im);
+                acc_dot2(acc[2], pn.re, p0.re, pn.im, p0.im);
+                acc_dot2(acc[3], pn.re, p0.im, neg(pn.im), p0.re);
             }
-            double pint = 0.0;  // the few sites of the population window in this chunk, in FP64
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[c] = renorm(acc[c].hi, acc[c].lo);
+            acc[4] = df{0.f, 0.f};  // the few sites of the population window in this chunk
             for (int64_t j = (lo > s0 ? lo : s0); j <= hi && j < s0 + m; j++) {
                 const cdf v = ld(psi + (j - s0) * kThreads + t);
-                pint += to_d(dot2(v.re, v.re, v.im, v.im));
+                acc[4] = add(acc[4], dot2(v.re, v.re, v.im, v.im));
             }
-            // warp sums in double-word arithmetic, across warps in FP64
+            // warp sums in double-word arithmetic; across warps at the next step (observables_out)
 #pragma unroll
-            for (int d = 16; d >= 1; d >>= 1) {
+            for (int d = 16; d >= 1; d >>= 1)
 #pragma unroll
-                for (int c = 0; c < 4; c++) acc[c] = add(acc[c], shfl_xor_df(acc[c], d));
-                pint += __shfl_xor_sync(0xffffffffu, pint, d);
-            }
-            if (lane == 0) {
+                for (int c = 0; c < 5; c++) acc[c] = add(acc[c], shfl_xor_df(acc[c], d));
+            if (lane == 0)
 #pragma unroll
-                for (int c = 0; c < 4; c++) red[w * 5 + c] = to_d(acc[c]);
-                red[w * 5 + 4] = pint;
-            }
+                for (int c = 0; c < 5; c++) redf[w * 5 + c] = acc[c];
             if (I.snap_off >= 0 && P.snapshots) {  // prop.c:248-263
                 int64_t slot = -1;
                 if (k % I.snap_every == 0 && k / I.snap_every < I.n_snap - 1) slot = k / I.snap_every;
@@ -466,19 +525,7 @@ __global__ void __launch_bounds__(kThreads, 2) propagate_df64_kernel(Args P)
             }
             __syncthreads();
         }
-        if (t == 0) {
-            double s[5];
-#pragma unroll
-            for (int c = 0; c < 5; c++) {
-                s[c] = 0.0;
-#pragma unroll
-                for (int q = 0; q < kWarps; q++) s[c] += red[q * 5 + c];
-            }
-            o_src[S] = -s[0] + o_e[S];
-            o_ptot[S] = s[2] * s[2] + s[3] * s[3];
-            o_x[S] = s[1];
-            o_pint[S] = s[4];
-        }
+        if (w == 0) observables_out(redf, lane, S, Fprev, o_src, o_x, o_ptot, o_pint);
         if (P.psi_final && I.psi_off >= 0) {
             double* pf = P.psi_final + I.psi_off;
             for (int64_t i = 0; i < m; i++)

@@ -513,13 +513,17 @@ extern "C" int mma_tdse_propagate_c64_impl(const mma_tdse_instance* insts, int n
 extern "C" int mma_tdse_propagate_df64_impl(const mma_tdse_instance* insts, int n_inst, const mma_tdse_grid* grids,
                                             const mma_tdse_buffers* bufs, int max_m, int grid_ctas, void* stream);
 extern "C" int mma_tdse_df64_default_ctas();
+extern "C" int mma_tdse_c64_default_ctas(int m32, int cta_threads);
 extern "C" size_t mma_tdse_df64_scratch_bytes(int max_m, int grid_ctas);
 
 extern "C" int mma_tdse_default_ctas(int max_m, int precision)
 {
     const int sms = sm_count();
     if (sms <= 0 || max_m < 1) return 0;
-    if (precision == 1) return sms;  // complex64 form: one register-resident instance per SM
+    if (precision == 1) {  // complex64 form with 256-thread tables of m32 = max_m sites per thread
+        const int c = mma_tdse_c64_default_ctas(max_m, 0);
+        return c > 0 ? c : sms;
+    }
     if (precision == 2) return mma_tdse_df64_default_ctas();
     int per_sm = 1;
     if (psi_fits_smem(max_m)) {
@@ -558,7 +562,9 @@ extern "C" int mma_tdse_propagate_ex(const mma_tdse_instance* insts, int n_inst,
         return MMA_ERR_ARG;
     if (precision < 0 || precision > 2) return MMA_ERR_UNSUPPORTED;
     if (sm_count() <= 0) return MMA_ERR_NO_DEVICE;
-    if (grid_ctas <= 0) grid_ctas = mma_tdse_default_ctas(max_m, precision);
+    if (grid_ctas <= 0)
+        grid_ctas = precision == 1 ? mma_tdse_c64_default_ctas(max_m, cta_threads) : mma_tdse_default_ctas(max_m, precision);
+    if (grid_ctas <= 0) return MMA_ERR_TOO_LARGE;  // no complex64 kernel for this shape
     if (grid_ctas > n_inst) grid_ctas = n_inst;
     if (precision == 1) {
         // max_m is the common m32 of the batch's complex64 tables, cta_threads their CTA size

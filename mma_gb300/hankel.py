@@ -413,7 +413,10 @@ def pre_factor_table(zgrid, ogrid, preset_gas="vacuum", pressure=1.0, absorption
 
 # ------------------------------------------------------------------------------ kernels
 def _dev(a, device):
-    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=device)
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if not a.flags.writeable:  # e.g. a view of a read-only archive buffer: torch wants writable memory
+        a = a.copy()
+    return torch.as_tensor(a, device=device)
 
 
 TC_MIN_PLANES = 16  # from this many requested planes the fast form computes them on the tensor cores

@@ -82,6 +82,8 @@ def _sig():
     lib.mma_tdse_scratch_bytes.restype = c_size_t
     lib.mma_tdse_default_ctas.argtypes = [c_int, c_int]
     lib.mma_tdse_default_ctas.restype = c_int
+    lib.mma_tdse_c64_default_ctas.argtypes = [c_int, c_int]
+    lib.mma_tdse_c64_default_ctas.restype = c_int
     lib.mma_tdse_prepare_fields.argtypes = [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p]
     lib.mma_tdse_prepare_fields.restype = c_int
     lib.mma_tdse_spectra.argtypes = [c_void_p, c_int64, c_int, c_int, c_double, c_double, c_void_p, c_int64,
@@ -385,7 +387,8 @@ class TDSEBatchPlan:
             idx = idx[np.argsort(-cost[idx], kind="stable")]
             max_m = int(shape) // 4096 if self.prec == 1 else int(grids.m[np.unique(gid[idx])].max())
             cta_threads = int(shape) % 4096 if self.prec == 1 else 0
-            ctas = grid_ctas or lib.mma_tdse_default_ctas(max_m, self.prec)
+            ctas = grid_ctas or (lib.mma_tdse_c64_default_ctas(max_m, cta_threads) if self.prec == 1
+                                 else lib.mma_tdse_default_ctas(max_m, self.prec))
             ctas = min(ctas, len(idx))
             sb = int(lib.mma_tdse_scratch_bytes(max_m, ctas, self.prec))
             self.launches.append(dict(idx=idx, max_m=max_m, ctas=ctas, cta_threads=cta_threads,
