@@ -12,11 +12,14 @@
 //   * B (the per-plane source tables A_k[w, r], scaled per row to |.| <= 1 and split into FP16
 //     hi + lo) is prepared once by prep_b and read by TMA (64-byte swizzle);
 //   * A (the kernel K_m, scaled per m to |.| <= 1 and split into FP16 hi + lo) is generated in
-//     shared memory by eight CUDA-core warps (J0/J1 seeds, then the recurrence in m);
-//   * one thread issues tcgen05.mma (M = 128, N = 256, K = 16): hi*hi + hi*lo + lo*hi into two
-//     FP32 accumulators in TMEM (two row tiles share each B stage);
+//     shared memory by groups of CUDA-core warps, one half-warp per rho row (J0/J1 seeds, then
+//     the recurrence in m), the groups taking K-blocks round robin;
+//   * one thread issues tcgen05.mma (M = 128, N = 256, K = 16): hi*hi + hi*lo + lo*hi into one of
+//     two FP32 accumulators in TMEM (256 columns each), alternating per tile;
 //   * the epilogue reads TMEM, applies v_k^m / s_m, reduces over m across lanes and writes the
-//     requested planes (complex128, [slot][rho][w]).
+//     requested planes (complex128, [slot][rho][w]).  The generator warps run it in chunks
+//     between the next tile's K-blocks, so one accumulator drains while the tensor cores fill
+//     the other.
 // Every mbarrier wait is bounded (time and a CTA-wide abort flag); a timeout sets a status word
 // and the kernel drains its tensor-core work and frees TMEM before returning.
 #include <cuda.h>
@@ -40,16 +43,15 @@ using namespace mma::tc;
 
 constexpr int KB = 32;       // r per K-block: 32 FP16 = one 64-byte swizzled row
 constexpr int NP = 128;      // planes per tile
-constexpr int NCOL = 2 * NP; // accumulator columns per row tile (re, im per plane)
-constexpr int MT = 2;        // row tiles (accumulators) per CTA tile
-constexpr int STAGES = 3;
-constexpr int GWARPS = 8;    // warps of one generator group (16 half-warps: 16 rho rows per pass)
-constexpr int NGEN = 2 * GWARPS;  // two groups take alternate K-blocks; all of them run the epilogue
+constexpr int NCOL = 2 * NP; // accumulator columns of a tile (re, im per plane)
+constexpr int NACC = 2;      // accumulators in TMEM (2 x 256 columns): tile n+1's MMAs run while tile n drains
+constexpr int STAGES = 4;
+constexpr int NGEN = 16;     // generator warps; they also run the epilogue
 constexpr int THREADS = 32 * (2 + NGEN);
-constexpr uint32_t A_BYTES = 128 * KB * 2;  // one row tile, hi or lo: 8 KB
+constexpr uint32_t A_BYTES = 128 * KB * 2;  // hi or lo: 8 KB
 constexpr uint32_t B_BYTES = NCOL * KB * 2; // hi or lo: 16 KB
-constexpr uint32_t B_OFF = MT * 2 * A_BYTES;
-constexpr uint32_t STAGE_BYTES = B_OFF + 2 * B_BYTES;  // 64 KB
+constexpr uint32_t B_OFF = 2 * A_BYTES;
+constexpr uint32_t STAGE_BYTES = B_OFF + 2 * B_BYTES;  // 48 KB
 constexpr uint64_t WAIT_NS = 2000000000ull;             // 2 s per wait
 
 struct Params {
@@ -102,18 +104,24 @@ template <int MM>
 __global__ void __launch_bounds__(THREADS, 1)
     planes_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo, Params P)
 {
-    constexpr int RT = 128 / MM;  // rho per row tile
-    constexpr int RC = MT * RT;   // rho per CTA tile
-    constexpr int CH = MM > 16 ? MM : 16;  // accumulator columns per epilogue step
-    static_assert(RC % 8 == 0, "rho rows per tile");
+    constexpr int RC = 128 / MM;  // rho rows per tile (the 128 accumulator rows are (rho, m))
+    constexpr int GW = RC / 2;    // warps of one generator group: a half-warp per rho row
+    // groups, taking K-blocks round robin.  At most STAGES: a group's consecutive K-blocks are then
+    // at most STAGES apart, so when it waits for a stage the stage's previous use has been waited
+    // for (the parity wait cannot see a phase two behind); further warps only run the epilogue.
+    constexpr int NG = NGEN / GW < STAGES ? NGEN / GW : STAGES;
+    constexpr int CH = MM > 16 ? MM : 16;  // accumulator columns per reduction
+    constexpr int CW = 32;                  // columns per TMEM load
+    constexpr int EPI = NCOL / 4 / CW;      // epilogue chunks per warp: 4 warps share a lane quadrant
+    static_assert(RC % 2 == 0 && NGEN % GW == 0, "generator groups");
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
     uint64_t* full = bars;
     uint64_t* empty = bars + STAGES;
-    uint64_t* acc_full = bars + 2 * STAGES;
-    uint64_t* acc_empty = acc_full + 1;
-    uint64_t* drain = acc_full + 2;
+    uint64_t* acc_full = bars + 2 * STAGES;       // [NACC]
+    uint64_t* acc_empty = acc_full + NACC;        // [NACC]
+    uint64_t* drain = acc_empty + NACC;
     uint32_t* tmem_s = reinterpret_cast<uint32_t*>(drain + 1);
     volatile int* abort_s = reinterpret_cast<volatile int*>(tmem_s + 1);
 
@@ -121,17 +129,19 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int nkb = (int)(P.rpad / KB);
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
-            mbar_init(&full[s], 1 + GWARPS);  // the producer + the generating group
+            mbar_init(&full[s], 1 + GW);  // the producer + the generating group
             mbar_init(&empty[s], 1);
         }
-        mbar_init(acc_full, 1);
-        mbar_init(acc_empty, NGEN);
+        for (int a = 0; a < NACC; a++) {
+            mbar_init(&acc_full[a], 1);
+            mbar_init(&acc_empty[a], NGEN);
+        }
         mbar_init(drain, 1);
         *abort_s = 0;
         fence_barrier_init();
     }
     if (warp == 1) {
-        tmem_alloc(tmem_s, 512);
+        tmem_alloc(tmem_s, NACC * NCOL);
         tmem_relinquish();
     }
     if (threadIdx.x == 0) {
@@ -177,11 +187,13 @@ __global__ void __launch_bounds__(THREADS, 1)
             bool ok = true;
             const uint32_t sbase = smem_u32(smem);
             for (int64_t tile = blockIdx.x; ok && tile < P.n_tiles; tile += gridDim.x, tt++) {
-                if (!mbar_wait(acc_empty, (tt & 1u) ^ 1u, abort_s, WAIT_NS)) {
+                const uint32_t a = tt % NACC;
+                if (!mbar_wait(&acc_empty[a], ((tt / NACC) & 1u) ^ 1u, abort_s, WAIT_NS)) {
                     fail(abort_s, P.status, 2);
                     break;
                 }
                 tc_fence_after();
+                const uint32_t d = tmem + a * (uint32_t)NCOL;
                 for (int kb = 0; kb < nkb; kb++, it++) {
                     const uint32_t s = it % STAGES, ph = (it / STAGES) & 1u;
                     if (!mbar_wait(&full[s], ph, abort_s, WAIT_NS)) {
@@ -195,19 +207,15 @@ __global__ void __launch_bounds__(THREADS, 1)
                     for (int ks = 0; ks < KB / 16; ks++) {
                         const uint64_t bh = sdesc_sw64(st + B_OFF + ks * 32);
                         const uint64_t bl = sdesc_sw64(st + B_OFF + B_BYTES + ks * 32);
-#pragma unroll
-                        for (int mt = 0; mt < MT; mt++) {
-                            const uint64_t ah = sdesc_sw64(st + mt * 2 * A_BYTES + ks * 32);
-                            const uint64_t al = sdesc_sw64(st + mt * 2 * A_BYTES + A_BYTES + ks * 32);
-                            const uint32_t d = tmem + (uint32_t)(mt * NCOL);
-                            mma_f16(d, ah, bh, idesc, (kb | ks) != 0);
-                            mma_f16(d, ah, bl, idesc, 1u);
-                            mma_f16(d, al, bh, idesc, 1u);
-                        }
+                        const uint64_t ah = sdesc_sw64(st + ks * 32);
+                        const uint64_t al = sdesc_sw64(st + A_BYTES + ks * 32);
+                        mma_f16(d, ah, bh, idesc, (kb | ks) != 0);
+                        mma_f16(d, ah, bl, idesc, 1u);
+                        mma_f16(d, al, bh, idesc, 1u);
                     }
                     mma_commit(&empty[s]);
                 }
-                if (ok) mma_commit(acc_full);
+                if (ok) mma_commit(&acc_full[a]);
             }
             mma_commit(drain);  // all MMAs of this CTA complete before TMEM is freed
             if (!mbar_wait(drain, 0u, abort_s, WAIT_NS)) fail(abort_s, P.status, 4);
@@ -216,26 +224,20 @@ __global__ void __launch_bounds__(THREADS, 1)
     } else {
         // ---------------------------------------------------------------- generators + epilogue
         const int gw = warp - 2;
-        const int grp = gw / GWARPS, gw8 = gw % GWARPS;  // generator group (alternate K-blocks), warp in it
+        const int grp = gw / GW, gwi = gw % GW;        // generator group (K-blocks it = grp mod NG), warp in it
         const int hw = lane >> 4, k0 = 2 * (lane & 15);  // half-warp -> rho row; lane -> r pair (k0, k0+1)
-        constexpr int PASSES = (RC + 2 * GWARPS - 1) / (2 * GWARPS);
-        uint32_t tt = 0;
-        bool ok = true;
+        const int q = 2 * gwi + hw;                      // this half-warp's rho row in the tile
+        const int qd = warp % 4, cb = gw / 4;            // epilogue: TMEM lane quadrant, 64-column block
         const float tw = P.two_over_ymax, iy = P.inv_ymax;
-        // k rho / d_ref of this half-warp's rows (float-float) for a tile
-        auto rows_of = [&](int64_t tile, float (&kh)[PASSES], float (&kl)[PASSES]) {
+        bool ok = true;
+        // k rho / d_ref of this half-warp's row (float-float) for a tile
+        auto row_of = [&](int64_t tile, float& kh, float& kl) {
             const int64_t o = tile / (P.n_pb * P.n_rb), rb = tile % P.n_rb;
-            const double kap = P.og[o] * P.inv_cd;
-#pragma unroll
-            for (int j = 0; j < PASSES; j++) {
-                const int q = gw8 + GWARPS * (2 * j + hw);
-                const int64_t ig = rb * RC + q;
-                split_d((q < RC && ig < P.n_rho) ? kap * P.rho[ig] : 0.0, kh[j], kl[j]);
-            }
+            const int64_t ig = rb * RC + q;
+            split_d(ig < P.n_rho ? P.og[o] * P.inv_cd * P.rho[ig] : 0.0, kh, kl);
         };
         // the A operand of K-block kb (this CTA's K-block number it) into its stage; false on timeout
-        auto gen_block = [&](int kb, uint32_t it, const float (&kh)[PASSES], const float (&kl)[PASSES]) -> bool {
-            if ((int)(it & 1u) != grp) return true;  // the other group generates this K-block
+        auto gen_block = [&](int kb, uint32_t it, float kh, float kl) -> bool {
             const uint32_t s = it % STAGES, ph = (it / STAGES) & 1u;
             // r and r+1 as float-float (hi0, lo0, hi1, lo1), loaded before the wait
             const float4 rv = __ldg(reinterpret_cast<const float4*>(P.rgf) + ((int64_t)kb * KB + k0) / 2);
@@ -243,136 +245,124 @@ __global__ void __launch_bounds__(THREADS, 1)
                 fail(abort_s, P.status, 5);
                 return false;
             }
-            uint8_t* st = smem + s * STAGE_BYTES;
+            uint8_t* ah = smem + s * STAGE_BYTES;
+            uint8_t* al = ah + A_BYTES;
+            const float y0h = kh * rv.x, y0l = fmaf(kh, rv.x, -y0h) + fmaf(kh, rv.y, kl * rv.x);
+            const float y1h = kh * rv.z, y1l = fmaf(kh, rv.z, -y1h) + fmaf(kh, rv.w, kl * rv.z);
+            float J00, J10, J01, J11;
+            bessel01<true>(y0h, y0l, J00, J10);
+            bessel01<true>(y1h, y1l, J01, J11);
+            // K^_m = u^m J_m(y), u = y / y_max <= 1:  K^_{m+1} = (2m / y_max) K^_m - u^2 K^_{m-1}
+            const float u0 = (y0h + y0l) * iy, u1 = (y1h + y1l) * iy;
+            const float w0 = u0 * u0, w1 = u1 * u1;
+            auto put2 = [&](int m, float x0, float x1) {
+                const __half2 h = __floats2half2_rn(x0, x1);
+                const float2 f = __half22float2(h);
+                const __half2 l = __floats2half2_rn(x0 - f.x, x1 - f.y);
+                const uint32_t off = sw64_offset((uint32_t)(q * MM + m), (uint32_t)k0);
+                *reinterpret_cast<__half2*>(ah + off) = h;
+                *reinterpret_cast<__half2*>(al + off) = l;
+            };
+            float a0 = J00, b0 = u0 * J10, a1 = J01, b1 = u1 * J11;
+            put2(0, a0, a1);
+            put2(1, b0, b1);
 #pragma unroll
-            for (int j = 0; j < PASSES; j++) {
-                const int q = gw8 + GWARPS * (2 * j + hw);  // rho row within the CTA tile
-                if (q >= RC) continue;                   // uniform per half-warp
-                const int mt = q / RT, rloc = q % RT;
-                uint8_t* ah = st + mt * 2 * A_BYTES;
-                uint8_t* al = ah + A_BYTES;
-                const float y0h = kh[j] * rv.x, y0l = fmaf(kh[j], rv.x, -y0h) + fmaf(kh[j], rv.y, kl[j] * rv.x);
-                const float y1h = kh[j] * rv.z, y1l = fmaf(kh[j], rv.z, -y1h) + fmaf(kh[j], rv.w, kl[j] * rv.z);
-                float J00, J10, J01, J11;
-                bessel01<true>(y0h, y0l, J00, J10);
-                bessel01<true>(y1h, y1l, J01, J11);
-                // K^_m = u^m J_m(y), u = y / y_max <= 1:  K^_{m+1} = (2m / y_max) K^_m - u^2 K^_{m-1}
-                const float u0 = (y0h + y0l) * iy, u1 = (y1h + y1l) * iy;
-                const float w0 = u0 * u0, w1 = u1 * u1;
-                auto put2 = [&](int m, float x0, float x1) {
-                    const __half2 h = __floats2half2_rn(x0, x1);
-                    const float2 f = __half22float2(h);
-                    const __half2 l = __floats2half2_rn(x0 - f.x, x1 - f.y);
-                    const uint32_t off = sw64_offset((uint32_t)(rloc * MM + m), (uint32_t)k0);
-                    *reinterpret_cast<__half2*>(ah + off) = h;
-                    *reinterpret_cast<__half2*>(al + off) = l;
-                };
-                float a0 = J00, b0 = u0 * J10, a1 = J01, b1 = u1 * J11;
-                put2(0, a0, a1);
-                put2(1, b0, b1);
-#pragma unroll
-                for (int m = 1; m + 1 < MM; m++) {
-                    const float c = (float)m * tw;
-                    const float n0 = fmaf(c, b0, -w0 * a0), n1 = fmaf(c, b1, -w1 * a1);
-                    put2(m + 1, n0, n1);
-                    a0 = b0;
-                    b0 = n0;
-                    a1 = b1;
-                    b1 = n1;
-                }
+            for (int m = 1; m + 1 < MM; m++) {
+                const float c = (float)m * tw;
+                const float n0 = fmaf(c, b0, -w0 * a0), n1 = fmaf(c, b1, -w1 * a1);
+                put2(m + 1, n0, n1);
+                a0 = b0;
+                b0 = n0;
+                a1 = b1;
+                b1 = n1;
             }
             fence_async_smem();
             __syncwarp();
             if (lane == 0) mbar_arrive(&full[s]);
             return true;
         };
-        // Each tile: its remaining K-blocks, then the next tile's first K-blocks (their stages free
-        // up as this tile's last MMAs complete, before its epilogue), then this tile's epilogue --
-        // so the next tile's MMAs start as soon as the accumulators are drained.
-        constexpr int AHEAD = STAGES;
-        float kh[PASSES], kl[PASSES], khn[PASSES], kln[PASSES];
-        if (blockIdx.x < P.n_tiles) rows_of(blockIdx.x, kh, kl);
-        int done_ahead = 0;
-        uint32_t it0 = 0;  // K-block number of this tile's first K-block
-        for (int64_t tile = blockIdx.x; ok && tile < P.n_tiles; tile += gridDim.x, tt++, it0 += (uint32_t)nkb) {
+        // chunk j (32 columns) of this warp's part of the epilogue of the tile in accumulator a:
+        // TMEM -> v_k^m / s_m -> sum over m across lanes -> planes.  Chunk 0 waits for the tile's
+        // MMAs; after the last one the warp releases the accumulator.
+        auto epilogue = [&](int64_t tile, uint32_t tt, int j) -> bool {
+            const uint32_t a = tt % NACC;
             const int64_t o = tile / (P.n_pb * P.n_rb), pb = (tile / P.n_rb) % P.n_pb, rb = tile % P.n_rb;
-            for (int kb = done_ahead; ok && kb < nkb; kb++) ok = gen_block(kb, it0 + kb, kh, kl);
-            if (!ok) break;
-            const int64_t next = tile + gridDim.x;
-            done_ahead = 0;
-            if (next < P.n_tiles) {
-                rows_of(next, khn, kln);
-                const int na = AHEAD < nkb ? AHEAD : nkb;
-                for (int kb = 0; ok && kb < na; kb++) ok = gen_block(kb, it0 + nkb + kb, khn, kln);
-                if (!ok) break;
-                done_ahead = na;
+            if (j == 0) {
+                {   // bring into L1 what this lane's epilogue reads: the per-plane factors of the 32
+                    // planes of its column block and their slot and alpha entries
+                    const int64_t kz0 = pb * NP + cb * (NCOL / 8);
+                    for (int i = lane; i < (NCOL / 8) * MM / 32; i += 32) prefetch_l1(P.ftab + kz0 * MM + 32 * i);
+                    if (lane < 2) prefetch_l1(P.slot + (kz0 + 16 * lane < P.n_z ? kz0 + 16 * lane : P.n_z - 1));
+                    if (lane == 2) prefetch_l1(P.alpha + o * P.zpad + kz0);
+                }
+                if (!mbar_wait(&acc_full[a], (tt / NACC) & 1u, abort_s, WAIT_NS)) {
+                    fail(abort_s, P.status, 6);
+                    return false;
+                }
+                tc_fence_after();
             }
-            // ------------------------------------------------------------ epilogue of this tile
-            {   // while the tile's MMAs run, bring into L1 what this lane's epilogue reads: its row
-                // of per-plane factors and the group's slot and alpha entries (64 planes each), so
-                // that the epilogue's table loads hit L1 instead of waiting on L2 one store at a time
-                const int64_t kz0 = pb * NP + grp * (NP / 2);  // first plane of this group's columns
-                for (int q = lane; q < (NP / 2) * MM / 32; q += 32) prefetch_l1(P.ftab + kz0 * MM + 32 * q);
-                const int64_t ks_ = kz0 + 16 * (lane & 3);  // 64 slot entries: four 128-byte lines
-                prefetch_l1(P.slot + (ks_ < P.n_z ? ks_ : P.n_z - 1));
-                prefetch_l1(P.alpha + o * P.zpad + kz0 + 32 * (lane & 1));  // 64 floats: two lines
-            }
-            if (!mbar_wait(acc_full, tt & 1u, abort_s, WAIT_NS)) {
-                fail(abort_s, P.status, 6);
-                break;
-            }
-            tc_fence_after();
-            // per-plane factors straight from global memory (ftab[plane][m], small and cached; the 16
-            // lanes of one rho row read one contiguous run per plane): no CTA-wide barrier here.
-            // Group grp takes columns [grp * NCOL/2, (grp + 1) * NCOL/2).
-            const int mt = gw8 / 4, qd = warp % 4;
             const int row = qd * 32 + lane;
             const int m = row % MM;
             const float* fm = P.ftab + pb * NP * MM + m;
-            const int64_t ig = rb * RC + mt * RT + row / MM;
-            // 32 columns per TMEM load (one wait), their CH-column groups reduced over the m lanes
-            // independently, so the groups' shuffle chains interleave
-            constexpr int CW = 32;
-            for (int c0 = grp * (NCOL / 2); c0 < (grp + 1) * (NCOL / 2); c0 += CW) {
-                float f[CW / 2];  // factors of the 16 planes of these columns, requested first
+            const int64_t ig = rb * RC + row / MM;
+            const int c0 = cb * (NCOL / 4) + j * CW;
+            float f[CW / 2];  // factors of the 16 planes of these columns, requested first
 #pragma unroll
-                for (int q = 0; q < CW / 2; q++) f[q] = __ldg(fm + ((c0 >> 1) + q) * MM);
-                float v[CW];
-                tmem_ld32(tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(mt * NCOL + c0), v);
+            for (int i = 0; i < CW / 2; i++) f[i] = __ldg(fm + ((c0 >> 1) + i) * MM);
+            float v[CW];
+            tmem_ld32(tmem + ((uint32_t)(qd * 32) << 16) + a * (uint32_t)NCOL + (uint32_t)c0, v);
 #pragma unroll
-                for (int h = 0; h < CW / CH; h++) {
-                    float u[CH];
+            for (int h = 0; h < CW / CH; h++) {
+                float u[CH];
 #pragma unroll
-                    for (int j = 0; j < CH; j++) u[j] = v[h * CH + j] * f[(h * CH + j) >> 1];
-                    reduce_scatter<MM, CH>(u, lane);
+                for (int i = 0; i < CH; i++) u[i] = v[h * CH + i] * f[(h * CH + i) >> 1];
+                reduce_scatter<MM, CH>(u, lane);
 #pragma unroll
-                    for (int j = 0; j < CH / MM; j++) {
-                        const int col = c0 + h * CH + (lane % MM) * (CH / MM) + j;
-                        const int64_t kz = pb * NP + (col >> 1);
-                        if (kz < P.n_z && ig < P.n_rho) {
-                            const int64_t sl = __ldg(P.slot + kz);
-                            if (sl >= 0)
-                                P.planes[((sl * P.n_rho + ig) * P.n_omega + o) * 2 + (col & 1)] =
-                                    (double)(u[j] * __ldg(P.alpha + o * P.zpad + kz));
-                        }
+                for (int i = 0; i < CH / MM; i++) {
+                    const int col = c0 + h * CH + (lane % MM) * (CH / MM) + i;
+                    const int64_t kz = pb * NP + (col >> 1);
+                    if (kz < P.n_z && ig < P.n_rho) {
+                        const int64_t sl = __ldg(P.slot + kz);
+                        if (sl >= 0)
+                            P.planes[((sl * P.n_rho + ig) * P.n_omega + o) * 2 + (col & 1)] =
+                                (double)(u[i] * __ldg(P.alpha + o * P.zpad + kz));
                     }
                 }
             }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(acc_empty);
-#pragma unroll
-            for (int j = 0; j < PASSES; j++) {
-                kh[j] = khn[j];
-                kl[j] = kln[j];
+            if (j == EPI - 1) {
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[a]);
             }
+            return true;
+        };
+        // Per tile: this group's K-blocks of the tile, each followed by one chunk of the previous
+        // tile's epilogue (its accumulator drains while this tile's MMAs run on the other one);
+        // the chunks left over (fewer K-blocks than chunks) and the last tile's epilogue after.
+        uint32_t tt = 0;
+        int64_t prev = -1;
+        for (int64_t tile = blockIdx.x; ok && tile < P.n_tiles; tile += gridDim.x, tt++) {
+            float kh, kl;
+            row_of(tile, kh, kl);
+            const uint32_t it0 = tt * (uint32_t)nkb;
+            int j = 0;
+            // this group's K-blocks: CTA-wide K-block numbers it = grp mod NG (not kb = grp mod NG,
+            // which across a tile boundary would put up to 2 NG - 1 > STAGES blocks between two)
+            const int kb0 = (int)((uint32_t)(grp + NG) - it0 % (uint32_t)NG) % NG;
+            for (int kb = kb0; ok && grp < NG && kb < nkb; kb += NG) {
+                ok = gen_block(kb, it0 + kb, kh, kl);
+                if (ok && prev >= 0 && j < EPI) ok = epilogue(prev, tt - 1, j++);
+            }
+            for (; ok && prev >= 0 && j < EPI; j++) ok = epilogue(prev, tt - 1, j);
+            prev = tile;
         }
+        for (int j = 0; ok && prev >= 0 && j < EPI; j++) ok = epilogue(prev, tt - 1, j);
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, 512);
+        tmem_dealloc(tmem, NACC * NCOL);
     }
 }
 
@@ -749,7 +739,7 @@ extern "C" int mma_hankel_planes_tc_run(const mma_hankel_problem* p, const mma_h
     P.n_rho = p->n_rho;
     P.rpad = L.rpad;
     P.zpad = L.zpad;
-    const int rc = MT * (128 / L.mm);
+    const int rc = 128 / L.mm;  // rho rows per tile
     P.n_pb = L.zpad / NP;
     P.n_rb = (p->n_rho + rc - 1) / rc;
     P.n_tiles = p->n_omega * P.n_pb * P.n_rb;
