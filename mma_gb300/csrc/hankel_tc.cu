@@ -69,6 +69,7 @@ struct Params {
     double* planes;           // [n_planes][n_rho][n_omega] complex128
     int* status;
     const float2* rgf;        // [rpad] r as float-float (0 beyond n_r)
+    const float2* krho;       // [n_omega][n_rho] w rho / (c d_ref) as float-float
     float inv_ymax, two_over_ymax;
 };
 
@@ -230,11 +231,13 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int qd = warp % 4, cb = gw / 4;            // epilogue: TMEM lane quadrant, 64-column block
         const float tw = P.two_over_ymax, iy = P.inv_ymax;
         bool ok = true;
-        // k rho / d_ref of this half-warp's row (float-float) for a tile
+        // k rho / d_ref of this half-warp's row (float-float) for a tile, from the table
         auto row_of = [&](int64_t tile, float& kh, float& kl) {
             const int64_t o = tile / (P.n_pb * P.n_rb), rb = tile % P.n_rb;
             const int64_t ig = rb * RC + q;
-            split_d(ig < P.n_rho ? P.og[o] * P.inv_cd * P.rho[ig] : 0.0, kh, kl);
+            const float2 v = ig < P.n_rho ? __ldg(P.krho + o * P.n_rho + ig) : make_float2(0.f, 0.f);
+            kh = v.x;
+            kl = v.y;
         };
         // the A operand of K-block kb (this CTA's K-block number it) into its stage; false on timeout
         auto gen_block = [&](int kb, uint32_t it, float kh, float kl) -> bool {
@@ -245,8 +248,13 @@ __global__ void __launch_bounds__(THREADS, 1)
                 fail(abort_s, P.status, 5);
                 return false;
             }
-            uint8_t* ah = smem + s * STAGE_BYTES;
-            uint8_t* al = ah + A_BYTES;
+            // store addresses of this lane's pair (row q MM + m, columns k0, k0 + 1) in the SW64 layout:
+            // q MM is a multiple of 8, so the 16-byte chunk is (k0 / 8) ^ ((m >> 1) & 3) and m enters
+            // only through that class and a constant offset
+            uint8_t* const base = smem + s * STAGE_BYTES + (q * MM / 8) * 512 + (k0 & 7) * 2;
+            uint8_t* sa[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) sa[c] = base + ((((k0 >> 3) ^ c) & 3) << 4);
             const float y0h = kh * rv.x, y0l = fmaf(kh, rv.x, -y0h) + fmaf(kh, rv.y, kl * rv.x);
             const float y1h = kh * rv.z, y1l = fmaf(kh, rv.z, -y1h) + fmaf(kh, rv.w, kl * rv.z);
             float J00, J10, J01, J11;
@@ -259,9 +267,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const __half2 h = __floats2half2_rn(x0, x1);
                 const float2 f = __half22float2(h);
                 const __half2 l = __floats2half2_rn(x0 - f.x, x1 - f.y);
-                const uint32_t off = sw64_offset((uint32_t)(q * MM + m), (uint32_t)k0);
-                *reinterpret_cast<__half2*>(ah + off) = h;
-                *reinterpret_cast<__half2*>(al + off) = l;
+                uint8_t* const pa = sa[(m >> 1) & 3] + (m >> 3) * 512 + (m & 7) * 64;
+                *reinterpret_cast<__half2*>(pa) = h;
+                *reinterpret_cast<__half2*>(pa + A_BYTES) = l;
             };
             float a0 = J00, b0 = u0 * J10, a1 = J01, b1 = u1 * J11;
             put2(0, a0, a1);
@@ -364,6 +372,17 @@ __global__ void __launch_bounds__(THREADS, 1)
         tc_fence_after();
         tmem_dealloc(tmem, NACC * NCOL);
     }
+}
+
+// k rho / d_ref per (frequency, screen radius) as float-float, for the A generators
+__global__ void rho_table(const double* og, const double* rho, double inv_cd, int64_t n_omega, int64_t n_rho,
+                          float2* krho)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n_omega * n_rho) return;
+    float h, l;
+    split_d(og[i / n_rho] * inv_cd * rho[i % n_rho], h, l);
+    krho[i] = make_float2(h, l);
 }
 
 // B operand: per (w, plane k) row the plane table A_k[w, r] = pre_k(w) e^{-i k r^2/(2 D_k)} r wr S_k[w, r]
@@ -622,7 +641,7 @@ int tc_terms(int64_t n_terms)
 struct Layout {
     int mm;
     int64_t rpad, zpad;
-    size_t off_bh, off_bl, off_alpha, off_ftab, off_dinv, off_rgf, off_status, total;
+    size_t off_bh, off_bl, off_alpha, off_ftab, off_dinv, off_rgf, off_krho, off_status, total;
 };
 
 size_t up256(size_t x) { return (x + 255) / 256 * 256; }
@@ -641,7 +660,8 @@ bool layout(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, Lay
     L.off_ftab = L.off_alpha + up256(sizeof(float) * p->n_omega * L.zpad);
     L.off_dinv = L.off_ftab + up256(sizeof(float) * L.zpad * L.mm);
     L.off_rgf = L.off_dinv + up256(sizeof(float2) * L.zpad);
-    L.off_status = L.off_rgf + up256(sizeof(float2) * L.rpad);
+    L.off_krho = L.off_rgf + up256(sizeof(float2) * L.rpad);
+    L.off_status = L.off_krho + up256(sizeof(float2) * p->n_omega * p->n_rho);
     L.total = L.off_status + 256;
     return true;
 }
@@ -754,6 +774,13 @@ extern "C" int mma_hankel_planes_tc_run(const mma_hankel_problem* p, const mma_h
     P.planes = planes;
     P.status = status;
     P.rgf = reinterpret_cast<const float2*>(sc + L.off_rgf);
+    P.krho = reinterpret_cast<const float2*>(sc + L.off_krho);
+    {
+        const int64_t nk = p->n_omega * p->n_rho;
+        rho_table<<<(unsigned)((nk + 255) / 256), 256, 0, st>>>(ogrid, rho, P.inv_cd, p->n_omega, p->n_rho,
+                                                                 reinterpret_cast<float2*>(sc + L.off_krho));
+        if (cudaGetLastError() != cudaSuccess) return MMA_ERR_CUDA;
+    }
     P.inv_ymax = plan->y_max > 0.0 ? (float)(1.0 / plan->y_max) : 0.f;
     P.two_over_ymax = plan->y_max > 0.0 ? (float)(2.0 / plan->y_max) : 0.f;
     switch (L.mm) {
