@@ -510,9 +510,15 @@ __global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c6
     extern __shared__ float4 tab4[];  // L sites x (1/beta re, im, V, psi0), then psi [L] complex float
     __shared__ cf sc[2 * NW], sb[2 * NW];
     __shared__ float red_hi[NW * 4], red_lo[NW * 4], red_pi[NW];
-    __shared__ cf wtab[M];
-    __shared__ float s_ahi, s_alo;
-    __shared__ double s_fbuf[3];  // field samples k-1, k, k+1 (slot k mod 3), k+1 copied ahead
+    // Field-derived tables for a block of KB = NW steps, filled at the block's first step with one
+    // step per warp (FP64 products spread over all warps instead of one warp every step):
+    // per-site phase factors e^{i F dt dx i} and F dt as a float pair.
+    constexpr int KB = NW;
+    __shared__ cf s_wtab[KB][M];
+    __shared__ float s_ahi[KB], s_alo[KB];
+    // the observables' float-pair totals of up to KB steps, converted to FP64 once per KB steps
+    // across lanes (one step per lane) instead of by warp 0 every step
+    __shared__ float obs_h[KB][4], obs_l[KB][4], obs_pi[KB];
     __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     constexpr int L = T * M;
@@ -556,7 +562,6 @@ __global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c6
             }
             s_lo = lo < 0 ? 0 : lo;
             s_hi = hi > num_r ? num_r : hi;
-            s_fbuf[0] = I.n_field > 0 ? P.fields[I.field_off] : 0.0;
         }
         const int64_t s0 = (int64_t)t * M;
 #pragma unroll
@@ -595,63 +600,84 @@ __global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c6
             const float t1 = fmaf(c12, v, c_lo2);
             return cf{fmaf(-t1, ii, fmaf(-c_hi2, ii, ir)), fmaf(t1, ir, fmaf(c_hi2, ir, ii))};
         };
+        // observables of output index ko (the state after step ko - 1), warp 0: two-sum of the
+        // warps' partial sums into float pairs, kept in ring slot (ko - 1) mod KB
+        auto obs_reduce = [&](int64_t ko) {
+            const int c = lane >> 3, q = lane & 7;
+            float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
+            for (int qq = q + 8; qq < NW; qq += 8) {  // warps beyond 8: fold into lanes 0..31 first
+                float s2, e2;
+                two_sum(hs, red_hi[qq * 4 + c], s2, e2);
+                hs = s2;
+                ls += red_lo[qq * 4 + c] + e2;
+            }
+#pragma unroll
+            for (int d = 4; d >= 1; d >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
+                const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
+                float s2, e2;
+                two_sum(hs, oh, s2, e2);
+                hs = s2;
+                ls += ol + e2;
+            }
+            const int j = (int)((ko - 1) % KB);
+            if (q == 0) {
+                obs_h[j][c] = hs;
+                obs_l[j][c] = ls;
+            }
+            if (lane == 24) {
+                float pi_sum = 0.f;
+                for (int qq = 0; qq < NW; qq++) pi_sum += red_pi[qq];
+                obs_pi[j] = pi_sum;
+            }
+        };
+        // FP64 outputs of the cnt indices ending at k_last, one per lane: sourceterm -<V'> + F of
+        // the step before, <x>, |<psi0|psi>|^2 and the window population (prop.c:266-300)
+        auto obs_flush = [&](int64_t k_last, int cnt) {
+            __syncwarp();
+            if (lane < cnt) {
+                const int64_t ko = k_last - cnt + 1 + lane, kp = ko - 1;
+                const int j = (int)(kp % KB);
+                double v[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) v[c] = (double)obs_h[j][c] + (double)obs_l[j][c];
+                o_src[ko] = -v[0] + ((kp <= gate || kp >= I.n_field) ? 0.0 : __ldg(f + kp));
+                o_x[ko] = v[1];
+                o_ptot[ko] = fma(v[2], v[2], v[3] * v[3]);
+                o_pint[ko] = (double)obs_pi[j];
+            }
+            __syncwarp();
+        };
         cf yl[M], fg[M];
 
         for (int64_t k = 0; k < S; k++) {
-            if (w == 0 && k > 0) {  // observables of the previous step: two-sum over warps, FP64 finish
-                const int c = lane >> 3, q = lane & 7;
-                float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
-                for (int qq = q + 8; qq < NW; qq += 8) {  // warps beyond 8: fold into lanes 0..31 first
-                    float s2, e2;
-                    two_sum(hs, red_hi[qq * 4 + c], s2, e2);
-                    hs = s2;
-                    ls += red_lo[qq * 4 + c] + e2;
-                }
-#pragma unroll
-                for (int d = 4; d >= 1; d >>= 1) {
-                    const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
-                    const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
-                    float s2, e2;
-                    two_sum(hs, oh, s2, e2);
-                    hs = s2;
-                    ls += ol + e2;
-                }
-                const double v = (double)hs + (double)ls;
-                const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
-                if (lane == 0) {  // o_e[k] = F_{k-1}, still in its shared slot
-                    const int64_t kp = k - 1;
-                    o_src[k] = -v + ((kp <= gate || kp >= I.n_field) ? 0.0 : s_fbuf[kp % 3]);
-                }
-                if (lane == 8) o_x[k] = v;
-                if (lane == 16) o_ptot[k] = fma(pr, pr, pim * pim);
-                if (lane == 24) {
-                    float pi_sum = 0.f;
-                    for (int qq = 0; qq < NW; qq++) pi_sum += red_pi[qq];
-                    o_pint[k] = (double)pi_sum;
-                }
+            if (w == 0 && k > 0) {  // observables of the previous step
+                obs_reduce(k);
+                if ((k - 1) % KB == KB - 1) obs_flush(k, KB);
             }
-            const int fs = (int)(k % 3);
-            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : s_fbuf[fs];
-            if (w == 1 && lane == 0 && k + 1 < I.n_field) cp_async8(&s_fbuf[fs == 2 ? 0 : fs + 1], f + k + 1);
             if (w == 1 && lane == 0) {
                 tt += dt;
                 o_t[k + 1] = tt;
-                o_e[k + 1] = Fk;
+                o_e[k + 1] = (k <= gate || k >= I.n_field) ? 0.0 : __ldg(f + k);
             }
-            if (w == NW - 1) {
-                // per-site phase factors, each from its own angle: a recurrence in i would carry
-                // the FP32 rounding of |e^{i F dt dx}| (1 +- 6e-8) as a bias growing with i, and it
-                // would compound over the steps into a drift of the norm along each chunk
-                for (int i = lane; i < M; i += 32) {
+            if (k % KB == 0) {
+                // per-site phase factors of step k + w, each from its own angle: a recurrence in i
+                // would carry the FP32 rounding of |e^{i F dt dx}| (1 +- 6e-8) as a bias growing
+                // with i, and it would compound over the steps into a drift of the norm along each
+                // chunk.  Read in pass 3, after the scans' barriers; refilled after the end-of-step
+                // barrier of the block's last step.
+                const int64_t ks = k + w;
+                const double Fs = (ks <= gate || ks >= I.n_field || ks >= S) ? 0.0 : __ldg(f + ks);
+                if (lane < M) {
                     float sn, cs;
-                    sincosf((float)(Fk * dt * G.dx) * (float)i, &sn, &cs);
-                    wtab[i] = cf{cs, sn};
+                    sincosf((float)(Fs * dt * G.dx) * (float)lane, &sn, &cs);
+                    s_wtab[w][lane] = cf{cs, sn};
                 }
-                if (lane == 31) {
-                    const double fdt = Fk * dt;
+                if (lane == 0) {
+                    const double fdt = Fs * dt;
                     const float a_hi = (float)fdt;
-                    s_ahi = a_hi;
-                    s_alo = (float)(fdt - (double)a_hi);
+                    s_ahi[w] = a_hi;
+                    s_alo[w] = (float)(fdt - (double)a_hi);
                 }
             }
             // ---- pass 1: right-hand side 2 M2 psi, local forward sweep, forward products F
@@ -693,7 +719,8 @@ __global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c6
             }
             const cf uin = scan_bwd<NW>(fg[0], unext, sc + NW, sb + NW);
             // ---- pass 3: backward correction, CN update, phase, observables
-            const float a_hi = s_ahi, a_lo = s_alo;
+            const int kb = (int)(k % KB);
+            const float a_hi = s_ahi[kb], a_lo = s_alo[kb];
             const float th_hi = a_hi * xs_hi;
             const float th_lo = fmaf(a_hi, xs_hi, -th_hi) + fmaf(a_hi, xs_lo, a_lo * xs_hi);
             const float kk = rintf(th_hi * (float)kInvTwoPi);
@@ -710,7 +737,7 @@ __global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c6
                 const cf u = cfma(fg[i], uin, yl[i]);  // u / 2
                 const cf p0 = psi[q];
                 const cf d{fmaf(2.f, u.re, -p0.re), fmaf(2.f, u.im, -p0.im)};
-                const cf pn = cmul(cmul(phs, wtab[i]), d);
+                const cf pn = cmul(cmul(phs, s_wtab[kb][i]), d);
                 psi[q] = pn;
                 const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
                 const float xj = fmaf(dxf, (float)i, xs_hi);
@@ -770,40 +797,11 @@ __global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c6
                         }
                 }
             }
-            if (w == 1 && lane == 0) cp_async_wait();  // the next step's field sample has landed
             __syncthreads();
         }
-        if (w == 0) {  // observables of the last step
-            const int c = lane >> 3, q = lane & 7;
-            float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
-            for (int qq = q + 8; qq < NW; qq += 8) {
-                float s2, e2;
-                two_sum(hs, red_hi[qq * 4 + c], s2, e2);
-                hs = s2;
-                ls += red_lo[qq * 4 + c] + e2;
-            }
-#pragma unroll
-            for (int d = 4; d >= 1; d >>= 1) {
-                const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
-                const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
-                float s2, e2;
-                two_sum(hs, oh, s2, e2);
-                hs = s2;
-                ls += ol + e2;
-            }
-            const double v = (double)hs + (double)ls;
-            const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
-            if (lane == 0) {
-                const int64_t kp = S - 1;
-                o_src[S] = -v + ((kp <= gate || kp >= I.n_field) ? 0.0 : s_fbuf[kp % 3]);
-            }
-            if (lane == 8) o_x[S] = v;
-            if (lane == 16) o_ptot[S] = fma(pr, pr, pim * pim);
-            if (lane == 24) {
-                float pi_sum = 0.f;
-                for (int qq = 0; qq < NW; qq++) pi_sum += red_pi[qq];
-                o_pint[S] = (double)pi_sum;
-            }
+        if (w == 0 && S > 0) {  // observables of the last step, then the steps not yet converted
+            obs_reduce(S);
+            obs_flush(S, (int)((S - 1) % KB) + 1);
         }
         if (P.psi_final && I.psi_off >= 0) {
             double* pf = P.psi_final + I.psi_off;
