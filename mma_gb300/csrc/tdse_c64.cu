@@ -14,12 +14,14 @@
 //     and -V'_j = -x_j V_j^3 -- nothing per step goes to L2 but the four observables.  Storing
 //     half of 1/beta (a power of two, so no rounding changes) halves y and u throughout the
 //     solve and saves the multiplications by 1/2 in h and g; the update takes 2u - psi;
-//   * the field sample of the next step is copied global -> shared (cp.async) one step ahead,
-//     so no warp waits on a global load before the step's first barrier;
 //   * the phase e^{+i E dt x}: the chunk-start angle is formed and reduced mod 2 pi in
-//     float-float arithmetic, then e^{i E dt dx i} per site from a 32-entry table;
+//     float-float arithmetic, then e^{i E dt dx i} per site from a table;
 //   * the observables summed per thread with Kahan compensation, across the warp with
-//     two-sum pairs, and across warps in FP64 by thread 0.
+//     two-sum pairs, across warps with two-sum pairs by warp 0;
+//   * no serial FP64 on single warps (a 32-lane FP64 instruction holds a sub-partition's FP64
+//     unit for about 64 cycles, and a late warp stalls the others at the next scan barrier):
+//     the field-derived tables are filled for a block of steps by all warps, one step each, and
+//     the observables are converted to FP64 once per block, one step per lane.
 // Reference: 1DTDSE/sources/prop.c:115-347 (step and observables), tridiag.c:26-70 (solve).
 #include <cuda_runtime.h>
 
@@ -106,13 +108,6 @@ __device__ __forceinline__ cf scan_bwd(cf c, cf b, cf* sc, cf* sb)
     return lane == 31 ? uw : cfma(cp, uw, bp);
 }
 
-// 8-byte global -> shared copy that holds no register while in flight; completed by cp_async_wait
-__device__ __forceinline__ void cp_async8(double* dst_smem, const double* src)
-{
-    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst_smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // error-free sum (Knuth two-sum)
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
@@ -154,9 +149,13 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
     __shared__ cf sc[2 * kWarps], sb[2 * kWarps];
     __shared__ float red_hi[kWarps * 4], red_lo[kWarps * 4];
     __shared__ cf bfirst[kWarps], blast[kWarps];
-    __shared__ cf wtab[M];          // e^{i F_k dt dx i}, i < M: phase of site i relative to site 0
-    __shared__ float s_ahi, s_alo;  // F_k dt as a float-float pair (phase angle of pass 5)
-    __shared__ double s_fbuf[3];    // field samples k-1, k, k+1 (slot k mod 3), k+1 copied ahead
+    // field-derived tables for a block of KB = kWarps steps, filled at the block's first step with
+    // one step per warp: e^{i F_k dt dx i} (i < M: phase of site i relative to site 0) and F_k dt
+    // as a float-float pair (phase angle of pass 5)
+    constexpr int KB = kWarps;
+    __shared__ cf s_wtab[KB][M];
+    __shared__ float s_ahi[KB], s_alo[KB];
+    __shared__ float obs_h[KB][4], obs_l[KB][4];  // observables' totals, FP64 once per KB steps
     __shared__ int64_t s_inst, s_gate, s_lo, s_hi, s_grid;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     constexpr int L = kThreads * M;
@@ -202,7 +201,6 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             }
             s_lo = lo < 0 ? 0 : lo;
             s_hi = hi > num_r ? num_r : hi;
-            s_fbuf[0] = I.n_field > 0 ? P.fields[I.field_off] : 0.0;
         }
         // ---- state: psi in registers, initialised from the ground state
         cf psi[M], yy[M];
@@ -257,55 +255,74 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
         const float v_left = (t == 0) ? 0.f : tab4[(M - 1) * kThreads + t - 1].z;   // V left of site 0
         const float v_right = (t == kThreads - 1) ? 0.f : tab4[t + 1].z;            // V right of site M-1
 
-        for (int64_t k = 0; k < S; k++) {
-            // FP64 work of a step is spread over three warps so that no single warp holds the
-            // (1/64-rate) FP64 pipe for long: warp 0 finishes the previous step's observables,
-            // warp 1 lane 0 advances the time grid and the field, the last warp's lanes build
-            // the step's phase constants.
-            if (w == 0 && k > 0) {
-                // lanes 8c+q hold warp q's two-sum pair of observable c; reduce over q
-                const int c = lane >> 3, q = lane & 7;
-                float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
+        // observables of output index ko (the state after step ko - 1), warp 0: lanes 8c+q hold
+        // warp q's two-sum pair of observable c; reduced over q into ring slot (ko - 1) mod KB
+        auto obs_reduce = [&](int64_t ko) {
+            const int c = lane >> 3, q = lane & 7;
+            float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
 #pragma unroll
-                for (int d = 4; d >= 1; d >>= 1) {
-                    const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
-                    const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
-                    float s2, e2;
-                    two_sum(hs, oh, s2, e2);
-                    hs = s2;
-                    ls += ol + e2;
-                }
-                const double v = (double)hs + (double)ls;  // FP64 finish
-                const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
-                if (lane == 0) {  // o_e[k] = F_{k-1}, still in its shared slot
-                    const int64_t kp = k - 1;
-                    o_src[k] = -v + ((kp <= gate || kp >= I.n_field) ? 0.0 : s_fbuf[kp % 3]);
-                }
-                if (lane == 8) o_x[k] = v;
-                if (lane == 16) o_ptot[k] = fma(pr, pr, pim * pim);
+            for (int d = 4; d >= 1; d >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
+                const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
+                float s2, e2;
+                two_sum(hs, oh, s2, e2);
+                hs = s2;
+                ls += ol + e2;
             }
-            const int fs = (int)(k % 3);
-            const double Fk = (k <= gate || k >= I.n_field) ? 0.0 : s_fbuf[fs];
-            if (w == 1 && lane == 0 && k + 1 < I.n_field) cp_async8(&s_fbuf[fs == 2 ? 0 : fs + 1], f + k + 1);
+            if (q == 0) {
+                const int j = (int)((ko - 1) % KB);
+                obs_h[j][c] = hs;
+                obs_l[j][c] = ls;
+            }
+        };
+        // FP64 outputs of the cnt indices ending at k_last, one per lane: sourceterm -<V'> + F of
+        // the step before, <x> and |<psi0|psi>|^2 (prop.c:266-300)
+        auto obs_flush = [&](int64_t k_last, int cnt) {
+            __syncwarp();
+            if (lane < cnt) {
+                const int64_t ko = k_last - cnt + 1 + lane, kp = ko - 1;
+                const int j = (int)(kp % KB);
+                double v[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) v[c] = (double)obs_h[j][c] + (double)obs_l[j][c];
+                o_src[ko] = -v[0] + ((kp <= gate || kp >= I.n_field) ? 0.0 : __ldg(f + kp));
+                o_x[ko] = v[1];
+                o_ptot[ko] = fma(v[2], v[2], v[3] * v[3]);
+            }
+            __syncwarp();
+        };
+        for (int64_t k = 0; k < S; k++) {
+            // FP64 work is kept off single warps (a 32-lane FP64 instruction holds a sub-partition's
+            // FP64 unit for about 64 cycles): warp 0 reduces the previous step's observables in FP32
+            // and converts them once per KB steps, one step per lane; the field tables are filled
+            // once per KB steps by all warps; warp 1 lane 0 advances the time grid.
+            if (w == 0 && k > 0) {
+                obs_reduce(k);
+                if ((k - 1) % KB == KB - 1) obs_flush(k, KB);
+            }
             if (w == 1 && lane == 0) {
                 tt += dt;
                 o_t[k + 1] = tt;
-                o_e[k + 1] = Fk;
+                o_e[k + 1] = (k <= gate || k >= I.n_field) ? 0.0 : __ldg(f + k);
             }
-            if (w == kWarps - 1) {
-                // per-site phase factors, each from its own angle: a recurrence in i would carry
-                // the FP32 rounding of |e^{i F dt dx}| (1 +- 6e-8) as a bias growing with i, and it
-                // would compound over the steps into a drift of the norm along each chunk
+            if (k % KB == 0) {
+                // per-site phase factors of step k + w, each from its own angle: a recurrence in i
+                // would carry the FP32 rounding of |e^{i F dt dx}| (1 +- 6e-8) as a bias growing
+                // with i, and it would compound over the steps into a drift of the norm along each
+                // chunk.  Read in pass 5, after the scans' barriers; refilled after the end-of-step
+                // barrier of the block's last step.
+                const int64_t ks = k + w;
+                const double Fs = (ks <= gate || ks >= I.n_field || ks >= S) ? 0.0 : __ldg(f + ks);
                 for (int i = lane; i < M; i += 32) {
                     float sn, cs;
-                    sincosf((float)(Fk * dt * G.dx) * (float)i, &sn, &cs);
-                    wtab[i] = cf{cs, sn};
+                    sincosf((float)(Fs * dt * G.dx) * (float)i, &sn, &cs);
+                    s_wtab[w][i] = cf{cs, sn};
                 }
-                if (lane == 31) {
-                    const double fdt = Fk * dt;
+                if (lane == 0) {
+                    const double fdt = Fs * dt;
                     const float a_hi = (float)fdt;
-                    s_ahi = a_hi;
-                    s_alo = (float)(fdt - (double)a_hi);
+                    s_ahi[w] = a_hi;
+                    s_alo[w] = (float)(fdt - (double)a_hi);
                 }
             }
             // right-hand side 2 M2 psi at site i (neighbours across threads by shuffle/shared)
@@ -362,7 +379,8 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             }
             // ---- pass 5: CN update, phase, observables
             // chunk-start angle F dt x_s in float-float, reduced mod 2 pi
-            const float a_hi = s_ahi, a_lo = s_alo;
+            const int kb = (int)(k % KB);
+            const float a_hi = s_ahi[kb], a_lo = s_alo[kb];
             float th_hi = a_hi * xs_hi;
             float th_lo = fmaf(a_hi, xs_hi, -th_hi) + fmaf(a_hi, xs_lo, a_lo * xs_hi);
             const float kk = rintf(th_hi * (float)kInvTwoPi);
@@ -381,7 +399,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             for (int i = 0; i < M; i++) {
                 const float4 tb = tab4[i * kThreads + t];
                 const cf d{fmaf(2.f, yy[i].re, -psi[i].re), fmaf(2.f, yy[i].im, -psi[i].im)};  // u = 2 yy
-                const cf pn = cmul(cmul(phs, wtab[i]), d);
+                const cf pn = cmul(cmul(phs, s_wtab[kb][i]), d);
                 psi[i] = pn;
                 const float n2 = fmaf(pn.re, pn.re, pn.im * pn.im);
                 const float xj = fmaf(dxf, (float)i, xs_hi);
@@ -447,7 +465,6 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
                         }
                 }
             }
-            if (w == 1 && lane == 0) cp_async_wait();  // the next step's field sample has landed
             __syncthreads();
             if (w == 2 && lane == 0) {
                 float pi_sum = 0.f;
@@ -455,26 +472,9 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
                 o_pint[k + 1] = (double)pi_sum;
             }
         }
-        if (w == 0) {  // observables of the last step, as at the top of the step loop
-            const int c = lane >> 3, q = lane & 7;
-            float hs = red_hi[q * 4 + c], ls = red_lo[q * 4 + c];
-#pragma unroll
-            for (int d = 4; d >= 1; d >>= 1) {
-                const float oh = __shfl_xor_sync(0xffffffffu, hs, d);
-                const float ol = __shfl_xor_sync(0xffffffffu, ls, d);
-                float s2, e2;
-                two_sum(hs, oh, s2, e2);
-                hs = s2;
-                ls += ol + e2;
-            }
-            const double v = (double)hs + (double)ls;
-            const double pr = __shfl_sync(0xffffffffu, v, 16), pim = __shfl_sync(0xffffffffu, v, 24);
-            if (lane == 0) {
-                const int64_t kp = S - 1;
-                o_src[S] = -v + ((kp <= gate || kp >= I.n_field) ? 0.0 : s_fbuf[kp % 3]);
-            }
-            if (lane == 8) o_x[S] = v;
-            if (lane == 16) o_ptot[S] = fma(pr, pr, pim * pim);
+        if (w == 0 && S > 0) {  // observables of the last step, then the steps not yet converted
+            obs_reduce(S);
+            obs_flush(S, (int)((S - 1) % KB) + 1);
         }
         if (P.psi_final && I.psi_off >= 0) {
             double* pf = P.psi_final + I.psi_off;
