@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(kThreads) fast_stage1(mma_hankel_problem P, co
                 const float th = kr2h * ih;
                 const float te = fmaf(kr2h, ih, -th) + fmaf(kr2h, il, kr2l * ih);
                 float sn, cs;
-                sincosf(reduce_2pi(th, te), &sn, &cs);  // e^{-i theta} = (cs, -sn)
+                sincos_reduced(reduce_2pi(th, te), sn, cs);  // e^{-i theta} = (cs, -sn)
                 a = make_float2(fmaf(a.x, cs, a.y * sn), fmaf(a.y, cs, -a.x * sn));
             }
             a.x *= wr;

@@ -52,7 +52,8 @@ __device__ __forceinline__ float reduce_2pi(float yh, float yl)
     return r + yl;
 }
 
-// sin and cos of x for |x| <= 5 (the reduced phases below): x = k pi/2 + r by Cody and Waite's
+// sin and cos of x for |x| <= 5 (phases already reduced mod 2 pi by reduce_2pi, and the Bessel
+// phases below): x = k pi/2 + r by Cody and Waite's
 // two-part additive reduction (pi/2 = 1.5703125 + 4.83826794896619e-4, the first part exact
 // times k), |r| <= pi/4, then the Taylor polynomials of sin (to r^9) and cos (to r^8), whose
 // remainders stay below 3e-8 there; the quadrant is k mod 4.  Max |error| 9e-8 on [-4.2, 3.6]

@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
                     const float th = kr2h[i] * di.x;
                     const float te = fmaf(kr2h[i], di.x, -th) + fmaf(kr2h[i], di.y, kr2l[i] * di.x);
                     float sn, cs;
-                    sincosf(reduce_2pi(th, te), &sn, &cs);  // e^{-i theta}
+                    sincos_reduced(reduce_2pi(th, te), sn, cs);  // e^{-i theta}
                     v = make_float2(fmaf(v.x, cs, v.y * sn), fmaf(v.y, cs, -v.x * sn));
                 }
                 a[u][i] = make_float2(v.x * wr[i], v.y * wr[i]);  // zero beyond n_r (wr = 0, source 0)
