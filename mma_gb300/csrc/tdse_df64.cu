@@ -87,6 +87,21 @@ __device__ __forceinline__ df dot2_add(df a, df b, df c, df d, df z)
     const float e = ((t1 + t2) + (ep + eq)) + z.lo;
     return renorm(s2, e);
 }
+// Results consumed only as operands of the next double-word product or sum (never stored, never
+// carried from site to site) skip the final renormalisation: their (hi, lo) come straight from
+// the error-free transformations, |lo| at most a few ulp(hi), which the products below take
+// exactly to first order like any pair.
+// a b + c d, unnormalised
+__device__ __forceinline__ df dot2_u(df a, df b, df c, df d)
+{
+    const float p = a.hi * b.hi, q = c.hi * d.hi;
+    float ep = fmaf(a.hi, b.hi, -p), eq = fmaf(c.hi, d.hi, -q);
+    ep = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, ep));
+    eq = fmaf(c.hi, d.lo, fmaf(c.lo, d.hi, eq));
+    float s1, t1;
+    two_sum(p, q, s1, t1);
+    return df{s1, t1 + (ep + eq)};
+}
 // a b + c d
 __device__ __forceinline__ df dot2(df a, df b, df c, df d)
 {
@@ -110,7 +125,7 @@ __device__ __forceinline__ df dot2_add2(df a, df b, df c, df d, df z, df w)
     two_sum(p, q, s1, t1);
     two_sum(z.hi, w.hi, s2, t2);
     two_sum(s1, s2, s3, t3);
-    return renorm(s3, ((t1 + t2) + t3) + ((ep + eq) + (z.lo + w.lo)));
+    return df{s3, ((t1 + t2) + t3) + ((ep + eq) + (z.lo + w.lo))};  // unnormalised (feeds cmul)
 }
 // Accumulators of a site loop: hi takes each term's leading part by a TwoSum, lo gathers every
 // low-order part; renormalised once after the loop (lo stays far below ulp(hi) over a chunk).
@@ -156,11 +171,15 @@ __device__ __forceinline__ df ten_sum(df p, df a, df b)
     float s1, t1, s2, t2;
     two_sum(a.hi, b.hi, s1, t1);
     two_sum(x, s1, s2, t2);
-    return renorm(s2, ((t1 + t2) + ex) + (a.lo + b.lo));
+    return df{s2, ((t1 + t2) + ex) + (a.lo + b.lo)};  // unnormalised (feeds cmul)
 }
 __device__ __forceinline__ cdf cmul(cdf a, cdf b)
 {
     return cdf{dot2(a.re, b.re, neg(a.im), b.im), dot2(a.re, b.im, a.im, b.re)};
+}
+__device__ __forceinline__ cdf cmul_u(cdf a, cdf b)  // unnormalised (feeds a sum)
+{
+    return cdf{dot2_u(a.re, b.re, neg(a.im), b.im), dot2_u(a.re, b.im, a.im, b.re)};
 }
 // z + a b
 __device__ __forceinline__ cdf cfma(cdf a, cdf b, cdf z)
@@ -419,7 +438,7 @@ __global__ void __launch_bounds__(kThreads, 2) propagate_df64_kernel(Args P)
                 cp_wait<kDepth - 1>();
                 const cdf pn = (i + 1 < mi || t + 1 < kThreads) ? ld(r) : zero;
                 const cdf r2{ten_sum(pc.re, pm.re, pn.re), ten_sum(pc.im, pm.im, pn.im)};
-                yprev = cfms(ld(r + kThreads), yprev, cmul(ld(r + 2 * kThreads), r2));
+                yprev = cfms(ld(r + kThreads), yprev, cmul_u(ld(r + 2 * kThreads), r2));
                 st(yl + i * kThreads + t, yprev);
                 pm = pc;
                 pc = pn;
@@ -487,7 +506,7 @@ __global__ void __launch_bounds__(kThreads, 2) propagate_df64_kernel(Args P)
                 const cdf pn = cmul(ph, d);
                 st(psi + q, pn);
                 ph = cmul(ph, z);
-                const df n2 = dot2(pn.re, pn.re, pn.im, pn.im);
+                const df n2 = dot2_u(pn.re, pn.re, pn.im, pn.im);
                 const cdf gx = ld(r + 3 * kThreads), p0 = ld(r + 4 * kThreads);
                 acc_mul(acc[0], n2, gx.re);
                 acc_mul(acc[1], n2, gx.im);
