@@ -101,3 +101,17 @@ def test_autotuner_picks_and_caches(gpu_lib, tmp_path, monkeypatch):
     assert autotune.choose_c64_threads(4001, 0.25, p) == t  # from the file, no timing
     g = TDSEGrids([p], dt=0.25, c64=True, c64_threads="auto")
     assert int(g.c64_threads[0]) == t
+
+
+def test_c64_default_ctas_follow_occupancy(gpu_lib):
+    """Persistent grid of the complex64 form per table shape: two CTAs per SM where the 256-thread
+    kernel fits twice (at most 16 sites per thread), one otherwise, none for a shape without a
+    kernel."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert gpu_lib.mma_tdse_c64_default_ctas(16, 256) == 2 * sms
+    assert gpu_lib.mma_tdse_c64_default_ctas(8, 0) == 2 * sms
+    assert gpu_lib.mma_tdse_c64_default_ctas(32, 256) == sms
+    assert gpu_lib.mma_tdse_c64_default_ctas(16, 512) == sms
+    assert gpu_lib.mma_tdse_c64_default_ctas(12, 256) == 0
