@@ -398,8 +398,16 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
                                                        int64_t zpad)
 {
     __shared__ float wmax[2][4][PREP_THREADS / 32];
+    extern __shared__ float2 pre_s[];  // [zpad]: this frequency's pre-factor per plane, as floats
     const int64_t o = blockIdx.x, Nr = P.n_r, No = P.n_omega;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    // converted once per CTA: a double -> float conversion runs on the FP64 unit (a 32-lane
+    // instruction holds a sub-partition's unit for about 64 cycles), so not per thread and plane
+    for (int64_t kz = t; kz < zpad; kz += PREP_THREADS) {
+        const double2 pf = (kz < P.n_z && pre && !P.pre_radial) ? pre[kz * No + o] : make_double2(1.0, 0.0);
+        pre_s[kz] = make_float2((float)pf.x, (float)pf.y);
+    }
+    __syncthreads();
     float kh, kl;
     split_d(og[o] / kC, kh, kl);
     float kr2h[2 * PREP_PAIRS], kr2l[2 * PREP_PAIRS], wr[2 * PREP_PAIRS];
@@ -436,8 +444,7 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
         for (int u = 0; u < PB; u++) {
             const int64_t kz = kz0 + u;
             const bool live = kz < P.n_z;
-            const double2 pf = (live && pre && !P.pre_radial) ? pre[kz * No + o] : make_double2(1.0, 0.0);
-            const float2 pr0 = make_float2((float)pf.x, (float)pf.y);
+            const float2 pr0 = pre_s[kz];
             const float2 di = live ? dinv[kz] : make_float2(0.f, 0.f);
             mx[u] = 0.f;
 #pragma unroll
@@ -653,6 +660,7 @@ bool layout(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, Lay
     L.rpad = (p->n_r + KB - 1) / KB * KB;
     L.zpad = (p->n_z + NP - 1) / NP * NP;
     if (L.rpad > 2 * 2 * PREP_THREADS) return false;
+    if (sizeof(float2) * (size_t)L.zpad > 200 * 1024) return false;  // prep_b's per-plane table
     const size_t nb = (size_t)p->n_omega * 2 * L.zpad * L.rpad * sizeof(__half);
     L.off_bh = 0;
     L.off_bl = up256(nb);
@@ -727,7 +735,11 @@ extern "C" int mma_hankel_planes_tc_prepare(const mma_hankel_problem* p, const m
                                                                reinterpret_cast<float2*>(sc + L.off_dinv),
                                                                reinterpret_cast<float*>(sc + L.off_ftab),
                                                                reinterpret_cast<float2*>(sc + L.off_rgf));
-    prep_b<<<(unsigned)p->n_omega, PREP_THREADS, 0, st>>>(
+    const size_t sp = sizeof(float2) * (size_t)L.zpad;
+    if (sp > 48 * 1024 &&
+        cudaFuncSetAttribute(prep_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp) != cudaSuccess)
+        return MMA_ERR_CUDA;
+    prep_b<<<(unsigned)p->n_omega, PREP_THREADS, sp, st>>>(
         *p, ogrid, rgrid, reinterpret_cast<const float2*>(sc + L.off_dinv), source,
         reinterpret_cast<const double2*>(pre), reinterpret_cast<__half*>(sc + L.off_bh),
         reinterpret_cast<__half*>(sc + L.off_bl), reinterpret_cast<float*>(sc + L.off_alpha), L.rpad, L.zpad);
