@@ -76,3 +76,45 @@ def test_single_energy_and_single_window(gpu_lib):
     refg = oa.gabor(sig, 0.3, len(t), len(om), 1, 0.0, 100.0, 5.0)
     Gh = G.cpu().numpy()[0]
     assert Gh.shape == refg.shape and np.abs(Gh - refg).max() <= 1e-9 * np.abs(refg).max()
+
+
+def test_df64_one_site_per_thread(gpu_lib, oracle_built):
+    """The float-float form on a 65-site grid: one site per thread, so each pass's operand ring
+    holds a single site (the prologue copies one, the rest of the ring stays empty)."""
+    import oracle.tdse as ot
+    from mma_gb300.tdse_batch import TDSEGrids, run_batch
+
+    num_r, dx = 64, 0.4
+    t = 0.25 * np.arange(1, 41)
+    E = 0.05 * np.sin(np.pi * t / (t[-1] + 0.25)) ** 2 * np.cos(0.3 * t)
+    grids = TDSEGrids([dict(num_r=num_r, dx=dx, trg_a=A_CONFIG)], dt=0.25, df64=True)
+    res = run_batch(grids, torch.tensor(E[None, :], device="cuda"), dt_field=0.25, tmax=t[-1] - t[0],
+                    precision="df64")
+    torch.cuda.synchronize()
+    x, psi0, e, _ = ot.ground_state(num_r, dx, A_CONFIG, -1.0, 1e-15)
+    o = ot.propagate(x, psi0, t, E, dx, A_CONFIG)
+    for k in ("sourceterm", "PopTot", "PopInt", "expval"):
+        assert rel_l2(res[k][0].cpu().numpy(), o[k]) < 1e-9, k
+
+
+def test_tensor_core_planes_one_k_block(gpu_lib):
+    """Every plane on the tensor cores with 20 radii: one K-block per tile, so most generator
+    groups have no K-block in a tile and only run their share of the epilogue."""
+    from mma_gb300 import hankel as H
+
+    omega0 = 0.057 / 2.4188843265857e-17
+    rg = np.linspace(0.0, 100e-6, 20)
+    zg = np.linspace(-5e-3, 5e-3, 24)
+    og = np.linspace(10 * omega0, 42 * omega0, 12)
+    rho = np.linspace(0.0, 4e-3, 30)
+    rng = np.random.default_rng(1)
+    S = np.exp(-(rg / 40e-6) ** 2)[None, None, :] * np.exp(1j * rng.uniform(0, 2 * np.pi, (len(zg), len(og))))[:, :, None]
+    S = torch.tensor(S, dtype=torch.complex64, device="cuda")
+    planes = list(range(len(zg)))
+    _, p64, _ = H.far_field(og, rg, zg, rho, S, 1.0, None, True, planes=planes, form="plain")
+    _, ptc, plan = H.far_field(og, rg, zg, rho, S, 1.0, None, True, planes=planes, form="fast", planes_via="tc")
+    assert plan["planes_via"] == "tc"
+    for k in planes:
+        a, b = ptc[k].cpu().numpy(), p64[k].cpu().numpy()
+        err = (np.linalg.norm(a - b, axis=0) / np.linalg.norm(b, axis=0)).max()
+        assert err < 2e-5, (k, err)
