@@ -34,11 +34,17 @@ def _sig():
     return lib
 
 
+def _on_device(t):
+    """The tensor on the current CUDA device (a host tensor is copied): the kernels take device
+    pointers only, so a host pointer never reaches them."""
+    return t if t.is_cuda else t.to(torch.device("cuda", torch.cuda.current_device()))
+
+
 def pes(psi, num_r, dx, trg_a, E_start=-0.6, num_E=10000, epsilon=5e-4, Estep=5e-4, chunk=16384, stream=None):
-    """Photoelectron spectrum of one wavefunction (complex cuda tensor of num_r + 1 values):
+    """Photoelectron spectrum of one wavefunction (complex tensor of num_r + 1 values; a host tensor is copied to the GPU):
     returns (E grid numpy, PES float64 cuda tensor [num_E]).  Energies run `chunk` at a time."""
     lib = _sig()
-    p = psi.to(torch.complex128).contiguous()
+    p = _on_device(psi).to(torch.complex128).contiguous()
     if p.numel() != num_r + 1:
         raise ValueError("psi must have num_r + 1 values")
     out = torch.empty(int(num_E), dtype=torch.float64, device=p.device)
@@ -55,7 +61,7 @@ def gabor(signals, dt, omega_max, t_min, t_max, N_G, a=8.0, stream=None):
     returns (t grid [N_G], omegas [N_freq], |G| cuda tensor [n_sig, N_G, N_freq]), with the
     frequency selection of PythonTDSE.gabor_transform (2 pi fftfreq(N, dt) <= omega_max)."""
     lib = _sig()
-    s = signals.to(torch.float64)
+    s = _on_device(signals).to(torch.float64)
     if s.dim() == 1:
         s = s[None]
     s = s.contiguous()

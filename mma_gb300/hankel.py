@@ -424,13 +424,16 @@ TC_MIN_PLANES = 16  # from this many requested planes the fast form computes the
 
 def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_field=True, planes=(), form="plain",
               tol=1e-9, stream=None, planes_via="auto", _events=None):
-    """Run the far-field kernels.  source: torch complex tensor [Nz, No, Nr] on the GPU.
+    """Run the far-field kernels.  source: torch complex tensor [Nz, No, Nr] (on the GPU; a host
+    tensor is copied there first).
     Returns (FF [Nrho, No] complex128 tensor, {plane: [Nrho, No] tensor}, fast plan dict or None).
 
     With form="fast", requested planes are computed either directly (one FP32 J0 per term,
     planes_via="direct") or by the tensor-core split-precision GEMM (planes_via="tc");
     "auto" takes the tensor cores from TC_MIN_PLANES planes on, where the problem fits them."""
     lib = _sig()
+    if not source.is_cuda:  # the kernels take device pointers only: a host source is copied first
+        source = source.to(torch.device("cuda", torch.cuda.current_device()))
     dev = source.device
     Nz, No, Nr = source.shape
     if len(zgrid) != Nz or len(ogrid) != No or len(rgrid) != Nr:

@@ -118,3 +118,28 @@ def test_tensor_core_planes_one_k_block(gpu_lib):
         a, b = ptc[k].cpu().numpy(), p64[k].cpu().numpy()
         err = (np.linalg.norm(a - b, axis=0) / np.linalg.norm(b, axis=0)).max()
         assert err < 2e-5, (k, err)
+
+
+def test_host_tensors_are_moved_to_the_gpu(gpu_lib):
+    """Host tensors passed to the tensor-level entry points are copied to the GPU (the kernels take
+    device pointers only) and give the same results as device tensors."""
+    from mma_gb300 import analysis
+    from mma_gb300 import hankel as H
+
+    num_r, dx, a = 200, 0.4, 1.0
+    x = np.arange(num_r + 1) * dx - 0.5 * num_r * dx
+    psi = torch.tensor(np.exp(-((x - 3) / 5) ** 2) * np.exp(0.3j * x))
+    _, Pd = analysis.pes(psi.cuda(), num_r, dx, a, E_start=0.05, num_E=64, epsilon=4e-3, Estep=3e-3)
+    _, Ph = analysis.pes(psi, num_r, dx, a, E_start=0.05, num_E=64, epsilon=4e-3, Estep=3e-3)
+    assert Ph.is_cuda and torch.equal(Ph, Pd)
+    sig = torch.tensor(np.cos(0.2 * 0.3 * np.arange(300))[None, :])
+    Gd = analysis.gabor(sig.cuda(), 0.3, 1.0, 0.0, 80.0, 4)[2]
+    Gh = analysis.gabor(sig, 0.3, 1.0, 0.0, 80.0, 4)[2]
+    assert Gh.is_cuda and torch.equal(Gh, Gd)
+    omega0 = 0.057 / 2.4188843265857e-17
+    rg, zg = np.linspace(0.0, 60e-6, 16), np.linspace(-1e-3, 1e-3, 5)
+    og, rho = np.array([15 * omega0, 21 * omega0]), np.linspace(0.0, 2e-3, 8)
+    S = torch.tensor(np.exp(-(rg / 30e-6) ** 2)[None, None, :] * np.ones((len(zg), len(og), 1)), dtype=torch.complex64)
+    ffd = H.far_field(og, rg, zg, rho, S.cuda(), 1.0, None, True, form="fast")[0]
+    ffh = H.far_field(og, rg, zg, rho, S, 1.0, None, True, form="fast")[0]
+    assert ffh.is_cuda and torch.equal(ffh, ffd)
