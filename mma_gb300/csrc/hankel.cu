@@ -217,6 +217,9 @@ __global__ void __launch_bounds__(kThreads) fast_stage2(mma_hankel_problem P, mm
         }
         __syncthreads();
         if (j < Nrho) {
+            // two radii per iteration: their seed and m-recurrence chains are independent, so the
+            // scheduler can interleave them (the loop is otherwise bound by dependent FMA latency)
+#pragma unroll 2
             for (int64_t q = 0; q < nt; q++) {
                 const float2 kk = kr[q];
                 const float yh = kk.x * rh;
