@@ -20,6 +20,10 @@
 // dependency chains and 16 warps hide them better than 8 (measured 27% faster on config 1).
 // Each pass reads its operands through a small cp.async ring in shared memory, two sites ahead,
 // which hides the L2 latency without registers (30% faster at one CTA per SM, 9% at two).
+// No warp carries serial FP64 work into the scan barriers (a 32-lane FP64 instruction holds a
+// sub-partition's FP64 unit for about 64 cycles): the phase factors come from one FP64 sincos
+// per thread for 25 steps at a time, and the observables' warp sums stay double-word until
+// lanes of warp 0 convert them.
 #include <cuda_runtime.h>
 
 #include "../../include/mma_tdse.h"
