@@ -86,7 +86,7 @@ __device__ __forceinline__ void sincos_small(float p, float& s, float& c)
 // with the phase argument x reduced mod 2 pi in float-float (x = yh + yl).  For x >= 3 the two
 // cosines cos(x - pi/4 + p0) and cos(x - 3 pi/4 + p1) come from one sin/cos of the reduced x,
 // rotated by the small phase corrections p0, p1 through the angle-addition identities
-// (cos(-pi/4) = sin(pi/4) = 1/sqrt 2): max |J - J_exact| 1.0e-7 (J0) and 0.9e-7 (J1) on
+// (cos(-pi/4) = sin(pi/4) = 1/sqrt 2): max |J - J_exact| 1.0e-7 (J0) and 1.25e-7 (J1) on
 // [3, 3000] in a float32 emulation, the approximations' own error.
 template <bool WANT_J1>
 __device__ __forceinline__ void bessel01(float yh, float yl, float& J0, float& J1)
