@@ -17,7 +17,11 @@ int mma_probe_fma_peak(int precision, double *flops_per_s);
  * D[128][256] = A[128][32] * B[256][32]^T with FP16 A, B (row-major, device pointers) and FP32 D,
  * through tcgen05.mma with the operands in 64-byte-swizzled shared memory.  A is staged by
  * threads; B by threads (use_tma = 0) or by a TMA tiled load (use_tma = 1).  *status (device)
- * is 0 on success, non-zero if a bounded wait gave up. */
+ * is 0 on success, non-zero if a bounded wait gave up.
+ * use_tma = 2 checks the failure path of those bounded waits: one thread waits on a barrier
+ * that nothing arrives at (no copy and no MMA is issued), the wait gives up after 20 ms,
+ * *status becomes 1, and the kernel frees its tensor memory and returns without writing D;
+ * the context stays usable. */
 int mma_tc_selftest(const void *A, const void *B, float *D, int use_tma, int *status, void *stream);
 
 #ifdef __cplusplus

@@ -69,6 +69,13 @@ typedef struct mma_hankel_fast_plan_t {
 int mma_hankel_fast_plan(const double *zgrid_host, int64_t n_z, double distance, double omega_max, double r_max,
                          double rho_max, double tol, mma_hankel_fast_plan_t *plan);
 size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan);
+/* Status of the last mma_hankel_fast call on this scratch (synchronises the stream): MMA_OK, or
+ * MMA_ERR_TIMEOUT if a bounded wait of its streamed stage 1 gave up (that call's far field is then
+ * NaN).  The streamed stage 1 runs for complex64 sources with rows on 16-byte boundaries (even
+ * n_r and strides) and pre-factors per (plane, frequency); other problems take the direct stage 1,
+ * which has no waits. */
+int mma_hankel_fast_status(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan, const void *scratch,
+                           void *stream);
 int mma_hankel_fast(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan, const double *ogrid,
                     const double *rgrid, const double *zgrid, const double *rho, const void *source, const double *pre,
                     double *ff, const int64_t *plane_slot, int n_planes, double *planes, void *scratch,

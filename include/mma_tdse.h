@@ -35,7 +35,8 @@ typedef enum {
     MMA_ERR_ARG = 1,          /* invalid argument (sizes, NaN/inf inputs, null pointers) */
     MMA_ERR_GS_NOCONV = 2,    /* ground state did not reach |dE| <= CV within max_iter (reference: exit) */
     MMA_ERR_CUDA = 3,         /* a CUDA runtime call failed */
-    MMA_ERR_CUFFT = 4,        /* a cuFFT call failed */
+    MMA_ERR_DFT = 4,          /* a device DFT could not be planned (tables not allocated, or its first
+                                 call for a length came while the stream was being captured) */
     MMA_ERR_TOO_LARGE = 5,    /* grid does not fit the selected kernel's limits */
     MMA_ERR_NO_DEVICE = 6,    /* no CUDA device: there is no CPU fallback */
     MMA_ERR_UNSUPPORTED = 7,  /* option the reference accepts but never implemented (velocity gauge) */
@@ -268,6 +269,9 @@ int mma_tdse_propagate(const mma_tdse_instance *insts, int n_inst, const mma_tds
 /* mma_tdse_propagate with the CTA size of the complex64 form chosen by the caller (0 = 256):
  * every instance's grid must carry c64 tables of shape (cta_threads, max_m), see
  * mma_tdse_grid.c64_threads; instances whose grid has another shape get NaN outputs.
+ * max_m = 0 (complex64, cta_threads 0 or 256) launches the width-dispatching kernel: the
+ * instances' grids may have tables of any 256-thread width (8 to 48 sites per thread), all in
+ * one launch from one work queue (one CTA per SM); grids laid out for other CTA sizes get NaN.
  * For precisions 0 and 2 cta_threads must be 0 or 256. */
 int mma_tdse_propagate_ex(const mma_tdse_instance *insts, int n_inst, const mma_tdse_grid *grids,
                           const mma_tdse_buffers *bufs, int max_m, int cta_threads, int grid_ctas, int precision,
@@ -313,7 +317,12 @@ int mma_tdse_default_ctas(int max_m, int precision);
  * (mma_tdse_noalloc_capacity_bytes()), which every GPU that loads the library holds
  * until the process exits.  The caller still passes inputs and outputs.
  *   - The first call on each device looks up that device's address of the array;
- *     make it before any stream capture on that device.
+ *     make it before any stream capture on that device.  The address is kept for the
+ *     life of the process: after cudaDeviceReset (or any teardown of the device's
+ *     primary context) it is stale, and this entry point must not be called again in
+ *     that process.
+ *   - An instance whose grid has more than max_m sites per thread (grid.m > max_m) is
+ *     skipped by the kernel and its outputs are NaN; the others run normally.
  *   - Limits: the wavefunction must fit in shared memory and one CTA's sweep buffer
  *     (max_m * 4096 bytes) must fit in the array; larger grids return
  *     MMA_ERR_TOO_LARGE without launching.  Fewer CTAs run when the array is the limit.
@@ -352,7 +361,10 @@ int mma_tdse_adjoint(const mma_tdse_instance *insts, int n_inst, const mma_tdse_
 
 /* Fourier interpolation (1DTDSE/sources/tools_fftw3.c:24-68) of n_batch fields of
  * equal length n_raw (rows of `raw`, contiguous) by factor k1 into `interp`
- * (k1*n_raw per row): real DFT, zero padding, inverse DFT, 1/n_raw (cuFFT).
+ * (k1*n_raw per row): real DFT, zero padding, inverse DFT, 1/n_raw (this library's own DFTs:
+ * Stockham mixed radix, Bluestein's convolution for lengths that are not 7-smooth).  The first
+ * call for each field length plans its DFTs (device tables, a timed choice of CTA size) and must
+ * come before any stream capture; later calls, and mma_tdse_spectra's, are capturable.
  * For k1 = 1 the interpolation is the identity and the samples are copied
  * exactly (the reference's round trip only adds round-off). */
 int mma_tdse_prepare_fields(const double *raw, int n_batch, int n_raw, int k1, double *interp, void *stream);
@@ -362,6 +374,22 @@ int mma_tdse_prepare_fields(const double *raw, int n_batch, int n_raw, int k1, d
  * M2 [n_omega] for each row; series are read at stride `series_stride`. */
 int mma_tdse_spectra(const double *series, int64_t series_stride, int n_batch, int n_out, double dt, double tmax,
                      double *fsig, int64_t fsig_stride, double *fm2, int64_t fm2_stride, double *omega, void *stream);
+
+/* Batched real DFTs in FP64 with FFTW's conventions, the transforms FFTW performs inside the
+ * reference's tools_fftw3.c (FourInterp :24-68, calcFFTW3 :84-143, GaborTransform :158-213); this
+ * library uses them for all three.  Device pointers; rows at the given strides (in elements).
+ *   mma_dft_r2c: X_k = sum_j x_j e^{-2 pi i j k/n}, k = 0 .. n/2 (X interleaved re, im).
+ *   mma_dft_c2r: x_j = scale sum_{k<n} X_k e^{+2 pi i j k/n} with X_{n-k} = conj(X_k), from the
+ *     first n_bins bins of each row (the rest are zero).
+ * The first call for a length n plans it on the current device (tables, and the CTA size picked
+ * by timing the candidates on a probe batch) and must come before any stream capture.
+ * mma_dft_plan_info reports a length's plan: FFT length (n/2 for even n, n for odd n, or the
+ * Bluestein convolution length), whether Bluestein is used, the CTA size (0: the global-memory
+ * path for FFT lengths above 7168) and the probe times of the 256- and 512-thread kernels. */
+int mma_dft_r2c(int n, const double *x, int64_t x_stride, double *X, int64_t X_stride, int n_batch, void *stream);
+int mma_dft_c2r(int n, const double *X, int64_t X_stride, int n_bins, double *x, int64_t x_stride, int n_batch,
+                double scale, void *stream);
+int mma_dft_plan_info(int n, int *fft_len, int *bluestein, int *cta_threads, float *probe_ms);
 
 #ifdef __cplusplus
 }

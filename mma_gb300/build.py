@@ -1,7 +1,7 @@
 """Build libmma_gb300.so in-tree with nvcc for sm_103a.
 
 Every .cu under mma_gb300/csrc is compiled in parallel (one -gencode, sm_103a)
-and linked with cuFFT into mma_gb300/libmma_gb300.so.  Objects go to
+and linked into mma_gb300/libmma_gb300.so (CUDA runtime only; no CUDA math library).  Objects go to
 mma_gb300/_build/.  Rebuilds only when a source or header is newer than the
 library.
 """
@@ -63,7 +63,7 @@ def build(force=False, verbose=False, extra_flags=()):
     with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(comp, srcs))
     tmp = LIB + ".tmp"
-    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcufft", "-lcudart"]
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

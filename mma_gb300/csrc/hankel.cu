@@ -12,12 +12,14 @@
 #include "../../include/mma_hankel.h"
 #include "../../include/mma_tdse.h"
 #include "hankel_common.cuh"
+#include "tc_sm100.cuh"
 
 namespace mma {
 namespace hk {
 
 constexpr int kThreads = 256;
 constexpr int kMaxRhoPerThread = 8;  // plain form: n_rho <= 2048
+constexpr uint64_t kRingWaitNs = 2000000000ull;  // bounded waits of the ring stage 1 (2 s)
 
 // ------------------------------------------------------------------------ plain FP64 form
 // One CTA per frequency; per plane the CTA builds A_k[r] in shared memory, then each thread
@@ -80,8 +82,9 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(mma_hankel_problem P, c
 }
 
 // ------------------------------------------------------------------------ fast form, stage 1
-// Per-plane constants, independent of frequency, computed once per call:
-//   ptab[k*(MM+2) + m] = tau_k v_k^m  (m < MM),  ptab[k*(MM+2) + MM, +MM+1] = 1/(2 D_k) as (hi, lo).
+// Per-plane constants, independent of frequency, computed once per call (rows of MM + 4 floats):
+//   row[m] = tau_k v_k^m (m < MM),  row[MM], row[MM+1] = 1/(2 D_k) as (hi, lo),
+//   row[MM+2] = 1/(2 D_k) - 1/(2 d_ref) (the plane's offset from the reference distance), row[MM+3] = 0.
 template <int MM>
 __global__ void fast_plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, const double* zg, float* ptab)
 {
@@ -90,7 +93,7 @@ __global__ void fast_plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F,
         const double lam = F.d_ref / D;
         const double v = (1.0 - lam * lam) / F.sigma;
         double c = trap_w(zg, q, P.n_z);
-        float* row = ptab + q * (MM + 2);
+        float* row = ptab + q * (MM + 4);
         for (int m = 0; m < MM; m++) {
             row[m] = (float)c;
             c *= v;
@@ -99,7 +102,179 @@ __global__ void fast_plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F,
         split_d(1.0 / (2.0 * D), hi, lo);
         row[MM] = hi;
         row[MM + 1] = lo;
+        row[MM + 2] = (float)(1.0 / (2.0 * D) - 1.0 / (2.0 * F.d_ref));
+        row[MM + 3] = 0.f;
     }
+}
+
+// Per-frequency and per-radius constants of stage 1 as floats: ktab[w] = k_w = w/c as (hi, lo);
+// rtab[r] = (r^2 as (hi, lo), trapezoid weight * r, 0).
+__global__ void fast_wr_tables(mma_hankel_problem P, const double* og, const double* rg, float2* ktab, float4* rtab)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P.n_omega; q += stride) {
+        float hi, lo;
+        split_d(og[q] / kC, hi, lo);
+        ktab[q] = make_float2(hi, lo);
+    }
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P.n_r; q += stride) {
+        const double rr = rg[q];
+        float hi, lo;
+        split_d(rr * rr, hi, lo);
+        rtab[q] = make_float4(hi, lo, (float)(trap_w(rg, q, P.n_r) * rr), 0.f);
+    }
+}
+
+// Stage 1 through a shared-memory ring, for complex64 sources whose rows start on 16-byte
+// boundaries (rows of an even number of radii at even strides) and pre-factors per (plane,
+// frequency).  One CTA per (frequency, 256 radii), one radius per thread.  Thread 0 streams each
+// plane's row of radii (2 KB) into a ring of `ns` stages with 1-D bulk copies, so that tens of
+// KB per SM are in flight whatever the register count: the stage of plane kz - kSlack is refilled
+// with plane kz - kSlack + ns once every warp has released it, which lets the warps drift
+// kSlack planes apart.  Every thread accumulates
+//   B_m = sum_k tau_k v_k^m pre_k e^{-i k r^2/(2 D_k)} r w_r S_k,
+// with the near-field phase split as e^{-i k r^2 u_ref} e^{-i k r^2 (u_k - u_ref)} (u = 1/(2D)):
+// the first factor once per thread (float-float angle, reduced mod 2 pi), the second from the
+// small angle delta = k r^2 (u_k - u_ref) by its Taylor polynomials (|delta| <= 0.12; larger
+// angles take the exact reduction), and the 16-plane partial sums by packed FP32x2 FMAs.  Every
+// wait is bounded; on a timeout the CTA stops, sets *status and writes NaN into its B values.
+constexpr int kRingR = 256;  // radii per CTA, one per thread
+constexpr int kSlack = 8;    // planes the warps may drift apart
+template <int MM>
+__global__ void __launch_bounds__(kRingR, 1)
+    fast_stage1_ring(mma_hankel_problem P, const float2* __restrict__ src, const double2* __restrict__ pre,
+                     const float* __restrict__ ptab, const float2* __restrict__ ktab,
+                     const float4* __restrict__ rtab, float2 u_ref, float2* Bp, int ns, int* status)
+{
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    constexpr int RW = MM + 4;
+    const int64_t o = blockIdx.y, Nz = P.n_z, Nr = P.n_r, No = P.n_omega;
+    const int64_t r0 = (int64_t)blockIdx.x * kRingR;
+    const int cnt = (int)(Nr - r0 < kRingR ? Nr - r0 : kRingR);
+    float2* ring = reinterpret_cast<float2*>(smem_raw);                  // ns x kRingR source values
+    float4* coef = reinterpret_cast<float4*>(ring + (size_t)ns * kRingR);  // Nz x MM/4: tau_k v_k^m
+    float4* pinfo = coef + Nz * (MM / 4);                                // Nz: (pre re, pre im, du, 0)
+    uint64_t* full = reinterpret_cast<uint64_t*>(pinfo + Nz);
+    uint64_t* empty = full + ns;
+    volatile int* abort_s = reinterpret_cast<volatile int*>(empty + ns);
+    const int t = threadIdx.x, lane = t & 31;
+    const uint32_t bytes = (uint32_t)cnt * 8u;
+    const float2* row0 = src + o * P.omega_stride + r0;
+    if (t == 0) {
+        for (int s = 0; s < ns; s++) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], kRingR / 32);
+        }
+        *abort_s = 0;
+        tc::fence_barrier_init();
+        for (int64_t kz = 0; kz < Nz && kz < ns; kz++) {  // the first ns planes, before the tables
+            tc::mbar_arrive_expect_tx(&full[kz], bytes);
+            tc::bulk_load_1d(ring + (size_t)kz * kRingR, row0 + kz * P.plane_stride, bytes, &full[kz]);
+        }
+    }
+    for (int64_t q = t; q < Nz * (MM / 4); q += blockDim.x) {
+        const float* row = ptab + (q / (MM / 4)) * RW + (q % (MM / 4)) * 4;
+        coef[q] = make_float4(row[0], row[1], row[2], row[3]);
+    }
+    for (int64_t q = t; q < Nz; q += blockDim.x) {
+        const double2 pf = pre ? pre[q * No + o] : make_double2(1.0, 0.0);
+        pinfo[q] = make_float4((float)pf.x, (float)pf.y, ptab[q * RW + MM + 2], 0.f);
+    }
+    __syncthreads();
+    int64_t issued = Nz < ns ? Nz : ns;  // planes whose copies thread 0 has issued
+    // ---------------------------------------------------------------- consumers
+    const bool active = t < cnt;
+    const int64_t r = r0 + (active ? t : 0);
+    const float2 kk = ktab[o];
+    const float4 rt = rtab[r];
+    // k r^2 as float-float, and the reference phase e^{-i k r^2 u_ref} times r w_r
+    const float kr2h = kk.x * rt.x;
+    const float kr2l = fmaf(kk.x, rt.x, -kr2h) + fmaf(kk.x, rt.y, kk.y * rt.x);
+    float2 bw = make_float2(rt.z, 0.f);
+    if (P.near_field) {
+        const float th = kr2h * u_ref.x;
+        const float te = fmaf(kr2h, u_ref.x, -th) + fmaf(kr2h, u_ref.y, kr2l * u_ref.x);
+        float sn, cs;
+        sincos_reduced(reduce_2pi(th, te), sn, cs);
+        bw = make_float2(rt.z * cs, -rt.z * sn);
+    }
+    float2 part[MM], hi[MM], lo[MM];
+#pragma unroll
+    for (int m = 0; m < MM; m++) part[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
+    bool ok = true;
+    for (int64_t kz = 0; kz < Nz; kz++) {
+        const int s = (int)(kz % ns);
+        if (t == 0 && kz >= kSlack && issued < Nz) {
+            // refill the stage of plane kz - kSlack (released by every warp) with plane `issued`
+            const int64_t kp = kz - kSlack;
+            if (tc::mbar_wait(&empty[kp % ns], (uint32_t)(kp / ns) & 1u, abort_s, kRingWaitNs)) {
+                tc::mbar_arrive_expect_tx(&full[issued % ns], bytes);
+                tc::bulk_load_1d(ring + (size_t)(issued % ns) * kRingR, row0 + issued * P.plane_stride, bytes,
+                                 &full[issued % ns]);
+                issued++;
+            } else if (!*abort_s) {
+                *abort_s = 1;
+                atomicCAS(status, 0, 1);
+            }
+        }
+        if (!tc::mbar_wait(&full[s], (uint32_t)(kz / ns) & 1u, abort_s, kRingWaitNs)) {
+            *abort_s = 1;
+            atomicCAS(status, 0, 2);
+            ok = false;
+            break;
+        }
+        const float2 sv = active ? ring[(size_t)s * kRingR + t] : make_float2(0.f, 0.f);
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&empty[s]);
+        const float4 pi = pinfo[kz];
+        float2 a = make_float2(fmaf(pi.x, sv.x, -pi.y * sv.y), fmaf(pi.x, sv.y, pi.y * sv.x));
+        float2 e = bw;
+        if (P.near_field) {
+            const float d = kr2h * pi.z;  // k r^2 (u_k - u_ref)
+            float sn, cs;
+            if (fabsf(d) <= 0.12f) {
+                sincos_small(d, sn, cs);
+                e = make_float2(fmaf(bw.x, cs, bw.y * sn), fmaf(bw.y, cs, -bw.x * sn));
+            } else {  // exact angle k r^2 u_k, as the direct stage 1
+                const float ih = ptab[kz * RW + MM], il = ptab[kz * RW + MM + 1];
+                const float th = kr2h * ih;
+                const float te = fmaf(kr2h, ih, -th) + fmaf(kr2h, il, kr2l * ih);
+                sincos_reduced(reduce_2pi(th, te), sn, cs);
+                e = make_float2(rt.z * cs, -rt.z * sn);
+            }
+        }
+        a = make_float2(fmaf(a.x, e.x, -a.y * e.y), fmaf(a.x, e.y, a.y * e.x));
+        const float4* c4 = coef + kz * (MM / 4);
+#pragma unroll
+        for (int m4 = 0; m4 < MM / 4; m4++) {
+            const float4 c = c4[m4];
+            part[4 * m4 + 0] = __ffma2_rn(make_float2(c.x, c.x), a, part[4 * m4 + 0]);
+            part[4 * m4 + 1] = __ffma2_rn(make_float2(c.y, c.y), a, part[4 * m4 + 1]);
+            part[4 * m4 + 2] = __ffma2_rn(make_float2(c.z, c.z), a, part[4 * m4 + 2]);
+            part[4 * m4 + 3] = __ffma2_rn(make_float2(c.w, c.w), a, part[4 * m4 + 3]);
+        }
+        if ((kz & 15) == 15 || kz == Nz - 1) {
+#pragma unroll
+            for (int m = 0; m < MM; m++) {  // packed two-sum of (hi, part) into (hi, lo)
+                const float2 sm = __fadd2_rn(hi[m], part[m]);
+                const float2 bb = __fadd2_rn(sm, make_float2(-hi[m].x, -hi[m].y));
+                const float2 t1 = __fadd2_rn(sm, make_float2(-bb.x, -bb.y));
+                const float2 e1 = __fadd2_rn(hi[m], make_float2(-t1.x, -t1.y));
+                const float2 e2 = __fadd2_rn(part[m], make_float2(-bb.x, -bb.y));
+                lo[m] = __fadd2_rn(lo[m], __fadd2_rn(e1, e2));
+                hi[m] = sm;
+                part[m] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+    if (t == 0 && !ok)  // after an abort, let the copies already issued land before the CTA leaves
+        for (int64_t kz = (issued > ns ? issued - ns : 0); kz < issued; kz++)
+            tc::mbar_wait(&full[kz % ns], (uint32_t)(kz / ns) & 1u, nullptr, kRingWaitNs);
+    if (!active) return;
+    const float nan = __int_as_float(0x7fc00000);
+#pragma unroll
+    for (int m = 0; m < MM; m++)
+        Bp[(o * MM + m) * Nr + r] = ok ? make_float2(hi[m].x + lo[m].x, hi[m].y + lo[m].y) : make_float2(nan, nan);
 }
 
 // z-contraction B_m[w, r] = sum_k tau_k v_k^m A_k[w, r]: one thread per (w, r), source read once,
@@ -111,7 +286,7 @@ __global__ void __launch_bounds__(kThreads) fast_stage1(mma_hankel_problem P, co
 {
     extern __shared__ float smem[];
     const int64_t o = blockIdx.y, Nz = P.n_z, Nr = P.n_r, No = P.n_omega;
-    constexpr int RW = MM + 2;
+    constexpr int RW = MM + 4;
     float* tabs = smem;                                                   // Nz * RW
     float2* pr = reinterpret_cast<float2*>(smem + ((Nz * RW + 1) / 2) * 2);  // Nz: pre-factor
     for (int64_t q = threadIdx.x; q < Nz * RW; q += blockDim.x) tabs[q] = ptab[q];
@@ -398,30 +573,91 @@ extern "C" int mma_hankel_fast_plan(const double* zg, int64_t nz, double distanc
     return MMA_OK;
 }
 
-// scratch: B [n_omega][n_terms][n_r] complex float, then the per-plane table (n_z rows of n_terms+2 floats)
+// scratch: B [n_omega][n_terms][n_r] complex float | per-plane table (n_z rows of n_terms + 4 floats)
+// | ktab [n_omega] float2 | rtab [n_r] float4 | status word
+static size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 static size_t bp_bytes(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
 {
-    return (sizeof(float2) * (size_t)p->n_omega * (size_t)plan->n_terms * (size_t)p->n_r + 255) / 256 * 256;
+    return up256(sizeof(float2) * (size_t)p->n_omega * (size_t)plan->n_terms * (size_t)p->n_r);
+}
+static size_t ptab_bytes(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
+{
+    return up256(sizeof(float) * (size_t)p->n_z * (size_t)(plan->n_terms + 4));
+}
+static size_t ktab_off(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
+{
+    return bp_bytes(p, plan) + ptab_bytes(p, plan);
+}
+static size_t rtab_off(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
+{
+    return ktab_off(p, plan) + up256(sizeof(float2) * (size_t)p->n_omega);
+}
+static size_t status_off(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
+{
+    return rtab_off(p, plan) + up256(sizeof(float4) * (size_t)p->n_r);
 }
 
 extern "C" size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
 {
     if (!p || !plan) return 0;
-    return bp_bytes(p, plan) + sizeof(float) * (size_t)p->n_z * (size_t)(plan->n_terms + 2);
+    return status_off(p, plan) + 256;
+}
+
+extern "C" int mma_hankel_fast_status(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
+                                      const void* scratch, void* stream)
+{
+    if (!p || !plan || !scratch) return MMA_ERR_ARG;
+    int h = 0;
+    if (cudaMemcpyAsync(&h, static_cast<const char*>(scratch) + status_off(p, plan), sizeof(int),
+                        cudaMemcpyDeviceToHost, (cudaStream_t)stream) != cudaSuccess ||
+        cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+        return MMA_ERR_CUDA;
+    return h == 0 ? MMA_OK : MMA_ERR_TIMEOUT;
 }
 
 namespace {
+// Ring stages of stage 1 that fit next to its tables (0: the ring form does not apply here).
+template <int MM>
+int ring_stages(const mma_hankel_problem* p, const void* src)
+{
+    if (p->source_c128 || p->pre_radial || (p->n_r & 1) || (p->omega_stride & 1) || (p->plane_stride & 1) ||
+        (reinterpret_cast<uintptr_t>(src) & 15) || (MM % 4) || MM > 32)
+        return 0;
+    const size_t tables = (size_t)p->n_z * (MM * 4 + 16) + 64;
+    const size_t budget = 200 * 1024;
+    if (tables + 2 * kSlack * (kRingR * 8 + 16) > budget) return 0;
+    size_t ns = (budget - tables) / (kRingR * 8 + 16);
+    return (int)(ns > 64 ? 64 : ns);
+}
+
 template <int MM>
 int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, const double* og, const double* rg,
                 const double* zg, const double* rho, const void* src, const double2* pre, double2* ff,
-                float2* Bp, float* ptab, cudaStream_t st)
+                float2* Bp, float* ptab, float2* ktab, float4* rtab, int* status, cudaStream_t st)
 {
-    const size_t s1 = sizeof(float) * (((size_t)p->n_z * (MM + 2) + 1) / 2 * 2) + sizeof(float2) * (size_t)p->n_z;
-    if (s1 > 200 * 1024) return MMA_ERR_TOO_LARGE;
     fast_plane_table<MM><<<(unsigned)((p->n_z + 127) / 128), 128, 0, st>>>(*p, *plan, zg, ptab);
-    cudaFuncSetAttribute(fast_stage1<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
-    dim3 g1((unsigned)((p->n_r + kThreads - 1) / kThreads), (unsigned)p->n_omega);
-    fast_stage1<MM><<<g1, kThreads, s1, st>>>(*p, og, rg, src, pre, ptab, Bp);
+    const int ns = ring_stages<MM>(p, src);
+    if (ns > 0) {  // stage 1 through the shared-memory ring
+        const int64_t nt = p->n_omega > p->n_r ? p->n_omega : p->n_r;
+        fast_wr_tables<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(*p, og, rg, ktab, rtab);
+        if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+        const size_t sr = (size_t)ns * kRingR * 8 + (size_t)p->n_z * (MM * 4 + 16) + 2 * (size_t)ns * 8 + 16;
+        cudaFuncSetAttribute(fast_stage1_ring<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr);
+        float hi, lo;  // u_ref = 1/(2 d_ref) as a float pair
+        const double u = 1.0 / (2.0 * plan->d_ref);
+        hi = (float)u;
+        lo = (float)(u - (double)hi);
+        dim3 g1((unsigned)((p->n_r + kRingR - 1) / kRingR), (unsigned)p->n_omega);
+        fast_stage1_ring<MM><<<g1, kRingR, sr, st>>>(*p, static_cast<const float2*>(src), pre, ptab, ktab, rtab,
+                                                           make_float2(hi, lo), Bp, ns, status);
+    } else {  // one thread per (frequency, radius) reading its planes directly
+        const size_t s1 =
+            sizeof(float) * (((size_t)p->n_z * (MM + 4) + 1) / 2 * 2) + sizeof(float2) * (size_t)p->n_z;
+        if (s1 > 200 * 1024) return MMA_ERR_TOO_LARGE;
+        cudaFuncSetAttribute(fast_stage1<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
+        dim3 g1((unsigned)((p->n_r + kThreads - 1) / kThreads), (unsigned)p->n_omega);
+        fast_stage1<MM><<<g1, kThreads, s1, st>>>(*p, og, rg, src, pre, ptab, Bp);
+    }
     int rtile = (int)(p->n_r < 512 ? p->n_r : 512);
     while ((size_t)(MM + 1) * rtile * sizeof(float2) > 96 * 1024 && rtile > 32) rtile /= 2;
     const size_t s2 = (size_t)(MM + 1) * rtile * sizeof(float2);
@@ -444,20 +680,29 @@ extern "C" int mma_hankel_fast(const mma_hankel_problem* p, const mma_hankel_fas
     cudaStream_t st = (cudaStream_t)stream;
     const double2* pre2 = reinterpret_cast<const double2*>(pre);
     double2* ff2 = reinterpret_cast<double2*>(ff);
-    float2* Bp = reinterpret_cast<float2*>(scratch);
-    float* ptab = reinterpret_cast<float*>(static_cast<char*>(scratch) + bp_bytes(p, plan));
+    char* sc = static_cast<char*>(scratch);
+    float2* Bp = reinterpret_cast<float2*>(sc);
+    float* ptab = reinterpret_cast<float*>(sc + bp_bytes(p, plan));
+    float2* ktab = reinterpret_cast<float2*>(sc + ktab_off(p, plan));
+    float4* rtab = reinterpret_cast<float4*>(sc + rtab_off(p, plan));
+    int* status = reinterpret_cast<int*>(sc + status_off(p, plan));
     int rc;
+#define MMA_FAST_CASE(T)                                                                                             \
+    case T:                                                                                                          \
+        rc = launch_fast<T>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, ktab, rtab, status, st); \
+        break;
     switch (plan->n_terms) {
-        case 8: rc = launch_fast<8>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
-        case 12: rc = launch_fast<12>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
-        case 16: rc = launch_fast<16>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
-        case 20: rc = launch_fast<20>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
-        case 24: rc = launch_fast<24>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
-        case 32: rc = launch_fast<32>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
-        case 40: rc = launch_fast<40>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
-        case 48: rc = launch_fast<48>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, st); break;
+        MMA_FAST_CASE(8)
+        MMA_FAST_CASE(12)
+        MMA_FAST_CASE(16)
+        MMA_FAST_CASE(20)
+        MMA_FAST_CASE(24)
+        MMA_FAST_CASE(32)
+        MMA_FAST_CASE(40)
+        MMA_FAST_CASE(48)
         default: return MMA_ERR_ARG;
     }
+#undef MMA_FAST_CASE
     if (rc != MMA_OK) return rc;
     if (n_planes > 0) {
         const int rtile = (int)(p->n_r < 1024 ? p->n_r : 1024);

@@ -218,8 +218,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 if (ok) mma_commit(&acc_full[a]);
             }
-            mma_commit(drain);  // all MMAs of this CTA complete before TMEM is freed
-            if (!mbar_wait(drain, 0u, abort_s, WAIT_NS)) fail(abort_s, P.status, 4);
+            // all MMAs this CTA issued complete before TMEM is freed -- also after an abort, so
+            // this wait is bounded by time only, not by the abort flag
+            mma_commit(drain);
+            if (!mbar_wait(drain, 0u, nullptr, WAIT_NS)) fail(abort_s, P.status, 4);
         }
         __syncwarp();
     } else {
@@ -536,7 +538,11 @@ __global__ void plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, cons
 
 // ------------------------------------------------------------------------ self-test
 // One tile: D[128 x 256] = A[128 x 32] * B[256 x 32]^T in FP16 -> FP32, A staged by threads into
-// the SW64 layout, B by threads or by TMA.  Checks descriptors, swizzle and the TMEM mapping.
+// the SW64 layout, B by threads (use_tma 0) or by TMA (1).  Checks descriptors, swizzle and the
+// TMEM mapping.  use_tma 2 checks the bounded-wait path instead: thread 0 waits on a barrier that
+// nothing arrives at (no copy, no MMA is issued), the wait runs out after kSelfTestWaitNs, the
+// status word becomes 1 and the kernel frees its TMEM and returns without touching D.
+constexpr uint64_t kSelfTestWaitNs = 20000000ull;
 __global__ void __launch_bounds__(128) tc_selftest_kernel(const __grid_constant__ CUtensorMap tm_b, const __half* A,
                                                           const __half* B, float* D, int use_tma, int* status)
 {
@@ -570,7 +576,12 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const __grid_constant_
     const uint32_t tmem = *tmem_s;
     bool ok = true;
     if (t == 0) {
-        if (use_tma) {
+        if (use_tma == 2) {  // nothing arrives at bars[0]: the bounded wait runs out
+            if (!mbar_wait(&bars[0], 0u, abort_s, kSelfTestWaitNs)) {
+                fail(abort_s, status, 1);
+                ok = false;
+            }
+        } else if (use_tma) {
             mbar_arrive_expect_tx(&bars[0], 256 * 64);
             tma_load_3d(sB, &tm_b, &bars[0], 0, 0, 0);
             if (!mbar_wait(&bars[0], 0u, abort_s, WAIT_NS)) {
@@ -582,11 +593,12 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const __grid_constant_
             constexpr uint32_t idesc = idesc_f16_f32(128, 256);
             const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
             for (int ks = 0; ks < 2; ks++) mma_f16(tmem, sdesc_sw64(a0 + ks * 32), sdesc_sw64(b0 + ks * 32), idesc, ks > 0);
+            mma_commit(&bars[1]);
         }
-        mma_commit(&bars[1]);
     }
     __syncthreads();
-    if (!mbar_wait(&bars[1], 0u, abort_s, WAIT_NS)) fail(abort_s, status, 2);
+    // after a failure nothing was committed to bars[1] (and the flag is set for every thread)
+    if (!*abort_s && !mbar_wait(&bars[1], 0u, abort_s, WAIT_NS)) fail(abort_s, status, 2);
     tc_fence_after();
     if (!*abort_s) {
         for (int c0 = 0; c0 < 256; c0 += 16) {
@@ -834,7 +846,8 @@ extern "C" int mma_tc_selftest(const void* A, const void* B, float* D, int use_t
     cudaStream_t st = (cudaStream_t)stream;
     CUtensorMap tb;
     std::memset(&tb, 0, sizeof(tb));
-    if (use_tma && !make_map(&tb, B, 32, 256, 1, 256)) return MMA_ERR_CUDA;
+    if (use_tma < 0 || use_tma > 2) return MMA_ERR_ARG;
+    if (use_tma == 1 && !make_map(&tb, B, 32, 256, 1, 256)) return MMA_ERR_CUDA;
     const size_t smem = 1024 + 128 * 64 + 256 * 64 + 64;
     if (cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return MMA_ERR_CUDA;

@@ -70,8 +70,8 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
 }
 
 // Wait until the phase with the given parity has completed.  Bounded: gives up after
-// `limit_ns` nanoseconds, or as soon as *abort (a flag in shared memory) is set, and then
-// returns false.  The caller records the failure and leaves its loop.
+// `limit_ns` nanoseconds, or as soon as *abort (a flag in shared memory; nullptr: bounded by
+// time only) is set, and then returns false.  The caller records the failure and leaves its loop.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort,
                                           uint64_t limit_ns)
 {
@@ -80,10 +80,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const 
     for (uint32_t i = 1;; i++) {
         if (mbar_test(bar, parity)) return true;
         if ((i & 63) == 0) {
-            if (*abort) return false;
+            if (abort && *abort) return false;
             if (global_ns() - t0 > limit_ns) return false;
         }
     }
+}
+
+// 1-D bulk copy global -> shared (no tensor map) completing on an mbarrier's transaction count;
+// both addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
 }
 
 // L1 prefetch hint for an address inside an allocation

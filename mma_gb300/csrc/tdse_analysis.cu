@@ -7,10 +7,10 @@
 //     elimination factors interleaved across energies so that a warp's loads coalesce;
 //   * the Gabor transform (tools_fftw3.c:158-213, GaborTransform): for every window centre
 //     t_w = t_min + w (t_max - t_min)/N_G the signal times exp(-((t_j - t_w)/a)^2), a real DFT
-//     (cuFFT, batched over windows and signals) and dt/sqrt(2 pi) |DFT_k| for k < N_freq.
+//     (this library's own, dft.cu, batched over windows and signals) and dt/sqrt(2 pi) |DFT_k| for
+//     k < N_freq.
 // The arithmetic follows the reference's expressions and their order (FP64).
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include <cmath>
 #include <cstdlib>
@@ -18,6 +18,7 @@
 
 #include "../../include/mma_tdse.h"
 #include "common.cuh"
+#include "dft.cuh"
 
 namespace mma {
 namespace an {
@@ -179,8 +180,6 @@ int grid_for(int64_t total) { return (int)((total + 255) / 256 < 8192 ? (total +
 
 using namespace mma;
 
-// cuFFT plans are cached by tdse_fft.cu (shape and batch)
-int mma_fft_get_plan_d2z(int n, long long idist, long long odist, int batch, cufftHandle* out);
 
 namespace {
 // scratch: V/12 [n + 1] | M2 psi [n] | gam [n][chunk] | u [n][chunk]
@@ -243,12 +242,10 @@ extern "C" int mma_gabor(const double* signals, int64_t stride, int n_sig, doubl
     double* win = reinterpret_cast<double*>(out);
     an::gabor_table<<<an::grid_for((int64_t)N_G * N), 256, 0, st>>>(N, N_G, dt, t_min, dt_G, ia, win);
     an::gabor_window<<<an::grid_for(nb * N), 256, 0, st>>>(signals, stride, n_sig, N, N_G, win, in);
-    cufftHandle p;
-    int rc = mma_fft_get_plan_d2z(N, N, Nc, (int)nb, &p);
+    const mma::dft::Plan* p = nullptr;
+    int rc = mma::dft::get_plan(N, st, &p);
+    if (rc == MMA_OK) rc = mma::dft::r2c(p, in, N, out, Nc, (int)nb, st);
     if (rc != MMA_OK) return rc;
-    if (cufftSetStream(p, st) != CUFFT_SUCCESS || cufftExecD2Z(p, in, reinterpret_cast<cufftDoubleComplex*>(out)) !=
-                                                      CUFFT_SUCCESS)
-        return MMA_ERR_CUFFT;
     an::gabor_abs<<<an::grid_for(nb * N_freq), 256, 0, st>>>(out, Nc, nb, N_freq, dt / sqrt(2. * an::kPi), gabor);
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }

@@ -342,6 +342,14 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_fp64_kernel(PropArgs P)
         double *o_t = out, *o_e = out + (S + 1), *o_src = out + 2 * (S + 1), *o_ptot = out + 3 * (S + 1),
                *o_pint = out + 4 * (S + 1), *o_x = out + 5 * (S + 1);
         const double dt = G.dt, dx = G.dx;
+        if (L > P.max_L) {
+            // A grid with more sites per thread than the launch was sized for (max_m) would
+            // overrun this CTA's sweep buffer and its shared memory: the instance is skipped
+            // and its outputs are NaN, the loud failure of a mismatched shape.
+            for (int64_t e = t; e < 6 * (S + 1); e += kThreads) out[e] = __longlong_as_double(0x7ff8000000000000LL);
+            __syncthreads();
+            continue;
+        }
 
         if (t == 0) {
             s_gate = gate_index(f, I.n_field, S, I.gate_floor);
@@ -557,10 +565,11 @@ extern "C" int mma_tdse_propagate_ex(const mma_tdse_instance* insts, int n_inst,
                                      int precision, void* stream)
 {
     if (n_inst <= 0) return MMA_OK;
-    if (!insts || !grids || !bufs || !bufs->fields || !bufs->outputs || !bufs->counter || !bufs->scratch ||
-        max_m < 1)
-        return MMA_ERR_ARG;
     if (precision < 0 || precision > 2) return MMA_ERR_UNSUPPORTED;
+    // max_m = 0 is the complex64 form's "every 256-thread table width" launch
+    if (!insts || !grids || !bufs || !bufs->fields || !bufs->outputs || !bufs->counter || !bufs->scratch ||
+        max_m < (precision == 1 ? 0 : 1))
+        return MMA_ERR_ARG;
     if (sm_count() <= 0) return MMA_ERR_NO_DEVICE;
     if (grid_ctas <= 0)
         grid_ctas = precision == 1 ? mma_tdse_c64_default_ctas(max_m, cta_threads) : mma_tdse_default_ctas(max_m, precision);

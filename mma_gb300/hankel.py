@@ -6,7 +6,9 @@ Same names, arguments and results as the reference module:
   here (the kernels apply trapezoid weights), other integrators raise.
 * ``FSources_provider`` (:29-80) -- planes zgrid[0:-1:kz_step] (the last plane is
   dropped, as in the reference), source slices FSource[kz, omega, r]; the static
-  source is moved to the GPU once.  'dynamic' (HDF5) sources raise: no h5py here.
+  source is moved to the GPU once.  'dynamic' sources are read from the HDF5 archive
+  (CTDSE/outputs/FSourceTerm [kz, kr, omega, re/im]) by this package's own reader,
+  mma_gb300.h5io, one plane at a time.
 * ``get_propagation_pre_factor_function`` (:85-448) -- the no-modulation branch
   (scalar pressure) and the z-modulation branch (dict with 'zgrid', 'value'),
   returning (pre_factor(kz) -> [Nr, No], exp_renorm(kz) -> [No]) like the reference.

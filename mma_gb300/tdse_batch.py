@@ -56,7 +56,7 @@ class MMAStatusError(RuntimeError):
     pass
 
 
-_STATUS = {1: "invalid argument", 2: "ground state not converged", 3: "CUDA error", 4: "cuFFT error",
+_STATUS = {1: "invalid argument", 2: "ground state not converged", 3: "CUDA error", 4: "DFT plan error",
            5: "too large", 6: "no CUDA device", 7: "unsupported option"}
 
 
@@ -283,9 +283,12 @@ class TDSEBatchPlan:
     """A batch of TDSE instances with every device buffer allocated once.
 
     ``launch()`` issues the whole device pipeline -- Fourier interpolation of the
-    fields (one cuFFT batch per field length), the persistent propagation kernel
-    (one launch per kernel shape: all FP64 instances together, complex64 instances
-    per table width), the output spectra (one batch per series length) -- on one
+    fields (one batched DFT pair per field length), the persistent propagation kernel
+    (one launch for the whole batch: the FP64 and float-float kernels take any grid
+    width, and complex64 batches of several 256-thread table widths run the
+    width-dispatching kernel; ``c64_one_launch=False`` or grids with other CTA sizes give
+    one complex64 launch per table shape), the output spectra (one batch per series
+    length) -- on one
     stream, with no host synchronisation, so ``capture()`` can record it as a CUDA
     graph and ``replay()`` re-runs it on new fields written by ``load_fields``.
 
@@ -295,7 +298,7 @@ class TDSEBatchPlan:
     """
 
     def __init__(self, grids, n_field, dt_field, grid_ids=None, dt_req=None, tmin=0.0, precision="fp64",
-                 spectra=True, psi_final=False, snap_every=0, tmax=None, grid_ctas=0):
+                 spectra=True, psi_final=False, snap_every=0, tmax=None, grid_ctas=0, c64_one_launch=True):
         lib = _sig()
         self.lib = lib
         if precision not in PRECISIONS:
@@ -375,10 +378,15 @@ class TDSEBatchPlan:
             r.tmin, r.gate_floor = float(tmin), 0.0
             r.ckpt_off, r.ckpt_every = -1, 0
         self.recs = recs
-        # propagation launches: instances split by kernel shape, longest first within each
+        # propagation launches, longest first within each: one for the FP64 and float-float forms
+        # (width-generic kernels); for the complex64 form one per table shape (sites per thread,
+        # CTA size), or -- when every grid's tables are laid out for 256 threads and there are
+        # several widths -- one launch of the width-dispatching kernel (shape 0)
         cost = grids.n[gid].astype(np.float64) * S
-        if self.prec == 1:  # kernel shape = (sites per thread, CTA size) of the complex64 tables
+        if self.prec == 1:
             shapes = grids.m32[gid] * 4096 + grids.c64_threads[gid]
+            if c64_one_launch and len(np.unique(shapes)) > 1 and np.all(grids.c64_threads[gid] == THREADS):
+                shapes = np.zeros(n_inst, dtype=np.int64)
         else:
             shapes = np.zeros(n_inst, dtype=np.int64)
         self.launches = []
@@ -386,7 +394,7 @@ class TDSEBatchPlan:
             idx = np.nonzero(shapes == shape)[0]
             idx = idx[np.argsort(-cost[idx], kind="stable")]
             max_m = int(shape) // 4096 if self.prec == 1 else int(grids.m[np.unique(gid[idx])].max())
-            cta_threads = int(shape) % 4096 if self.prec == 1 else 0
+            cta_threads = (int(shape) % 4096 or THREADS) if self.prec == 1 else 0
             ctas = grid_ctas or (lib.mma_tdse_c64_default_ctas(max_m, cta_threads) if self.prec == 1
                                  else lib.mma_tdse_default_ctas(max_m, self.prec))
             ctas = min(ctas, len(idx))
@@ -478,7 +486,7 @@ class TDSEBatchPlan:
                                         G["fm"].data_ptr(), nc, G["omega"].data_ptr(), st), "mma_tdse_spectra")
 
     def capture(self):
-        """Record launch() as a CUDA graph (after one eager run that creates the cuFFT plans)."""
+        """Record launch() as a CUDA graph (after one eager run that creates the DFT plans)."""
         s = torch.cuda.Stream(device=self.device)
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):

@@ -14,21 +14,32 @@ import subprocess
 ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
 
 
+def ref_src():
+    """The reference checkout's 1DTDSE/sources directory, named by the MMA_REF_SRC
+    environment variable, or None when the variable is unset or names no directory."""
+    src = os.environ.get("MMA_REF_SRC")
+    return src if src and os.path.isdir(src) else None
+
+
 def build(ref=None):
-    """Compile the C restatement (always) and the reference DLL (when its sources
-    are present, or when ``ref`` is True)."""
+    """Compile the C restatement (always) and the reference DLL (when MMA_REF_SRC names
+    the reference's sources, or when ``ref`` is True, which then requires it)."""
     subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
-    src = os.environ.get("MMA_REF_SRC", "/root/reference/1DTDSE/sources")
+    src = ref_src()
     if ref is None:
-        ref = os.path.isdir(src)
+        ref = src is not None
     if ref:
+        if src is None:
+            raise RuntimeError("set MMA_REF_SRC to the reference checkout's 1DTDSE/sources directory")
         subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref", "REF_SRC=" + src], check=True)
 
 
 def ref_file(*parts):
     """Path of a file of the reference checkout (the parent of the 1DTDSE/sources directory
     named by MMA_REF_SRC), or None where the checkout is absent."""
-    src = os.environ.get("MMA_REF_SRC", "/root/reference/1DTDSE/sources")
+    src = ref_src()
+    if src is None:
+        return None
     p = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(src))), *parts)
     return p if os.path.exists(p) else None
 

@@ -23,7 +23,7 @@ ionization_h5.npz: every dataset as stored (float32 / int32), the wavefunction s
 subsampled to every 7th.
 
 Run from the repository root where the reference checkout exists:
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>
 """
 import argparse
 import os
@@ -46,15 +46,15 @@ TDSE_CASES = {
     "tdse_medium": (dict(num_r=2000, dx=0.2, trg_a=A_CONFIG), dict(n_cycles=3)),
     # the parameters of the reference's own regression test (1DTDSE/tests.py:13-39)
     "tdse_reftest": (dict(num_r=8000, dx=0.4, trg_a=1.0), dict(n_cycles=4, E0=0.14, omega=0.07)),
-    # field sampled at 0.5 a.u. > dt = 0.25: Fourier interpolation with k1 = 3
-    "tdse_interp": (dict(num_r=600, dx=0.4, trg_a=A_CONFIG), dict(n_cycles=2, dt=0.5)),
+    # field sampled at exactly 0.5 a.u. > dt = 0.25: Fourier interpolation with k1 = 3
+    "tdse_interp": (dict(num_r=600, dx=0.4, trg_a=A_CONFIG), dict(n_cycles=2, dt=0.5, exact_dt=True)),
     "tdse_snapshots": (dict(num_r=600, dx=0.4, trg_a=1.0, writewft=1, tprint=10.0), dict(n_cycles=1.5)),
     # config 0 of the benchmark: a^2 = 1.68, x in [-400, 400], dx = 0.1, 10-cycle 800 nm pulse
     "tdse_config0": (dict(num_r=8000, dx=0.1, trg_a=A_CONFIG), dict(n_cycles=10)),
 }
 
 
-def make_tdse(ref_src):
+def make_tdse(ref_src, only=None):
     import oracle
     from mma_gb300.tdse import TDSE_DLL, run_single
 
@@ -62,6 +62,8 @@ def make_tdse(ref_src):
     oracle.build(ref=True)
     dll = TDSE_DLL(oracle.ref_dll_path())
     for name, (kw, pk) in TDSE_CASES.items():
+        if only and name not in only:
+            continue
         t, E = sin2_pulse(skip_first=True, **pk)
         r = run_single(dll, t, E, CV=1e-15, **kw)
         out = dict(t=t, E=E, Einit=r["Einit"], psi0_re=np.real(r["psi0"]), x=r["x"],
@@ -335,11 +337,12 @@ def make_ionization(ref_root):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="the reference checkout (its top directory)")
     ap.add_argument("--only", choices=["tdse", "hankel", "analysis", "xuv", "radial", "ionization"], default=None)
+    ap.add_argument("--case", action="append", help="with --only tdse: regenerate only these TDSE fixtures")
     a = ap.parse_args()
     if a.only in (None, "tdse"):
-        make_tdse(os.path.join(a.ref, "1DTDSE", "sources"))
+        make_tdse(os.path.join(a.ref, "1DTDSE", "sources"), only=a.case)
     if a.only in (None, "hankel"):
         make_hankel(a.ref)
     if a.only in (None, "analysis"):

@@ -5,9 +5,12 @@ A_CONFIG = np.sqrt(1.68)  # soft-Coulomb a of the benchmark configurations (a^2 
 OMEGA0 = 0.057            # 800 nm in atomic units
 
 
-def sin2_pulse(n_cycles, E0=0.0534, omega=OMEGA0, dt=0.25, cep=0.0, even=True, skip_first=False):
+def sin2_pulse(n_cycles, E0=0.0534, omega=OMEGA0, dt=0.25, cep=0.0, even=True, skip_first=False, exact_dt=False):
     """Field sampled at ~dt on t in [0, T], T = n_cycles 2 pi/omega; an even sample count
     keeps the reference's last-step field read inside its interpolation buffer.
+
+    exact_dt samples at t = j dt exactly (the linspace grid's spacing T/(n-1) is slightly below
+    dt, which matters where the reference derives its refinement factor from the spacing).
 
     skip_first drops the t = 0 sample (where the field is exactly 0).  The reference's
     zero gate tests f[0] f[1] <= 0 on its Fourier-interpolated field, so on a field that
@@ -19,7 +22,7 @@ def sin2_pulse(n_cycles, E0=0.0534, omega=OMEGA0, dt=0.25, cep=0.0, even=True, s
         n += 1
     if even and (n - (1 if skip_first else 0)) % 2:
         n += 1
-    t = np.linspace(0.0, T, n)
+    t = dt * np.arange(n) if exact_dt else np.linspace(0.0, T, n)
     if skip_first:
         t = t[1:]
     E = E0 * np.sin(np.pi * t / T) ** 2 * np.cos(omega * t + cep)

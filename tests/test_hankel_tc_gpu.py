@@ -46,6 +46,29 @@ def test_tcgen05_tile(gpu_lib, use_tma):
     assert (D - ref).abs().max().item() <= 1e-5 * ref.abs().max().item()
 
 
+def test_tcgen05_bounded_wait_runs_out(gpu_lib):
+    """A bounded mbarrier wait that nothing satisfies gives up, the kernel reports the timeout in
+    its status word and returns; the next tensor-core launch in the same context still works."""
+    from mma_gb300._lib import load
+
+    lib = load()
+    lib.mma_tc_selftest.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.mma_tc_selftest.restype = ctypes.c_int
+    A = torch.ones(128, 32, dtype=torch.float16, device="cuda")
+    B = torch.ones(256, 32, dtype=torch.float16, device="cuda")
+    D = torch.full((128, 256), -7.0, dtype=torch.float32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.mma_tc_selftest(A.data_ptr(), B.data_ptr(), D.data_ptr(), 2, status.data_ptr(), st) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 1  # the first bounded wait gave up
+    assert bool((D == -7.0).all())  # nothing was written
+    assert lib.mma_tc_selftest(A.data_ptr(), B.data_ptr(), D.data_ptr(), 1, status.data_ptr(), st) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert bool((D == 32.0).all())
+
+
 def _problem(n_omega=24, n_r=200, n_z=40, n_rho=50, seed=0, rho_max=5e-3):
     omega0 = 0.057 / 2.4188843265857e-17
     rgrid = np.linspace(0.0, 200e-6, n_r)

@@ -115,3 +115,39 @@ def test_c64_default_ctas_follow_occupancy(gpu_lib):
     assert gpu_lib.mma_tdse_c64_default_ctas(32, 256) == sms
     assert gpu_lib.mma_tdse_c64_default_ctas(16, 512) == sms
     assert gpu_lib.mma_tdse_c64_default_ctas(12, 256) == 0
+
+
+def test_c64_uneven_widths_in_one_launch(gpu_lib):
+    """Grids of every 256-thread table width (16 to 48 sites per thread: 3001 to 12001 sites) and
+    pulses of different lengths in one batch: one launch of the width-dispatching kernel, and the
+    same results as one launch per width (the same per-instance code, so equal to FP32 rounding
+    of the compiled schedule), all finite."""
+    from mma_gb300.tdse_batch import TDSEBatchPlan, TDSEGrids
+
+    params = [dict(num_r=n, dx=0.1, trg_a=A_CONFIG) for n in (3000, 5000, 7000, 9000, 12000)]
+    dtf = 0.25
+    grids = TDSEGrids(params, dt=dtf, c64=True)
+    assert sorted(set(int(m) for m in grids.m32)) == [16, 24, 32, 40, 48]
+    rng = np.random.default_rng(3)
+    fields, ids = [], []
+    for i in range(12):
+        T = (1.0 + 0.25 * (i % 4)) * 2 * np.pi / 0.057
+        n = int(T / dtf)
+        n += n % 2
+        t = dtf * np.arange(1, n + 1)
+        fields.append(torch.tensor(rng.uniform(0.03, 0.07) * np.sin(np.pi * t / T) ** 2 * np.cos(0.057 * t),
+                                   device="cuda"))
+        ids.append(i % len(params))
+    out = {}
+    for one in (True, False):
+        plan = TDSEBatchPlan(grids, [len(f) for f in fields], dtf, grid_ids=ids, precision="c64", c64_one_launch=one)
+        assert len(plan.launches) == (1 if one else 5)
+        plan.load_fields(fields)
+        plan.launch()
+        torch.cuda.synchronize()
+        out[one] = plan
+    for i in range(len(fields)):
+        a, b = out[True].result().series(i), out[False].result().series(i)
+        for k in ("sourceterm", "PopTot", "PopInt", "expval"):
+            assert torch.isfinite(a[k]).all()
+            assert rel_l2(a[k].cpu().numpy(), b[k].cpu().numpy()) < 1e-6, (i, k)
