@@ -105,7 +105,7 @@ def run_config2(args, device):
 
     from mma_gb300.tdse_batch import TDSEBatchPlan, TDSEGrids
 
-    n_inst = 4096 if args.workload == "config2" else 256
+    n_inst = 4096 if args.workload in ("config2", "config1") else 256
     params, fields, E0 = config2_instances(n_inst)
     t0 = time.perf_counter()
     # 256-thread complex64 tables for every grid, so that every width goes in one launch
@@ -116,11 +116,14 @@ def run_config2(args, device):
     out = {"instances": n_inst, "grid_build_s": t_grids, "site_steps": float(sum(
         (p["num_r"] + 1) * (len(f) + 2) for p, f in zip(params, fields)))}
     res = {}
-    for prec in ("df64", "c64", "fp64"):
-        plan = TDSEBatchPlan(grids, [len(f) for f in fields], 0.25, grid_ids=np.arange(n_inst), precision=prec)
+    for prec in ("df64", "c64", "c64_per_shape", "fp64"):
+        plan = TDSEBatchPlan(grids, [len(f) for f in fields], 0.25, grid_ids=np.arange(n_inst),
+                             precision="c64" if prec == "c64_per_shape" else prec,
+                             c64_one_launch=prec != "c64_per_shape")
         plan.load_fields(tf)
-        plan.capture()
-        plan.replay()
+        plan.capture()  # one eager run (DFT plans), then the graph
+        if prec != "fp64":  # the FP64 form (18 s a batch) is timed on its first replay
+            plan.replay()
         torch.cuda.synchronize()
         reps = 3 if prec != "fp64" else 1
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
@@ -165,7 +168,7 @@ def run_config4(args, device):
     from mma_gb300.tdse_adjoint import yield_and_grad
     from mma_gb300.tdse_batch import TDSEGrids
 
-    n_inst = 256 if args.workload == "config4" else 16
+    n_inst = 256 if args.workload in ("config4", "config1") else 16
     t, fields_np = focus_fields()
     fields = torch.tensor(fields_np[::len(fields_np) // n_inst][:n_inst], device=device)
     dtf = t[1] - t[0]
@@ -181,7 +184,7 @@ def run_config4(args, device):
     e[2].record()
     torch.cuda.synchronize()
     t_fwd, t_grad = e[0].elapsed_time(e[1]) * 1e-3, e[1].elapsed_time(e[2]) * 1e-3
-    n_samples = 32 if args.workload == "config4" else 4
+    n_samples = getattr(args, "fd_samples", None) or (32 if args.workload == "config4" else 4)
     rng = np.random.default_rng(0)
     nf = fields.shape[1]
     idx = np.stack([rng.choice(np.arange(4, nf - 4), size=n_samples, replace=False) for _ in range(n_inst)])
@@ -426,7 +429,7 @@ def run_all_planes(args, target, z, rho, pre, flush, stream):
         ptc = None
         flush.add_(1.0)
         e0.record(stream)
-        _, ptc, plan = call("fast", "tc", (k0, k1))
+        ff_tc, ptc, plan = call("fast", "tc", (k0, k1))
         e1.record(stream)
         torch.cuda.synchronize()
         t_all.append(e0.elapsed_time(e1) * 1e-3)
@@ -443,12 +446,13 @@ def run_all_planes(args, target, z, rho, pre, flush, stream):
     del pdir
     flush.add_(1.0)
     e0.record(stream)
-    _, p64, _ = call("plain")
+    ff64, p64, _ = call("plain")
     e1.record(stream)
     torch.cuda.synchronize()
     t_plain = e0.elapsed_time(e1) * 1e-3
     P64 = torch.stack([p64[k] for k in allp])
     del p64
+    e_ff = (torch.linalg.norm(ff_tc - ff64, dim=0) / torch.linalg.norm(ff64, dim=0)).cpu().numpy()
     nrm = torch.linalg.norm(P64, dim=1)  # [plane, omega]
     e_tc = (torch.linalg.norm(P_tc - P64, dim=1) / nrm).flatten()
     e_dir = (torch.linalg.norm(P_dir - P64, dim=1) / nrm).flatten()
@@ -474,8 +478,12 @@ def run_all_planes(args, target, z, rho, pre, flush, stream):
                             "gemm": geo,
                             "per_harmonic_rel_err_vs_plain": {"max": float(e_tc.max()),
                                                               "median": float(e_tc.median())},
-                            "includes": "FF_integrated (fast form) + plane tables + B operand + tensor-core "
-                                        "kernel; kernel_seconds is the tensor-core kernel alone"},
+                            "ff_integrated_via": plan.get("ff_via"),
+                            "ff_integrated_per_harmonic_rel_err_vs_plain": {"max": float(e_ff.max()),
+                                                                            "median": float(np.median(e_ff))},
+                            "includes": "plane tables + B operand + tensor-core kernel + FF_integrated (the z "
+                                        "trapezoid of the planes); kernel_seconds is the tensor-core kernel "
+                                        "alone"},
             "direct_fp32": {"seconds": t_dir, "per_harmonic_rel_err_vs_plain": {"max": float(e_dir.max()),
                                                                                  "median": float(e_dir.median())}},
             "plain_fp64": {"seconds": t_plain},
@@ -624,6 +632,7 @@ WORKLOADS = {
     "small_df": (16, 19, 2, 128),  # profiling case: 304 instances, two float-float CTAs per SM
     "small_wide": (8, 19, 2, 128),  # profiling case: grids of 9001-12001 sites (run_profile_case)
     "small_adjoint": (8, 19, 2, 128),  # profiling case: the adjoint on 16 short pulses (run_profile_case)
+    "small_ff": (8, 19, 2, 256),  # profiling case: config-3 far field with 256 frequencies (268 MB source)
 }
 
 
@@ -738,6 +747,7 @@ def run_ours(args, rank, world, precision):
 
     out = dict(value=value, ms_per_step=ms_step, S=S, n_inst=n_inst, kernel_ms=k_ms, peak=peak,
                cta_threads=int(grids.c64_threads[0]), m32=int(grids.m32[0]), autotune=autotune.last_report(),
+               dft=autotune.dft_choice(S),
                clocks=clk.summary(), e2e_ms=e2e_ms, h2d=host_fields.numel() * 8, d2h=d2h,
                t=t, fields=fields_np, spectrum=res["Fsourceterm"], omega=res["omegagrid"],
                sourceterm=res["sourceterm"])
@@ -801,6 +811,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-hankel", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the config-2 (uneven batch) and config-4 (adjoint) sub-lines of the default run")
+    ap.add_argument("--fd-samples", type=int, default=None,
+                    help="finite-difference samples per instance of the adjoint check (config 4: 32)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config1")
     ap.add_argument("--forms", choices=["all", "both", "fp64", "c64", "df64"], default="all",
                     help="all: FP64, complex64 and float-float; both: FP64 and complex64")
@@ -835,12 +849,12 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
-    if args.workload in ("config2", "config3", "config4", "analysis", "small_wide", "small_adjoint"):
+    if args.workload in ("config2", "config3", "config4", "analysis", "small_wide", "small_adjoint", "small_ff"):
         import torch
 
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
         torch.cuda.set_device(dev)
-        fn = {"config2": run_config2, "config3": run_hankel, "config4": run_config4,
+        fn = {"config2": run_config2, "config3": run_hankel, "small_ff": run_hankel, "config4": run_config4,
               "analysis": run_analysis, "small_wide": run_profile_case,
               "small_adjoint": run_profile_case}[args.workload]
         print(json.dumps({"workload": args.workload, "result": fn(args, dev)}))
@@ -898,6 +912,7 @@ def main():
                             "meets_plateau_target": err_c64["plateau_rel_err_max"] <= target},
         "plateau_target": "|F|^2 over H11-H41 within %g relative of the FP64 form (which equals the oracle "
                           "within 1e-8)" % target,
+        "spectrum_dft": dict(rdf["dft"], series_length=rdf["S"]),
     }
     line = {"metric": METRIC, "value": rdf["value"], "unit": "site-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": rdf["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -920,6 +935,17 @@ def main():
         import torch
 
         line["hankel"] = run_hankel(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
+    if not args.no_extra and args.workload == "config1":
+        import torch
+
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+        # the uneven batch (config 2: 4096 instances, one launch per form) and the adjoint
+        # (config 4: 256 instances, central finite differences at 4 samples per instance here;
+        # `--workload config4` checks 32)
+        line["config2"] = run_config2(args, dev)
+        if args.fd_samples is None:
+            args.fd_samples = 4
+        line["config4"] = run_config4(args, dev)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(r["t"], r["fields"], 4 * (os.cpu_count() or 1))
         if not args.no_hankel:

@@ -69,6 +69,11 @@ typedef struct mma_hankel_fast_plan_t {
 int mma_hankel_fast_plan(const double *zgrid_host, int64_t n_z, double distance, double omega_max, double r_max,
                          double rho_max, double tol, mma_hankel_fast_plan_t *plan);
 size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan);
+/* FF[rho][w] = sum_k tau_k planes[plane_slot[k]][rho][w] (tau: trapezoid weights of zgrid), the
+ * integrated far field from plane transforms already computed for every plane (plane_slot >= 0
+ * for all n_z planes; complex128 planes [slot][n_rho][n_omega], ff [n_rho][n_omega]). */
+int mma_hankel_ff_from_planes(const mma_hankel_problem *p, const double *zgrid, const int64_t *plane_slot,
+                              const double *planes, double *ff, void *stream);
 /* Status of the last mma_hankel_fast call on this scratch (synchronises the stream): MMA_OK, or
  * MMA_ERR_TIMEOUT if a bounded wait of its streamed stage 1 gave up (that call's far field is then
  * NaN).  The streamed stage 1 runs for complex64 sources with rows on 16-byte boundaries (even

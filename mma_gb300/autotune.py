@@ -1,6 +1,13 @@
-"""Autotuner of the batched TDSE's launch shape (the tuning step of the batching form).
+"""Autotuners of the batched TDSE's launch shapes (the tuning step of the batching form).
 
-The knob is the CTA size of the complex64 kernel, per grid size: 256 threads x M sites, 512 x M/2
+Two knobs are tuned by measurement:
+
+* the spectrum and interpolation DFTs' tiling, per transform length: the library's plan for a
+  length (``mma_dft_plan_info``, made on first use) times its shared-memory kernel at 256 and at
+  512 threads per row on a probe batch and keeps the faster; ``dft_choice(n)`` reports it;
+* the CTA size of the complex64 kernel, per grid size, which also sets the partition depth of its
+  tridiagonal solve (the sites per thread, M = n / CTA size, each thread's sequential sweep
+  length between the CTA-wide scans): 256 threads x M sites, 512 x M/2
 or 1024 x M/4 (where the grid fits the shared-memory kernel, n <= 8192 for 512 threads and
 n <= 8192 with M = 8 for 1024).  More threads per instance hide more latency (the kernel is
 latency-bound: three CTA-wide barriers per step, dependent sweeps); wider CTAs pay for wider
@@ -138,3 +145,25 @@ def choose_c64_threads(n, dt, param, device="cuda", retune=False):
 def last_report():
     """{cache key: {cta_threads: seconds}} of the tuning runs made by this process."""
     return {k: dict(v) for k, v in _LAST.items()}
+
+
+def dft_choice(n):
+    """The tiling the DFT plan of a length-n real transform runs: {'fft_len': complex FFT
+    length, 'bluestein': bool, 'cta_threads': 256 or 512 (one CTA per row, every pass in shared
+    memory; 0 = one launch per pass through global memory for FFT lengths above 7168),
+    'probe_ms': {threads: probe-batch ms}}.  Makes the plan on the current device if needed."""
+    import ctypes
+
+    from ._lib import load
+
+    lib = load()
+    lib.mma_dft_plan_info.argtypes = [ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3 + [
+        ctypes.POINTER(ctypes.c_float)]
+    lib.mma_dft_plan_info.restype = ctypes.c_int
+    m, b, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    ms = (ctypes.c_float * 2)()
+    rc = lib.mma_dft_plan_info(int(n), ctypes.byref(m), ctypes.byref(b), ctypes.byref(t), ms)
+    if rc != 0:
+        raise RuntimeError("mma_dft_plan_info failed with status %d" % rc)
+    return {"fft_len": m.value, "bluestein": bool(b.value), "cta_threads": t.value,
+            "probe_ms": {256: float(ms[0]), 512: float(ms[1])}}

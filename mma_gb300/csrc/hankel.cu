@@ -127,62 +127,83 @@ __global__ void fast_wr_tables(mma_hankel_problem P, const double* og, const dou
 
 // Stage 1 through a shared-memory ring, for complex64 sources whose rows start on 16-byte
 // boundaries (rows of an even number of radii at even strides) and pre-factors per (plane,
-// frequency).  One CTA per (frequency, 256 radii), one radius per thread.  Thread 0 streams each
-// plane's row of radii (2 KB) into a ring of `ns` stages with 1-D bulk copies, so that tens of
-// KB per SM are in flight whatever the register count: the stage of plane kz - kSlack is refilled
-// with plane kz - kSlack + ns once every warp has released it, which lets the warps drift
-// kSlack planes apart.  Every thread accumulates
+// frequency).  One CTA per (frequency, 256 radii), one radius per thread, two CTAs per SM.
+// Thread 0 streams the source with 1-D bulk copies (one per plane: the plane's row of radii,
+// 2 KB) into a ring of `ns` stages of kG planes each, one mbarrier per stage, so that tens of KB
+// per SM are in flight whatever the register count; the stage kSlack stages back is refilled
+// once every warp has released it, which lets the warps drift that far apart.  A thread waits
+// once per stage and then accumulates its kG planes (independent chains the scheduler can
+// interleave):
 //   B_m = sum_k tau_k v_k^m pre_k e^{-i k r^2/(2 D_k)} r w_r S_k,
 // with the near-field phase split as e^{-i k r^2 u_ref} e^{-i k r^2 (u_k - u_ref)} (u = 1/(2D)):
 // the first factor once per thread (float-float angle, reduced mod 2 pi), the second from the
-// small angle delta = k r^2 (u_k - u_ref) by its Taylor polynomials (|delta| <= 0.12; larger
-// angles take the exact reduction), and the 16-plane partial sums by packed FP32x2 FMAs.  Every
-// wait is bounded; on a timeout the CTA stops, sets *status and writes NaN into its B values.
+// small angle delta = k r^2 (u_k - u_ref) by its Taylor polynomials when every |delta| of the CTA
+// is within 0.12 (else the exact reduction per element; the choice is uniform over the CTA);
+// 16-plane partial sums by packed FP32x2 FMAs (coefficients stored as pairs in shared memory),
+// then their FP32 total.  Every wait is bounded; on a timeout the CTA stops, sets *status and
+// writes NaN into its B values.
 constexpr int kRingR = 256;  // radii per CTA, one per thread
-constexpr int kSlack = 8;    // planes the warps may drift apart
+constexpr int kG = 4;        // planes per ring stage
+constexpr int kSlack = 2;    // stages the warps may drift apart
 template <int MM>
-__global__ void __launch_bounds__(kRingR, 1)
+__global__ void __launch_bounds__(kRingR, 2)
     fast_stage1_ring(mma_hankel_problem P, const float2* __restrict__ src, const double2* __restrict__ pre,
                      const float* __restrict__ ptab, const float2* __restrict__ ktab,
                      const float4* __restrict__ rtab, float2 u_ref, float2* Bp, int ns, int* status)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ unsigned s_dumax;
     constexpr int RW = MM + 4;
-    const int64_t o = blockIdx.y, Nz = P.n_z, Nr = P.n_r, No = P.n_omega;
+    const int Nz = (int)P.n_z;
+    const int64_t o = blockIdx.y, Nr = P.n_r, No = P.n_omega;
     const int64_t r0 = (int64_t)blockIdx.x * kRingR;
     const int cnt = (int)(Nr - r0 < kRingR ? Nr - r0 : kRingR);
-    float2* ring = reinterpret_cast<float2*>(smem_raw);                  // ns x kRingR source values
-    float4* coef = reinterpret_cast<float4*>(ring + (size_t)ns * kRingR);  // Nz x MM/4: tau_k v_k^m
-    float4* pinfo = coef + Nz * (MM / 4);                                // Nz: (pre re, pre im, du, 0)
+    const int n_st = (Nz + kG - 1) / kG;  // stages of planes, the last possibly partial
+    float2* ring = reinterpret_cast<float2*>(smem_raw);                        // ns x kG x kRingR values
+    float4* coef = reinterpret_cast<float4*>(ring + (size_t)ns * kG * kRingR);  // Nz x MM/2: (c_m, c_m, c_m+1, c_m+1)
+    float4* pinfo = coef + Nz * (MM / 2);                                     // Nz: (pre re, pre im, du, 0)
     uint64_t* full = reinterpret_cast<uint64_t*>(pinfo + Nz);
     uint64_t* empty = full + ns;
     volatile int* abort_s = reinterpret_cast<volatile int*>(empty + ns);
     const int t = threadIdx.x, lane = t & 31;
     const uint32_t bytes = (uint32_t)cnt * 8u;
     const float2* row0 = src + o * P.omega_stride + r0;
+    // issue stage j (planes j kG ...) into ring slot `slot`: one copy per plane, one barrier
+    auto issue = [&](int j, int slot) {
+        const int k0 = j * kG, np = Nz - k0 < kG ? Nz - k0 : kG;
+        tc::mbar_arrive_expect_tx(&full[slot], bytes * (uint32_t)np);
+        for (int g = 0; g < np; g++)
+            tc::bulk_load_1d(ring + ((size_t)slot * kG + g) * kRingR, row0 + (int64_t)(k0 + g) * P.plane_stride,
+                             bytes, &full[slot]);
+    };
     if (t == 0) {
-        for (int s = 0; s < ns; s++) {
-            tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], kRingR / 32);
+        for (int q = 0; q < ns; q++) {
+            tc::mbar_init(&full[q], 1);
+            tc::mbar_init(&empty[q], kRingR / 32);
         }
         *abort_s = 0;
+        s_dumax = 0u;
         tc::fence_barrier_init();
-        for (int64_t kz = 0; kz < Nz && kz < ns; kz++) {  // the first ns planes, before the tables
-            tc::mbar_arrive_expect_tx(&full[kz], bytes);
-            tc::bulk_load_1d(ring + (size_t)kz * kRingR, row0 + kz * P.plane_stride, bytes, &full[kz]);
+        for (int j = 0; j < n_st && j < ns; j++) issue(j, j);  // the first stages, before the tables
+    }
+    for (int q = t; q < Nz * (MM / 2); q += blockDim.x) {
+        const float* row = ptab + (q / (MM / 2)) * RW + (q % (MM / 2)) * 2;
+        coef[q] = make_float4(row[0], row[0], row[1], row[1]);
+    }
+    __syncthreads();  // s_dumax initialised
+    {
+        unsigned mx = 0u;  // max |u_k - u_ref| as float bits (non-negative floats order as integers)
+        for (int q = t; q < Nz; q += blockDim.x) {
+            const double2 pf = pre ? pre[q * No + o] : make_double2(1.0, 0.0);
+            const float du = ptab[q * RW + MM + 2];
+            pinfo[q] = make_float4((float)pf.x, (float)pf.y, du, 0.f);
+            mx = max(mx, __float_as_uint(fabsf(du)));
         }
-    }
-    for (int64_t q = t; q < Nz * (MM / 4); q += blockDim.x) {
-        const float* row = ptab + (q / (MM / 4)) * RW + (q % (MM / 4)) * 4;
-        coef[q] = make_float4(row[0], row[1], row[2], row[3]);
-    }
-    for (int64_t q = t; q < Nz; q += blockDim.x) {
-        const double2 pf = pre ? pre[q * No + o] : make_double2(1.0, 0.0);
-        pinfo[q] = make_float4((float)pf.x, (float)pf.y, ptab[q * RW + MM + 2], 0.f);
+        atomicMax(&s_dumax, mx);
     }
     __syncthreads();
-    int64_t issued = Nz < ns ? Nz : ns;  // planes whose copies thread 0 has issued
-    // ---------------------------------------------------------------- consumers
+    int issued = n_st < ns ? n_st : ns;  // stages whose copies thread 0 has issued
+    // ---------------------------------------------------------------- per-thread constants
     const bool active = t < cnt;
     const int64_t r = r0 + (active ? t : 0);
     const float2 kk = ktab[o];
@@ -191,90 +212,108 @@ __global__ void __launch_bounds__(kRingR, 1)
     const float kr2h = kk.x * rt.x;
     const float kr2l = fmaf(kk.x, rt.x, -kr2h) + fmaf(kk.x, rt.y, kk.y * rt.x);
     float2 bw = make_float2(rt.z, 0.f);
-    if (P.near_field) {
+    const bool near = P.near_field != 0;
+    if (near) {
         const float th = kr2h * u_ref.x;
         const float te = fmaf(kr2h, u_ref.x, -th) + fmaf(kr2h, u_ref.y, kr2l * u_ref.x);
         float sn, cs;
         sincos_reduced(reduce_2pi(th, te), sn, cs);
         bw = make_float2(rt.z * cs, -rt.z * sn);
     }
-    float2 part[MM], hi[MM], lo[MM];
+    // near-field mode, uniform over the CTA: 0 none, 1 small angles, 2 exact reduction per element
+    const bool small = __syncthreads_and(fabsf(kr2h) * __uint_as_float(s_dumax) <= 0.12f);
+    const int mode = !near ? 0 : (small ? 1 : 2);
+    // two-level FP32 sums: 16-plane partials, then their total (two CTAs per SM fit in registers)
+    float2 part[MM], tot[MM];
 #pragma unroll
-    for (int m = 0; m < MM; m++) part[m] = hi[m] = lo[m] = make_float2(0.f, 0.f);
+    for (int m = 0; m < MM; m++) part[m] = tot[m] = make_float2(0.f, 0.f);
+    // one plane: A = pre S e^{-i theta} r w_r, then the MM partial sums
+    auto plane = [&](const float2 sv, const int kz, const int md) {
+        const float4 pi = pinfo[kz];
+        float2 a = make_float2(fmaf(pi.x, sv.x, -pi.y * sv.y), fmaf(pi.x, sv.y, pi.y * sv.x));
+        float2 e = bw;
+        if (md == 1) {
+            float sn, cs;
+            sincos_small(kr2h * pi.z, sn, cs);  // delta = k r^2 (u_k - u_ref)
+            e = make_float2(fmaf(bw.x, cs, bw.y * sn), fmaf(bw.y, cs, -bw.x * sn));
+        } else if (md == 2) {  // exact angle k r^2 u_k, as the direct stage 1
+            const float ih = ptab[kz * RW + MM], il = ptab[kz * RW + MM + 1];
+            const float th = kr2h * ih;
+            const float te = fmaf(kr2h, ih, -th) + fmaf(kr2h, il, kr2l * ih);
+            float sn, cs;
+            sincos_reduced(reduce_2pi(th, te), sn, cs);
+            e = make_float2(rt.z * cs, -rt.z * sn);
+        }
+        a = make_float2(fmaf(a.x, e.x, -a.y * e.y), fmaf(a.x, e.y, a.y * e.x));
+        const float4* c4 = coef + kz * (MM / 2);
+#pragma unroll
+        for (int m2 = 0; m2 < MM / 2; m2++) {
+            const float4 c = c4[m2];
+            part[2 * m2] = __ffma2_rn(make_float2(c.x, c.y), a, part[2 * m2]);
+            part[2 * m2 + 1] = __ffma2_rn(make_float2(c.z, c.w), a, part[2 * m2 + 1]);
+        }
+    };
     bool ok = true;
-    for (int64_t kz = 0; kz < Nz; kz++) {
-        const int s = (int)(kz % ns);
-        if (t == 0 && kz >= kSlack && issued < Nz) {
-            // refill the stage of plane kz - kSlack (released by every warp) with plane `issued`
-            const int64_t kp = kz - kSlack;
-            if (tc::mbar_wait(&empty[kp % ns], (uint32_t)(kp / ns) & 1u, abort_s, kRingWaitNs)) {
-                tc::mbar_arrive_expect_tx(&full[issued % ns], bytes);
-                tc::bulk_load_1d(ring + (size_t)(issued % ns) * kRingR, row0 + issued * P.plane_stride, bytes,
-                                 &full[issued % ns]);
-                issued++;
-            } else if (!*abort_s) {
-                *abort_s = 1;
-                atomicCAS(status, 0, 1);
+    // ring slot and phase parity of stage j (s, ph) and of stage j - kSlack (sp, php), counted
+    // incrementally (no divisions); stage `issued` = (j - kSlack) + ns reuses slot sp
+    int s = 0, sp = 0;
+    uint32_t ph = 0, php = 0;
+    for (int j = 0; j < n_st; j++) {
+        if (j >= kSlack) {
+            if (t == 0 && issued < n_st) {  // refill slot sp (stage j - kSlack, released by every warp)
+                if (tc::mbar_wait(&empty[sp], php, abort_s, kRingWaitNs)) {
+                    issue(issued, sp);
+                    issued++;
+                } else if (!*abort_s) {
+                    *abort_s = 1;
+                    atomicCAS(status, 0, 1);
+                }
+            }
+            if (++sp == ns) {
+                sp = 0;
+                php ^= 1u;
             }
         }
-        if (!tc::mbar_wait(&full[s], (uint32_t)(kz / ns) & 1u, abort_s, kRingWaitNs)) {
+        if (!tc::mbar_wait(&full[s], ph, abort_s, kRingWaitNs)) {
             *abort_s = 1;
             atomicCAS(status, 0, 2);
             ok = false;
             break;
         }
-        const float2 sv = active ? ring[(size_t)s * kRingR + t] : make_float2(0.f, 0.f);
+        const int k0 = j * kG;
+        float2 sv[kG];
+#pragma unroll
+        for (int g = 0; g < kG; g++) sv[g] = ring[((size_t)s * kG + g) * kRingR + t];  // rows beyond cnt: unused
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&empty[s]);
-        const float4 pi = pinfo[kz];
-        float2 a = make_float2(fmaf(pi.x, sv.x, -pi.y * sv.y), fmaf(pi.x, sv.y, pi.y * sv.x));
-        float2 e = bw;
-        if (P.near_field) {
-            const float d = kr2h * pi.z;  // k r^2 (u_k - u_ref)
-            float sn, cs;
-            if (fabsf(d) <= 0.12f) {
-                sincos_small(d, sn, cs);
-                e = make_float2(fmaf(bw.x, cs, bw.y * sn), fmaf(bw.y, cs, -bw.x * sn));
-            } else {  // exact angle k r^2 u_k, as the direct stage 1
-                const float ih = ptab[kz * RW + MM], il = ptab[kz * RW + MM + 1];
-                const float th = kr2h * ih;
-                const float te = fmaf(kr2h, ih, -th) + fmaf(kr2h, il, kr2l * ih);
-                sincos_reduced(reduce_2pi(th, te), sn, cs);
-                e = make_float2(rt.z * cs, -rt.z * sn);
-            }
-        }
-        a = make_float2(fmaf(a.x, e.x, -a.y * e.y), fmaf(a.x, e.y, a.y * e.x));
-        const float4* c4 = coef + kz * (MM / 4);
+        if (k0 + kG <= Nz && mode == 1) {  // the common case: kG independent chains, no control flow
 #pragma unroll
-        for (int m4 = 0; m4 < MM / 4; m4++) {
-            const float4 c = c4[m4];
-            part[4 * m4 + 0] = __ffma2_rn(make_float2(c.x, c.x), a, part[4 * m4 + 0]);
-            part[4 * m4 + 1] = __ffma2_rn(make_float2(c.y, c.y), a, part[4 * m4 + 1]);
-            part[4 * m4 + 2] = __ffma2_rn(make_float2(c.z, c.z), a, part[4 * m4 + 2]);
-            part[4 * m4 + 3] = __ffma2_rn(make_float2(c.w, c.w), a, part[4 * m4 + 3]);
-        }
-        if ((kz & 15) == 15 || kz == Nz - 1) {
+            for (int g = 0; g < kG; g++) plane(sv[g], k0 + g, 1);
+        } else {  // no near field, exact angles, or the last, partial stage (static indices keep sv in registers)
 #pragma unroll
-            for (int m = 0; m < MM; m++) {  // packed two-sum of (hi, part) into (hi, lo)
-                const float2 sm = __fadd2_rn(hi[m], part[m]);
-                const float2 bb = __fadd2_rn(sm, make_float2(-hi[m].x, -hi[m].y));
-                const float2 t1 = __fadd2_rn(sm, make_float2(-bb.x, -bb.y));
-                const float2 e1 = __fadd2_rn(hi[m], make_float2(-t1.x, -t1.y));
-                const float2 e2 = __fadd2_rn(part[m], make_float2(-bb.x, -bb.y));
-                lo[m] = __fadd2_rn(lo[m], __fadd2_rn(e1, e2));
-                hi[m] = sm;
+            for (int g = 0; g < kG; g++)
+                if (k0 + g < Nz) plane(sv[g], k0 + g, mode);
+        }
+        if (++s == ns) {
+            s = 0;
+            ph ^= 1u;
+        }
+        if ((j & (16 / kG - 1)) == 16 / kG - 1 || j == n_st - 1) {
+#pragma unroll
+            for (int m = 0; m < MM; m++) {
+                tot[m] = __fadd2_rn(tot[m], part[m]);
                 part[m] = make_float2(0.f, 0.f);
             }
         }
     }
     if (t == 0 && !ok)  // after an abort, let the copies already issued land before the CTA leaves
-        for (int64_t kz = (issued > ns ? issued - ns : 0); kz < issued; kz++)
-            tc::mbar_wait(&full[kz % ns], (uint32_t)(kz / ns) & 1u, nullptr, kRingWaitNs);
+        for (int j = (issued > ns ? issued - ns : 0); j < issued; j++)
+            tc::mbar_wait(&full[j % ns], (uint32_t)(j / ns) & 1u, nullptr, kRingWaitNs);
     if (!active) return;
     const float nan = __int_as_float(0x7fc00000);
 #pragma unroll
     for (int m = 0; m < MM; m++)
-        Bp[(o * MM + m) * Nr + r] = ok ? make_float2(hi[m].x + lo[m].x, hi[m].y + lo[m].y) : make_float2(nan, nan);
+        Bp[(o * MM + m) * Nr + r] = ok ? tot[m] : make_float2(nan, nan);
 }
 
 // z-contraction B_m[w, r] = sum_k tau_k v_k^m A_k[w, r]: one thread per (w, r), source read once,
@@ -621,13 +660,15 @@ template <int MM>
 int ring_stages(const mma_hankel_problem* p, const void* src)
 {
     if (p->source_c128 || p->pre_radial || (p->n_r & 1) || (p->omega_stride & 1) || (p->plane_stride & 1) ||
-        (reinterpret_cast<uintptr_t>(src) & 15) || (MM % 4) || MM > 32)
+        (reinterpret_cast<uintptr_t>(src) & 15) || (MM % 4) || MM > 16)
         return 0;
-    const size_t tables = (size_t)p->n_z * (MM * 4 + 16) + 64;
-    const size_t budget = 200 * 1024;
-    if (tables + 2 * kSlack * (kRingR * 8 + 16) > budget) return 0;
-    size_t ns = (budget - tables) / (kRingR * 8 + 16);
-    return (int)(ns > 64 ? 64 : ns);
+    // two CTAs per SM: at most ~110 KB of shared memory each
+    const size_t stage = (size_t)kG * kRingR * 8 + 16;
+    const size_t tables = (size_t)p->n_z * (MM * 8 + 16) + 64;
+    const size_t budget = 110 * 1024;
+    if (tables + 3 * kSlack * stage > budget) return 0;
+    const size_t ns = (budget - tables) / stage;
+    return (int)(ns > 16 ? 16 : ns);
 }
 
 template <int MM>
@@ -641,7 +682,7 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
         const int64_t nt = p->n_omega > p->n_r ? p->n_omega : p->n_r;
         fast_wr_tables<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(*p, og, rg, ktab, rtab);
         if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
-        const size_t sr = (size_t)ns * kRingR * 8 + (size_t)p->n_z * (MM * 4 + 16) + 2 * (size_t)ns * 8 + 16;
+        const size_t sr = (size_t)ns * kG * kRingR * 8 + (size_t)p->n_z * (MM * 8 + 16) + 2 * (size_t)ns * 8 + 16;
         cudaFuncSetAttribute(fast_stage1_ring<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr);
         float hi, lo;  // u_ref = 1/(2 d_ref) as a float pair
         const double u = 1.0 / (2.0 * plan->d_ref);
@@ -667,6 +708,35 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }
 }  // namespace
+
+// FF[rho, w] = sum_k tau_k P_k[rho, w] (the z trapezoid) from plane transforms already computed:
+// planes[slot[k]][rho][w], one thread per (rho, w), coalesced over w.
+__global__ void ff_from_planes_kernel(mma_hankel_problem P, const double* zg, const int64_t* slot,
+                                      const double2* planes, double2* ff)
+{
+    const int64_t Nz = P.n_z, No = P.n_omega, n = P.n_rho * No;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        double re = 0.0, im = 0.0;
+        for (int64_t k = 0; k < Nz; k++) {
+            const double tau = trap_w(zg, k, Nz);
+            const double2 v = planes[slot[k] * n + e];
+            re = fma(tau, v.x, re);
+            im = fma(tau, v.y, im);
+        }
+        ff[e] = make_double2(re, im);
+    }
+}
+
+extern "C" int mma_hankel_ff_from_planes(const mma_hankel_problem* p, const double* zgrid, const int64_t* plane_slot,
+                                         const double* planes, double* ff, void* stream)
+{
+    if (!valid(p) || !zgrid || !plane_slot || !planes || !ff) return MMA_ERR_ARG;
+    const int64_t n = p->n_rho * p->n_omega;
+    const int64_t b = (n + kThreads - 1) / kThreads;
+    ff_from_planes_kernel<<<(unsigned)(b < 65536 ? b : 65536), kThreads, 0, (cudaStream_t)stream>>>(
+        *p, zgrid, plane_slot, reinterpret_cast<const double2*>(planes), reinterpret_cast<double2*>(ff));
+    return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+}
 
 extern "C" int mma_hankel_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, const double* ogrid,
                                const double* rgrid, const double* zgrid, const double* rho, const void* source,

@@ -394,8 +394,9 @@ __global__ void rho_table(const double* og, const double* rho, double inv_cd, in
 constexpr int PREP_THREADS = 256;
 constexpr int PREP_PAIRS = 2;  // rpad <= 2 * 2 * 256 = 1024
 
-__global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, const double* og, const double* rg,
-                                                       const float2* dinv, const void* src, const double2* pre,
+__global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, float2 u_ref, const double* og,
+                                                       const double* rg, const float4* dinv, const void* src,
+                                                       const double2* pre,
                                                        __half* Bh, __half* Bl, float* alpha, int64_t rpad,
                                                        int64_t zpad)
 {
@@ -413,10 +414,12 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
     float kh, kl;
     split_d(og[o] / kC, kh, kl);
     float kr2h[2 * PREP_PAIRS], kr2l[2 * PREP_PAIRS], wr[2 * PREP_PAIRS];
+    float2 base[2 * PREP_PAIRS];  // e^{-i k r^2 u_ref} per radius (the near-field phase's reference part)
 #pragma unroll
     for (int i = 0; i < 2 * PREP_PAIRS; i++) {
         const int64_t r = 2 * (t + (int64_t)PREP_THREADS * (i / 2)) + (i & 1);
         kr2h[i] = kr2l[i] = wr[i] = 0.f;
+        base[i] = make_float2(1.f, 0.f);
         if (r < Nr) {
             const double rr = rg[r];
             float r2h, r2l;
@@ -424,8 +427,29 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
             kr2h[i] = kh * r2h;
             kr2l[i] = fmaf(kh, r2h, -kr2h[i]) + fmaf(kh, r2l, kl * r2h);
             wr[i] = (float)(trap_w(rg, r, Nr) * rr);
+            const float th = kr2h[i] * u_ref.x;
+            const float te = fmaf(kr2h[i], u_ref.x, -th) + fmaf(kr2h[i], u_ref.y, kr2l[i] * u_ref.x);
+            float sn, cs;
+            sincos_reduced(reduce_2pi(th, te), sn, cs);
+            base[i] = make_float2(cs, -sn);
         }
     }
+    // the phase e^{-i k r^2 u_k} = base e^{-i delta}, delta = k r^2 (u_k - u_ref): by Taylor
+    // polynomials when every |delta| of this CTA is within 0.12 (config 3: at most 0.033), else by
+    // the exact float-float reduction; the choice is uniform over the CTA
+    __shared__ unsigned s_dumax;
+    if (t == 0) s_dumax = 0u;
+    __syncthreads();
+    {
+        unsigned mx = 0u;
+        for (int64_t kz = t; kz < P.n_z; kz += PREP_THREADS) mx = max(mx, __float_as_uint(fabsf(dinv[kz].z)));
+        atomicMax(&s_dumax, mx);
+    }
+    __syncthreads();
+    float kmax = 0.f;
+#pragma unroll
+    for (int i = 0; i < 2 * PREP_PAIRS; i++) kmax = fmaxf(kmax, fabsf(kr2h[i]));
+    const bool small = __syncthreads_and(kmax * __uint_as_float(s_dumax) <= 0.12f);
     constexpr int PB = 4;  // planes per iteration: their loads are in flight together, one barrier for all
     for (int64_t kz0 = 0; kz0 < zpad; kz0 += PB) {
         float2 a[PB][2 * PREP_PAIRS];
@@ -447,7 +471,7 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
             const int64_t kz = kz0 + u;
             const bool live = kz < P.n_z;
             const float2 pr0 = pre_s[kz];
-            const float2 di = live ? dinv[kz] : make_float2(0.f, 0.f);
+            const float4 di = live ? dinv[kz] : make_float4(0.f, 0.f, 0.f, 0.f);
             mx[u] = 0.f;
 #pragma unroll
             for (int i = 0; i < 2 * PREP_PAIRS; i++) {
@@ -462,11 +486,18 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
                 }
                 float2 v = make_float2(fmaf(pr.x, sv.x, -pr.y * sv.y), fmaf(pr.x, sv.y, pr.y * sv.x));
                 if (P.near_field) {
-                    const float th = kr2h[i] * di.x;
-                    const float te = fmaf(kr2h[i], di.x, -th) + fmaf(kr2h[i], di.y, kr2l[i] * di.x);
                     float sn, cs;
-                    sincos_reduced(reduce_2pi(th, te), sn, cs);  // e^{-i theta}
-                    v = make_float2(fmaf(v.x, cs, v.y * sn), fmaf(v.y, cs, -v.x * sn));
+                    if (small) {  // e^{-i theta} = base e^{-i delta}
+                        sincos_small(kr2h[i] * di.z, sn, cs);
+                        const float2 e = make_float2(fmaf(base[i].x, cs, base[i].y * sn),
+                                                     fmaf(base[i].y, cs, -base[i].x * sn));
+                        v = make_float2(fmaf(v.x, e.x, -v.y * e.y), fmaf(v.x, e.y, v.y * e.x));
+                    } else {
+                        const float th = kr2h[i] * di.x;
+                        const float te = fmaf(kr2h[i], di.x, -th) + fmaf(kr2h[i], di.y, kr2l[i] * di.x);
+                        sincos_reduced(reduce_2pi(th, te), sn, cs);  // e^{-i theta}
+                        v = make_float2(fmaf(v.x, cs, v.y * sn), fmaf(v.y, cs, -v.x * sn));
+                    }
                 }
                 a[u][i] = make_float2(v.x * wr[i], v.y * wr[i]);  // zero beyond n_r (wr = 0, source 0)
                 mx[u] = fmaxf(mx[u], fmaxf(fabsf(a[u][i].x), fabsf(a[u][i].y)));
@@ -506,10 +537,11 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, con
     }
 }
 
-// per plane: dinv = 1/(2 D_k) as (hi, lo); ftab[k][m] = v_k^m / s_m = (v_k x)^m / m!, x = sigma y_max / 2;
+// per plane: dinv = (1/(2 D_k) as (hi, lo), 1/(2 D_k) - 1/(2 d_ref), 0); ftab[k][m] = v_k^m / s_m =
+// (v_k x)^m / m!, x = sigma y_max / 2;
 // per radius: rgf = r as float-float
 __global__ void plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, const double* zg, const double* rg,
-                            int mm, int64_t zpad, int64_t rpad, float2* dinv, float* ftab, float2* rgf)
+                            int mm, int64_t zpad, int64_t rpad, float4* dinv, float* ftab, float2* rgf)
 {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < rpad; q += (int64_t)gridDim.x * blockDim.x) {
         float hi, lo;
@@ -532,7 +564,7 @@ __global__ void plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, cons
         }
         float hi, lo;
         split_d(1.0 / (2.0 * D), hi, lo);
-        dinv[q] = make_float2(hi, lo);
+        dinv[q] = make_float4(hi, lo, (float)(1.0 / (2.0 * D) - 1.0 / (2.0 * F.d_ref)), 0.f);
     }
 }
 
@@ -679,7 +711,7 @@ bool layout(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, Lay
     L.off_alpha = L.off_bl + up256(nb);
     L.off_ftab = L.off_alpha + up256(sizeof(float) * p->n_omega * L.zpad);
     L.off_dinv = L.off_ftab + up256(sizeof(float) * L.zpad * L.mm);
-    L.off_rgf = L.off_dinv + up256(sizeof(float2) * L.zpad);
+    L.off_rgf = L.off_dinv + up256(sizeof(float4) * L.zpad);
     L.off_krho = L.off_rgf + up256(sizeof(float2) * L.rpad);
     L.off_status = L.off_krho + up256(sizeof(float2) * p->n_omega * p->n_rho);
     L.total = L.off_status + 256;
@@ -744,15 +776,21 @@ extern "C" int mma_hankel_planes_tc_prepare(const mma_hankel_problem* p, const m
     char* sc = static_cast<char*>(scratch);
     const int64_t nt = L.zpad > L.rpad ? L.zpad : L.rpad;
     plane_table<<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(*p, *plan, zgrid, rgrid, L.mm, L.zpad, L.rpad,
-                                                               reinterpret_cast<float2*>(sc + L.off_dinv),
+                                                               reinterpret_cast<float4*>(sc + L.off_dinv),
                                                                reinterpret_cast<float*>(sc + L.off_ftab),
                                                                reinterpret_cast<float2*>(sc + L.off_rgf));
     const size_t sp = sizeof(float2) * (size_t)L.zpad;
     if (sp > 48 * 1024 &&
         cudaFuncSetAttribute(prep_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp) != cudaSuccess)
         return MMA_ERR_CUDA;
+    float uh, ul;  // u_ref = 1/(2 d_ref) as a float pair
+    {
+        const double u = 1.0 / (2.0 * plan->d_ref);
+        uh = (float)u;
+        ul = (float)(u - (double)uh);
+    }
     prep_b<<<(unsigned)p->n_omega, PREP_THREADS, sp, st>>>(
-        *p, ogrid, rgrid, reinterpret_cast<const float2*>(sc + L.off_dinv), source,
+        *p, make_float2(uh, ul), ogrid, rgrid, reinterpret_cast<const float4*>(sc + L.off_dinv), source,
         reinterpret_cast<const double2*>(pre), reinterpret_cast<__half*>(sc + L.off_bh),
         reinterpret_cast<__half*>(sc + L.off_bl), reinterpret_cast<float*>(sc + L.off_alpha), L.rpad, L.zpad);
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;

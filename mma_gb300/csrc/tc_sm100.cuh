@@ -75,7 +75,9 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort,
                                           uint64_t limit_ns)
 {
-    if (mbar_test(bar, parity)) return true;
+#pragma unroll 1
+    for (int i = 0; i < 64; i++)  // the common short wait: no timer read
+        if (mbar_test(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (uint32_t i = 1;; i++) {
         if (mbar_test(bar, parity)) return true;

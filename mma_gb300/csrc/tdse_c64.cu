@@ -151,12 +151,16 @@ __device__ __forceinline__ void nan_outputs(const Args& P, const mma_tdse_instan
 }
 
 
+// The grid whose tables a CTA holds in shared memory (-1: none yet), common to every width.
+__shared__ int64_t c64_s_grid;
+
 // One instance of the register-resident form (T = 256 threads, M sites per thread): the
-// instance's tables are loaded into tab4 unless *s_grid says they are there already.
+// instance's tables are loaded into tab4 unless c64_s_grid says they are there already.
 template <int M>
-__device__ __forceinline__ void c64_reg_instance(const Args& P, const mma_tdse_instance& I, const mma_tdse_grid& G,
-                                                 float4* tab4, int64_t& s_grid)
+__device__ __forceinline__ void c64_reg_instance(const Args& P, const mma_tdse_instance& I, const mma_tdse_grid& G)
 {
+    extern __shared__ float4 tab4[];  // the kernel's dynamic shared memory (named here: shared loads)
+    int64_t& s_grid = c64_s_grid;
     __shared__ cf sc[2 * kWarps], sb[2 * kWarps];
     __shared__ float red_hi[kWarps * 4], red_lo[kWarps * 4];
     __shared__ cf bfirst[kWarps], blast[kWarps];
@@ -487,10 +491,9 @@ __device__ __forceinline__ void c64_reg_instance(const Args& P, const mma_tdse_i
 template <int M>
 __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
 {
-    extern __shared__ float4 tab4[];  // 256 * M sites x (1/beta re, im, V, psi0)
-    __shared__ int64_t s_inst, s_grid;
+    __shared__ int64_t s_inst;  // tables: 256 * M sites x (1/beta re, im, V, psi0) in dynamic shared memory
     const int t = threadIdx.x;
-    if (t == 0) s_grid = -1;
+    if (t == 0) c64_s_grid = -1;
     for (;;) {
         if (t == 0) s_inst = atomicAdd(P.counter, 1);
         __syncthreads();
@@ -502,7 +505,7 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
             nan_outputs(P, I, kThreads);
             continue;
         }
-        c64_reg_instance<M>(P, I, G, tab4, s_grid);
+        c64_reg_instance<M>(P, I, G);
     }
 }
 
@@ -521,11 +524,12 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_kernel(Args P)
 // exactly 0 there: the last row's super-diagonal then multiplies u_n = 0 and the first row's
 // sub-diagonal an incoming carry of 0, so the sweeps need no boundary tests.
 // One instance of the shared-memory form (T threads, M sites per thread): tables and psi in
-// tab4, the tables loaded unless *s_grid says they are there already.
+// tab4, the tables loaded unless c64_s_grid says they are there already.
 template <int M, int T>
-__device__ __forceinline__ void c64_smem_instance(const Args& P, const mma_tdse_instance& I, const mma_tdse_grid& G,
-                                                  float4* tab4, int64_t& s_grid)
+__device__ __forceinline__ void c64_smem_instance(const Args& P, const mma_tdse_instance& I, const mma_tdse_grid& G)
 {
+    extern __shared__ float4 tab4[];  // the kernel's dynamic shared memory (named here: shared loads)
+    int64_t& s_grid = c64_s_grid;
     constexpr int NW = T / 32;
     __shared__ cf sc[2 * NW], sb[2 * NW];
     __shared__ float red_hi[NW * 4], red_lo[NW * 4], red_pi[NW];
@@ -822,10 +826,9 @@ __device__ __forceinline__ void c64_smem_instance(const Args& P, const mma_tdse_
 template <int M, int T>  // 256 threads with M <= 16 fit twice on an SM (128 registers, <= 96 KB)
 __global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c64_smem_kernel(Args P)
 {
-    extern __shared__ float4 tab4[];  // L sites x (1/beta re, im, V, psi0), then psi [L] complex float
-    __shared__ int64_t s_inst, s_grid;
+    __shared__ int64_t s_inst;  // L sites x (1/beta re, im, V, psi0), then psi [L] complex float, dynamic
     const int t = threadIdx.x;
-    if (t == 0) s_grid = -1;
+    if (t == 0) c64_s_grid = -1;
     for (;;) {
         if (t == 0) s_inst = atomicAdd(P.counter, 1);
         __syncthreads();
@@ -837,8 +840,30 @@ __global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c6
             nan_outputs(P, I, T);
             continue;
         }
-        c64_smem_instance<M, T>(P, I, G, tab4, s_grid);
+        c64_smem_instance<M, T>(P, I, G);
     }
+}
+
+// The per-width bodies as separate (not inlined) functions for the width-dispatching kernel, so
+// that each width keeps its own register allocation instead of the union of all six.  The
+// records arrive by reference to the caller's stack; copies taken at entry keep their fields in
+// registers inside the step loop instead of reloading them from local memory.
+template <int M>
+__device__ __noinline__ void c64_smem_instance_ni(const Args& P_, const mma_tdse_instance& I_,
+                                                  const mma_tdse_grid& G_)
+{
+    const Args P = P_;
+    const mma_tdse_instance I = I_;
+    const mma_tdse_grid G = G_;
+    c64_smem_instance<M, kThreads>(P, I, G);
+}
+template <int M>
+__device__ __noinline__ void c64_reg_instance_ni(const Args& P_, const mma_tdse_instance& I_, const mma_tdse_grid& G_)
+{
+    const Args P = P_;
+    const mma_tdse_instance I = I_;
+    const mma_tdse_grid G = G_;
+    c64_reg_instance<M>(P, I, G);
 }
 
 // Uneven batches in one launch: instances of every 256-thread table width (8 to 48 sites per
@@ -848,10 +873,9 @@ __global__ void __launch_bounds__(T, (T == 256 && M <= 16) ? 2 : 1) propagate_c6
 // one CTA runs per SM.  A CTA that changes width reloads the tables (s_grid is common to all).
 __global__ void __launch_bounds__(kThreads, 1) propagate_c64_mixed_kernel(Args P)
 {
-    extern __shared__ float4 tab4[];
-    __shared__ int64_t s_inst, s_grid;
+    __shared__ int64_t s_inst;
     const int t = threadIdx.x;
-    if (t == 0) s_grid = -1;
+    if (t == 0) c64_s_grid = -1;
     for (;;) {
         if (t == 0) s_inst = atomicAdd(P.counter, 1);
         __syncthreads();
@@ -864,12 +888,12 @@ __global__ void __launch_bounds__(kThreads, 1) propagate_c64_mixed_kernel(Args P
             continue;
         }
         switch (G.m32) {
-        case 8: c64_smem_instance<8, kThreads>(P, I, G, tab4, s_grid); break;
-        case 16: c64_smem_instance<16, kThreads>(P, I, G, tab4, s_grid); break;
-        case 24: c64_smem_instance<24, kThreads>(P, I, G, tab4, s_grid); break;
-        case 32: c64_smem_instance<32, kThreads>(P, I, G, tab4, s_grid); break;
-        case 40: c64_reg_instance<40>(P, I, G, tab4, s_grid); break;
-        case 48: c64_reg_instance<48>(P, I, G, tab4, s_grid); break;
+        case 8: c64_smem_instance_ni<8>(P, I, G); break;
+        case 16: c64_smem_instance_ni<16>(P, I, G); break;
+        case 24: c64_smem_instance_ni<24>(P, I, G); break;
+        case 32: c64_smem_instance_ni<32>(P, I, G); break;
+        case 40: c64_reg_instance_ni<40>(P, I, G); break;
+        case 48: c64_reg_instance_ni<48>(P, I, G); break;
         default: nan_outputs(P, I, kThreads); break;
         }
     }

@@ -85,6 +85,10 @@ def _sig():
     lib.mma_hankel_planes_tc_run.restype = c_int
     lib.mma_hankel_planes_tc_status.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p]
     lib.mma_hankel_planes_tc_status.restype = c_int
+    lib.mma_hankel_ff_from_planes.argtypes = [P, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+    lib.mma_hankel_ff_from_planes.restype = c_int
+    lib.mma_hankel_fast_status.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p]
+    lib.mma_hankel_fast_status.restype = c_int
     lib._mma_hankel_sig = True
     return lib
 
@@ -425,14 +429,18 @@ TC_MIN_PLANES = 16  # from this many requested planes the fast form computes the
 
 
 def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_field=True, planes=(), form="plain",
-              tol=1e-9, stream=None, planes_via="auto", _events=None):
+              tol=1e-9, stream=None, planes_via="auto", ff_via="auto", _events=None):
     """Run the far-field kernels.  source: torch complex tensor [Nz, No, Nr] (on the GPU; a host
     tensor is copied there first).
     Returns (FF [Nrho, No] complex128 tensor, {plane: [Nrho, No] tensor}, fast plan dict or None).
 
     With form="fast", requested planes are computed either directly (one FP32 J0 per term,
     planes_via="direct") or by the tensor-core split-precision GEMM (planes_via="tc");
-    "auto" takes the tensor cores from TC_MIN_PLANES planes on, where the problem fits them."""
+    "auto" takes the tensor cores from TC_MIN_PLANES planes on, where the problem fits them.
+    FF_integrated comes from the fast form's z-first series (ff_via="fast"), or, when every plane
+    is computed on the tensor cores, as the z trapezoid of those planes (ff_via="planes": the
+    quantity the cumulative results end on, at the planes' accuracy, without the series pass);
+    "auto" takes "planes" in that case and "fast" otherwise."""
     lib = _sig()
     if not source.is_cuda:  # the kernels take device pointers only: a host source is copied first
         source = source.to(torch.device("cuda", torch.cuda.current_device()))
@@ -483,10 +491,16 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
                                                                       len(planes) >= TC_MIN_PLANES))
         if planes_via == "tc" and planes and ntc == 0:
             raise HankelError("the tensor-core plane form does not support this problem (n_r > 1024 or > 32 terms)")
-        _check(lib.mma_hankel_fast(ctypes.byref(prob), ctypes.byref(plan), og.data_ptr(), rg.data_ptr(), zg.data_ptr(),
-                                   rh.data_ptr(), S.data_ptr(), ptr(pre), ff.data_ptr(),
-                                   None if use_tc else ptr(slot), 0 if use_tc else len(planes),
-                                   None if use_tc else ptr(pl), scratch.data_ptr(), int(nb), st), "mma_hankel_fast")
+        if ff_via not in ("auto", "fast", "planes"):
+            raise ValueError("ff_via must be 'auto', 'fast' or 'planes'")
+        ff_planes = use_tc and len(planes) == Nz and ff_via in ("auto", "planes")
+        if ff_via == "planes" and not ff_planes:
+            raise HankelError("ff_via='planes' needs every plane computed on the tensor cores")
+        if not ff_planes:
+            _check(lib.mma_hankel_fast(ctypes.byref(prob), ctypes.byref(plan), og.data_ptr(), rg.data_ptr(),
+                                       zg.data_ptr(), rh.data_ptr(), S.data_ptr(), ptr(pre), ff.data_ptr(),
+                                       None if use_tc else ptr(slot), 0 if use_tc else len(planes),
+                                       None if use_tc else ptr(pl), scratch.data_ptr(), int(nb), st), "mma_hankel_fast")
         if use_tc:
             tcs = torch.empty(ntc, dtype=torch.uint8, device=dev)
             _check(lib.mma_hankel_planes_tc_prepare(ctypes.byref(prob), ctypes.byref(plan), og.data_ptr(),
@@ -499,10 +513,14 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
                                                 tcs.data_ptr(), ntc, st), "mma_hankel_planes_tc_run")
             if _events is not None:
                 _events[1].record(stream or torch.cuda.current_stream())
+            if ff_planes:
+                _check(lib.mma_hankel_ff_from_planes(ctypes.byref(prob), zg.data_ptr(), slot.data_ptr(), pl.data_ptr(),
+                                                     ff.data_ptr(), st), "mma_hankel_ff_from_planes")
             _check(lib.mma_hankel_planes_tc_status(ctypes.byref(prob), ctypes.byref(plan), tcs.data_ptr(), st),
                    "mma_hankel_planes_tc (kernel status)")
         plan_d = plan.as_dict()
         plan_d["planes_via"] = ("tc" if use_tc else "direct") if planes else None
+        plan_d["ff_via"] = "planes" if ff_planes else "fast"
     else:
         raise ValueError("form must be 'plain' or 'fast'")
     out_planes = {p: pl[i] for i, p in enumerate(planes)} if planes else {}
