@@ -335,14 +335,49 @@ def make_ionization(ref_root):
     print("ionization_h5", len(out), "arrays")
 
 
+LAYOUT_STRUCTS = ["Efield_var", "trg_def", "analy_def", "output_print_def", "inputs_def", "outputs_def"]
+
+
+def make_layout(ref_src):
+    """sizeof/offsetof of every field of the records in the reference's own
+    1DTDSE/sources/structures.h (a probe compiled against that header), with the field names
+    of this package's ctypes mirrors (the reference's names), kept as record_layout.json."""
+    import json
+    import subprocess
+    import tempfile
+
+    from mma_gb300 import structures as S
+
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "structures.h"', "int main(void){"]
+    for name in LAYOUT_STRUCTS:
+        cls = getattr(S, name)
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (name, name))
+        for f, _ in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (name, f, name, f))
+    lines.append("return 0;}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "probe.c")
+        open(c, "w").write("\n".join(lines))
+        exe = os.path.join(d, "probe")
+        subprocess.run(["gcc", "-I", ref_src, c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {k: int(v) for k, v in (l.split() for l in out if l.strip())}
+    json.dump({"source": "1DTDSE/sources/structures.h", "compiler": "gcc, this machine's x86-64 ABI",
+               "layout": got}, open(os.path.join(HERE, "record_layout.json"), "w"), indent=1, sort_keys=True)
+    print("record_layout", len(got), "entries")
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", required=True, help="the reference checkout (its top directory)")
-    ap.add_argument("--only", choices=["tdse", "hankel", "analysis", "xuv", "radial", "ionization"], default=None)
+    ap.add_argument("--only", choices=["tdse", "hankel", "analysis", "xuv", "radial", "ionization", "layout"],
+                    default=None)
     ap.add_argument("--case", action="append", help="with --only tdse: regenerate only these TDSE fixtures")
     a = ap.parse_args()
     if a.only in (None, "tdse"):
         make_tdse(os.path.join(a.ref, "1DTDSE", "sources"), only=a.case)
+    if a.only in (None, "layout"):
+        make_layout(os.path.join(a.ref, "1DTDSE", "sources"))
     if a.only in (None, "hankel"):
         make_hankel(a.ref)
     if a.only in (None, "analysis"):

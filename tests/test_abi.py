@@ -170,3 +170,104 @@ def test_batched_record_layouts_match_mirrors():
         assert int(got[cname]) == ctypes.sizeof(cls), cname
         for f, _ in cls._fields_:
             assert int(got[cname + "." + f]) == getattr(cls, f).offset, (cname, f)
+
+
+def _probe_layout(header_dir, header, names):
+    from mma_gb300 import structures as S
+
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "%s"' % header, "int main(void){"]
+    for name in names:
+        cls = getattr(S, name)
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (name, name))
+        for f, _ in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (name, f, name, f))
+    lines.append("return 0;}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "probe.c")
+        open(c, "w").write("\n".join(lines))
+        exe = os.path.join(d, "probe")
+        subprocess.run(["gcc", "-I", header_dir, c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    return {k: int(v) for k, v in (l.split() for l in out if l.strip())}
+
+
+def test_record_layout_matches_reference_header():
+    """The records' sizeof/offsetof as the reference's own 1DTDSE/sources/structures.h lays them
+    out (tests/golden/record_layout.json, from a probe compiled against that header by
+    tests/golden/make_golden.py --only layout) equal this repository's header and ctypes mirrors;
+    where the reference checkout is named by MMA_REF_SRC the probe is also rebuilt against it."""
+    import json
+
+    from mma_gb300 import structures as S
+
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "record_layout.json")))["layout"]
+    ours = _probe_layout(os.path.join(ROOT, "include"), "mma_tdse.h", STRUCTS)
+    assert ours == ref
+    for name in STRUCTS:
+        cls = getattr(S, name)
+        assert ref[name] == ctypes.sizeof(cls), name
+        for f, _ in cls._fields_:
+            assert ref[name + "." + f] == getattr(cls, f).offset, (name, f)
+    import oracle
+
+    src = oracle.ref_src()
+    if src is not None:
+        assert _probe_layout(src, "structures.h", STRUCTS) == ref
+
+
+def test_reference_host_class_binds_this_library():
+    """The reference's own, unmodified host class (1DTDSE/PythonTDSE.py and PythonCTDSE/*.py,
+    imported from the checkout named by MMA_REF_SRC; h5py, matplotlib and MMA_administration,
+    which this path does not use, stubbed) loads libmma_gb300.so: every symbol it binds
+    resolves, and its call sequence -- default inputs, field, ground state, propagation --
+    returns without exiting; with no GPU the library records MMA_ERR_NO_DEVICE (6) for the ground
+    state, and the propagation without a ground state is refused with a status."""
+    import importlib
+    import sys
+    import types
+
+    import oracle
+
+    top = oracle.ref_file("1DTDSE")
+    if top is None:
+        pytest.skip("the reference checkout is not named here (MMA_REF_SRC)")
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("checks the no-device path; the GPU tests cover the computation")
+    from mma_gb300._lib import lib_path
+
+    saved = dict(sys.modules)
+    saved_path = list(sys.path)
+    try:
+        for name in ("h5py", "matplotlib", "matplotlib.pyplot", "matplotlib.colors", "MMA_administration"):
+            sys.modules[name] = types.ModuleType(name)
+        sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]
+        sys.modules["matplotlib"].colors = sys.modules["matplotlib.colors"]
+        sys.modules["matplotlib.colors"].LogNorm = sys.modules["matplotlib.colors"].Normalize = object
+        for name in [m for m in sys.modules if m == "PythonTDSE" or m.startswith("PythonCTDSE")]:
+            del sys.modules[name]
+        sys.path.insert(0, top)
+        try:
+            PT = importlib.import_module("PythonTDSE")
+        except ImportError as e:
+            pytest.skip("the reference host class needs %s here" % e.name)
+        dll = PT.TDSE_DLL(lib_path())
+        for sym in ("Initialise_grid_and_ground_state", "call1DTDSE", "window_analysis", "GaborTransform",
+                    "free_mtrx", "free_arr", "outputs_destructor", "inputs_destructor", "set_time_and_field",
+                    "Set_all_prints"):
+            assert hasattr(dll.DLL, sym), sym
+        inp = PT.inputs_def()
+        inp.init_default_inputs(num_r=600, dx=0.4)
+        t = np.linspace(0.0, 50.0, 201)
+        inp.init_time_and_field(dll, E=0.05 * np.sin(0.057 * t), t=t)
+        out = PT.outputs_def()
+        dll.DLL.mma_last_error.restype = ctypes.c_int
+        dll.init_GS(inp)
+        assert dll.DLL.mma_last_error() == 6  # no device: reported, not exit()
+        dll.call1DTDSE(inp, out)
+        assert dll.DLL.mma_last_error() in (1, 6)  # no ground state (argument check) or no device
+    finally:
+        sys.modules.clear()
+        sys.modules.update(saved)
+        sys.path[:] = saved_path
