@@ -108,7 +108,7 @@ def run_config2(args, device):
     n_inst = 4096 if args.workload in ("config2", "config1") else 256
     params, fields, E0 = config2_instances(n_inst)
     t0 = time.perf_counter()
-    # 256-thread complex64 tables for every grid, so that every width goes in one launch
+    # 256-thread complex64 tables for every grid, so that the one-launch variant takes every width
     grids = TDSEGrids(params, dt=0.25, c64=True, df64=True)
     torch.cuda.synchronize()
     t_grids = time.perf_counter() - t0
@@ -116,10 +116,10 @@ def run_config2(args, device):
     out = {"instances": n_inst, "grid_build_s": t_grids, "site_steps": float(sum(
         (p["num_r"] + 1) * (len(f) + 2) for p, f in zip(params, fields)))}
     res = {}
-    for prec in ("df64", "c64", "c64_per_shape", "fp64"):
+    for prec in ("df64", "c64", "c64_one_launch", "fp64"):
         plan = TDSEBatchPlan(grids, [len(f) for f in fields], 0.25, grid_ids=np.arange(n_inst),
-                             precision="c64" if prec == "c64_per_shape" else prec,
-                             c64_one_launch=prec != "c64_per_shape")
+                             precision="c64" if prec == "c64_one_launch" else prec,
+                             c64_one_launch=prec == "c64_one_launch")
         plan.load_fields(tf)
         plan.capture()  # one eager run (DFT plans), then the graph
         if prec != "fp64":  # the FP64 form (18 s a batch) is timed on its first replay

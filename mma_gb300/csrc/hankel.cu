@@ -84,7 +84,8 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(mma_hankel_problem P, c
 // ------------------------------------------------------------------------ fast form, stage 1
 // Per-plane constants, independent of frequency, computed once per call (rows of MM + 4 floats):
 //   row[m] = tau_k v_k^m (m < MM),  row[MM], row[MM+1] = 1/(2 D_k) as (hi, lo),
-//   row[MM+2] = 1/(2 D_k) - 1/(2 d_ref) (the plane's offset from the reference distance), row[MM+3] = 0.
+//   row[MM+2], row[MM+3] = 1/(2 D_k) - 1/(2 d_ref) as (hi, lo) (the plane's offset from the
+//   reference distance).
 template <int MM>
 __global__ void fast_plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F, const double* zg, float* ptab)
 {
@@ -102,8 +103,9 @@ __global__ void fast_plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F,
         split_d(1.0 / (2.0 * D), hi, lo);
         row[MM] = hi;
         row[MM + 1] = lo;
-        row[MM + 2] = (float)(1.0 / (2.0 * D) - 1.0 / (2.0 * F.d_ref));
-        row[MM + 3] = 0.f;
+        split_d(1.0 / (2.0 * D) - 1.0 / (2.0 * F.d_ref), hi, lo);
+        row[MM + 2] = hi;
+        row[MM + 3] = lo;
     }
 }
 
@@ -134,14 +136,16 @@ __global__ void fast_wr_tables(mma_hankel_problem P, const double* og, const dou
 // once every warp has released it, which lets the warps drift that far apart.  A thread waits
 // once per stage and then accumulates its kG planes (independent chains the scheduler can
 // interleave):
-//   B_m = sum_k tau_k v_k^m pre_k e^{-i k r^2/(2 D_k)} r w_r S_k,
-// with the near-field phase split as e^{-i k r^2 u_ref} e^{-i k r^2 (u_k - u_ref)} (u = 1/(2D)):
-// the first factor once per thread (float-float angle, reduced mod 2 pi), the second from the
-// small angle delta = k r^2 (u_k - u_ref) by its Taylor polynomials when every |delta| of the CTA
-// is within 0.12 (else the exact reduction per element; the choice is uniform over the CTA);
-// 16-plane partial sums by packed FP32x2 FMAs (coefficients stored as pairs in shared memory),
-// then their FP32 total.  Every wait is bounded; on a timeout the CTA stops, sets *status and
-// writes NaN into its B values.
+//   B_m = e^{-i k r^2 u_ref} r w_r sum_k tau_k v_k^m pre_k e^{-i delta_k} S_k,
+//   delta_k = k r^2 (u_k - u_ref),  u = 1/(2 D),
+// i.e. the near-field phase e^{-i k r^2 u_k} split into a per-thread reference factor, applied
+// once to the finished sums together with r w_r, and the plane's offset from it.  e^{-i delta}
+// comes from Taylor polynomials when every |delta| of the CTA is within 0.12, else from the
+// float-float angle reduced mod 2 pi (the choice is uniform over the CTA).  The MM sums run as
+// real and imaginary pairs (B_m, B_m+1) in packed FP32x2 FMAs against coefficient pairs read as
+// float4 quads from shared memory; every 16 planes they are added into FP32 totals kept in
+// shared memory (each thread its own column), which leaves the registers to the partial sums.
+// Every wait is bounded; on a timeout the CTA stops, sets *status and writes NaN into its B values.
 constexpr int kRingR = 256;  // radii per CTA, one per thread
 constexpr int kG = 4;        // planes per ring stage
 constexpr int kSlack = 2;    // stages the warps may drift apart
@@ -151,17 +155,20 @@ __global__ void __launch_bounds__(kRingR, 2)
                      const float* __restrict__ ptab, const float2* __restrict__ ktab,
                      const float4* __restrict__ rtab, float2 u_ref, float2* Bp, int ns, int* status)
 {
+    static_assert(MM % 4 == 0 && MM <= 16, "ring stage 1 takes 4, 8, 12 or 16 terms");
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ unsigned s_dumax;
     constexpr int RW = MM + 4;
+    constexpr int MQ = MM / 4;  // coefficient quads per plane
     const int Nz = (int)P.n_z;
     const int64_t o = blockIdx.y, Nr = P.n_r, No = P.n_omega;
     const int64_t r0 = (int64_t)blockIdx.x * kRingR;
     const int cnt = (int)(Nr - r0 < kRingR ? Nr - r0 : kRingR);
     const int n_st = (Nz + kG - 1) / kG;  // stages of planes, the last possibly partial
     float2* ring = reinterpret_cast<float2*>(smem_raw);                        // ns x kG x kRingR values
-    float4* coef = reinterpret_cast<float4*>(ring + (size_t)ns * kG * kRingR);  // Nz x MM/2: (c_m, c_m, c_m+1, c_m+1)
-    float4* pinfo = coef + Nz * (MM / 2);                                     // Nz: (pre re, pre im, du, 0)
+    float4* tots = reinterpret_cast<float4*>(ring + (size_t)ns * kG * kRingR);  // 2 MQ x kRingR: re, im quads
+    float4* coef = tots + 2 * MQ * kRingR;                                     // Nz x MQ: c_4q .. c_4q+3
+    float4* pinfo = coef + Nz * MQ;                                            // Nz: (pre re, pre im, du hi, du lo)
     uint64_t* full = reinterpret_cast<uint64_t*>(pinfo + Nz);
     uint64_t* empty = full + ns;
     volatile int* abort_s = reinterpret_cast<volatile int*>(empty + ns);
@@ -186,18 +193,20 @@ __global__ void __launch_bounds__(kRingR, 2)
         tc::fence_barrier_init();
         for (int j = 0; j < n_st && j < ns; j++) issue(j, j);  // the first stages, before the tables
     }
-    for (int q = t; q < Nz * (MM / 2); q += blockDim.x) {
-        const float* row = ptab + (q / (MM / 2)) * RW + (q % (MM / 2)) * 2;
-        coef[q] = make_float4(row[0], row[0], row[1], row[1]);
+    for (int q = t; q < Nz * MQ; q += blockDim.x) {
+        const float* row = ptab + (q / MQ) * RW + (q % MQ) * 4;
+        coef[q] = make_float4(row[0], row[1], row[2], row[3]);
     }
+#pragma unroll
+    for (int q = 0; q < 2 * MQ; q++) tots[q * kRingR + t] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();  // s_dumax initialised
     {
         unsigned mx = 0u;  // max |u_k - u_ref| as float bits (non-negative floats order as integers)
         for (int q = t; q < Nz; q += blockDim.x) {
             const double2 pf = pre ? pre[q * No + o] : make_double2(1.0, 0.0);
-            const float du = ptab[q * RW + MM + 2];
-            pinfo[q] = make_float4((float)pf.x, (float)pf.y, du, 0.f);
-            mx = max(mx, __float_as_uint(fabsf(du)));
+            const float duh = ptab[q * RW + MM + 2], dul = ptab[q * RW + MM + 3];
+            pinfo[q] = make_float4((float)pf.x, (float)pf.y, duh, dul);
+            mx = max(mx, __float_as_uint(fabsf(duh)));
         }
         atomicMax(&s_dumax, mx);
     }
@@ -208,49 +217,41 @@ __global__ void __launch_bounds__(kRingR, 2)
     const int64_t r = r0 + (active ? t : 0);
     const float2 kk = ktab[o];
     const float4 rt = rtab[r];
-    // k r^2 as float-float, and the reference phase e^{-i k r^2 u_ref} times r w_r
+    // k r^2 as float-float
     const float kr2h = kk.x * rt.x;
     const float kr2l = fmaf(kk.x, rt.x, -kr2h) + fmaf(kk.x, rt.y, kk.y * rt.x);
-    float2 bw = make_float2(rt.z, 0.f);
     const bool near = P.near_field != 0;
-    if (near) {
-        const float th = kr2h * u_ref.x;
-        const float te = fmaf(kr2h, u_ref.x, -th) + fmaf(kr2h, u_ref.y, kr2l * u_ref.x);
-        float sn, cs;
-        sincos_reduced(reduce_2pi(th, te), sn, cs);
-        bw = make_float2(rt.z * cs, -rt.z * sn);
-    }
     // near-field mode, uniform over the CTA: 0 none, 1 small angles, 2 exact reduction per element
     const bool small = __syncthreads_and(fabsf(kr2h) * __uint_as_float(s_dumax) <= 0.12f);
     const int mode = !near ? 0 : (small ? 1 : 2);
-    // two-level FP32 sums: 16-plane partials, then their total (two CTAs per SM fit in registers)
-    float2 part[MM], tot[MM];
+    // partial sums of the current 16 planes: pr[j] = (Re B_2j, Re B_2j+1), pi[j] likewise imaginary
+    float2 pr[MM / 2], pim[MM / 2];
 #pragma unroll
-    for (int m = 0; m < MM; m++) part[m] = tot[m] = make_float2(0.f, 0.f);
-    // one plane: A = pre S e^{-i theta} r w_r, then the MM partial sums
+    for (int q = 0; q < MM / 2; q++) pr[q] = pim[q] = make_float2(0.f, 0.f);
+    // one plane: a = pre S e^{-i delta}, then the MM partial sums
     auto plane = [&](const float2 sv, const int kz, const int md) {
-        const float4 pi = pinfo[kz];
-        float2 a = make_float2(fmaf(pi.x, sv.x, -pi.y * sv.y), fmaf(pi.x, sv.y, pi.y * sv.x));
-        float2 e = bw;
-        if (md == 1) {
+        const float4 pf = pinfo[kz];
+        float2 a = make_float2(fmaf(pf.x, sv.x, -pf.y * sv.y), fmaf(pf.x, sv.y, pf.y * sv.x));
+        if (md != 0) {
             float sn, cs;
-            sincos_small(kr2h * pi.z, sn, cs);  // delta = k r^2 (u_k - u_ref)
-            e = make_float2(fmaf(bw.x, cs, bw.y * sn), fmaf(bw.y, cs, -bw.x * sn));
-        } else if (md == 2) {  // exact angle k r^2 u_k, as the direct stage 1
-            const float ih = ptab[kz * RW + MM], il = ptab[kz * RW + MM + 1];
-            const float th = kr2h * ih;
-            const float te = fmaf(kr2h, ih, -th) + fmaf(kr2h, il, kr2l * ih);
-            float sn, cs;
-            sincos_reduced(reduce_2pi(th, te), sn, cs);
-            e = make_float2(rt.z * cs, -rt.z * sn);
+            if (md == 1) {
+                sincos_small(kr2h * pf.z, sn, cs);
+            } else {  // the angle k r^2 (u_k - u_ref) in float-float, reduced mod 2 pi
+                const float th = kr2h * pf.z;
+                const float te = fmaf(kr2h, pf.z, -th) + fmaf(kr2h, pf.w, kr2l * pf.z);
+                sincos_reduced(reduce_2pi(th, te), sn, cs);
+            }
+            a = make_float2(fmaf(a.x, cs, a.y * sn), fmaf(a.y, cs, -a.x * sn));
         }
-        a = make_float2(fmaf(a.x, e.x, -a.y * e.y), fmaf(a.x, e.y, a.y * e.x));
-        const float4* c4 = coef + kz * (MM / 2);
+        const float2 ax = make_float2(a.x, a.x), ay = make_float2(a.y, a.y);
+        const float4* c4 = coef + kz * MQ;
 #pragma unroll
-        for (int m2 = 0; m2 < MM / 2; m2++) {
-            const float4 c = c4[m2];
-            part[2 * m2] = __ffma2_rn(make_float2(c.x, c.y), a, part[2 * m2]);
-            part[2 * m2 + 1] = __ffma2_rn(make_float2(c.z, c.w), a, part[2 * m2 + 1]);
+        for (int q = 0; q < MQ; q++) {
+            const float4 c = c4[q];
+            pr[2 * q] = __ffma2_rn(make_float2(c.x, c.y), ax, pr[2 * q]);
+            pr[2 * q + 1] = __ffma2_rn(make_float2(c.z, c.w), ax, pr[2 * q + 1]);
+            pim[2 * q] = __ffma2_rn(make_float2(c.x, c.y), ay, pim[2 * q]);
+            pim[2 * q + 1] = __ffma2_rn(make_float2(c.z, c.w), ay, pim[2 * q + 1]);
         }
     };
     bool ok = true;
@@ -261,7 +262,7 @@ __global__ void __launch_bounds__(kRingR, 2)
     for (int j = 0; j < n_st; j++) {
         if (j >= kSlack) {
             if (t == 0 && issued < n_st) {  // refill slot sp (stage j - kSlack, released by every warp)
-                if (tc::mbar_wait(&empty[sp], php, abort_s, kRingWaitNs)) {
+                if (tc::mbar_wait_spin(&empty[sp], php, abort_s, kRingWaitNs)) {
                     issue(issued, sp);
                     issued++;
                 } else if (!*abort_s) {
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(kRingR, 2)
                 php ^= 1u;
             }
         }
-        if (!tc::mbar_wait(&full[s], ph, abort_s, kRingWaitNs)) {
+        if (!tc::mbar_wait_spin(&full[s], ph, abort_s, kRingWaitNs)) {
             *abort_s = 1;
             atomicCAS(status, 0, 2);
             ok = false;
@@ -298,11 +299,19 @@ __global__ void __launch_bounds__(kRingR, 2)
             s = 0;
             ph ^= 1u;
         }
-        if ((j & (16 / kG - 1)) == 16 / kG - 1 || j == n_st - 1) {
+        if ((j & (16 / kG - 1)) == 16 / kG - 1 || j == n_st - 1) {  // add the 16-plane sums into the totals
 #pragma unroll
-            for (int m = 0; m < MM; m++) {
-                tot[m] = __fadd2_rn(tot[m], part[m]);
-                part[m] = make_float2(0.f, 0.f);
+            for (int q = 0; q < MQ; q++) {
+                float4* tr = tots + (2 * q) * kRingR + t;
+                float4* ti = tots + (2 * q + 1) * kRingR + t;
+                float4 vr = *tr, vi = *ti;
+                const float2 r01 = __fadd2_rn(make_float2(vr.x, vr.y), pr[2 * q]);
+                const float2 r23 = __fadd2_rn(make_float2(vr.z, vr.w), pr[2 * q + 1]);
+                const float2 i01 = __fadd2_rn(make_float2(vi.x, vi.y), pim[2 * q]);
+                const float2 i23 = __fadd2_rn(make_float2(vi.z, vi.w), pim[2 * q + 1]);
+                *tr = make_float4(r01.x, r01.y, r23.x, r23.y);
+                *ti = make_float4(i01.x, i01.y, i23.x, i23.y);
+                pr[2 * q] = pr[2 * q + 1] = pim[2 * q] = pim[2 * q + 1] = make_float2(0.f, 0.f);
             }
         }
     }
@@ -310,10 +319,26 @@ __global__ void __launch_bounds__(kRingR, 2)
         for (int j = (issued > ns ? issued - ns : 0); j < issued; j++)
             tc::mbar_wait(&full[j % ns], (uint32_t)(j / ns) & 1u, nullptr, kRingWaitNs);
     if (!active) return;
+    // the per-thread factor r w_r e^{-i k r^2 u_ref}
+    float2 bw = make_float2(rt.z, 0.f);
+    if (near) {
+        const float th = kr2h * u_ref.x;
+        const float te = fmaf(kr2h, u_ref.x, -th) + fmaf(kr2h, u_ref.y, kr2l * u_ref.x);
+        float sn, cs;
+        sincos_reduced(reduce_2pi(th, te), sn, cs);
+        bw = make_float2(rt.z * cs, -rt.z * sn);
+    }
     const float nan = __int_as_float(0x7fc00000);
 #pragma unroll
-    for (int m = 0; m < MM; m++)
-        Bp[(o * MM + m) * Nr + r] = ok ? tot[m] : make_float2(nan, nan);
+    for (int q = 0; q < MQ; q++) {
+        const float4 vr = tots[(2 * q) * kRingR + t], vi = tots[(2 * q + 1) * kRingR + t];
+        const float re[4] = {vr.x, vr.y, vr.z, vr.w}, im[4] = {vi.x, vi.y, vi.z, vi.w};
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const float2 b = make_float2(fmaf(bw.x, re[u], -bw.y * im[u]), fmaf(bw.x, im[u], bw.y * re[u]));
+            Bp[(o * MM + 4 * q + u) * Nr + r] = ok ? b : make_float2(nan, nan);
+        }
+    }
 }
 
 // z-contraction B_m[w, r] = sum_k tau_k v_k^m A_k[w, r]: one thread per (w, r), source read once,
@@ -664,7 +689,7 @@ int ring_stages(const mma_hankel_problem* p, const void* src)
         return 0;
     // two CTAs per SM: at most ~110 KB of shared memory each
     const size_t stage = (size_t)kG * kRingR * 8 + 16;
-    const size_t tables = (size_t)p->n_z * (MM * 8 + 16) + 64;
+    const size_t tables = (size_t)p->n_z * (MM * 4 + 16) + (size_t)MM * 8 * kRingR + 64;
     const size_t budget = 110 * 1024;
     if (tables + 3 * kSlack * stage > budget) return 0;
     const size_t ns = (budget - tables) / stage;
@@ -677,21 +702,27 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
                 float2* Bp, float* ptab, float2* ktab, float4* rtab, int* status, cudaStream_t st)
 {
     fast_plane_table<MM><<<(unsigned)((p->n_z + 127) / 128), 128, 0, st>>>(*p, *plan, zg, ptab);
-    const int ns = ring_stages<MM>(p, src);
-    if (ns > 0) {  // stage 1 through the shared-memory ring
-        const int64_t nt = p->n_omega > p->n_r ? p->n_omega : p->n_r;
-        fast_wr_tables<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(*p, og, rg, ktab, rtab);
-        if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
-        const size_t sr = (size_t)ns * kG * kRingR * 8 + (size_t)p->n_z * (MM * 8 + 16) + 2 * (size_t)ns * 8 + 16;
-        cudaFuncSetAttribute(fast_stage1_ring<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr);
-        float hi, lo;  // u_ref = 1/(2 d_ref) as a float pair
-        const double u = 1.0 / (2.0 * plan->d_ref);
-        hi = (float)u;
-        lo = (float)(u - (double)hi);
-        dim3 g1((unsigned)((p->n_r + kRingR - 1) / kRingR), (unsigned)p->n_omega);
-        fast_stage1_ring<MM><<<g1, kRingR, sr, st>>>(*p, static_cast<const float2*>(src), pre, ptab, ktab, rtab,
-                                                           make_float2(hi, lo), Bp, ns, status);
-    } else {  // one thread per (frequency, radius) reading its planes directly
+    bool ringed = false;
+    if constexpr (MM % 4 == 0 && MM <= 16) {
+        const int ns = ring_stages<MM>(p, src);
+        if (ns > 0) {  // stage 1 through the shared-memory ring
+            ringed = true;
+            const int64_t nt = p->n_omega > p->n_r ? p->n_omega : p->n_r;
+            fast_wr_tables<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(*p, og, rg, ktab, rtab);
+            if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+            const size_t sr = (size_t)ns * kG * kRingR * 8 + (size_t)MM * 8 * kRingR +
+                              (size_t)p->n_z * (MM * 4 + 16) + 2 * (size_t)ns * 8 + 16;
+            cudaFuncSetAttribute(fast_stage1_ring<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr);
+            float hi, lo;  // u_ref = 1/(2 d_ref) as a float pair
+            const double u = 1.0 / (2.0 * plan->d_ref);
+            hi = (float)u;
+            lo = (float)(u - (double)hi);
+            dim3 g1((unsigned)((p->n_r + kRingR - 1) / kRingR), (unsigned)p->n_omega);
+            fast_stage1_ring<MM><<<g1, kRingR, sr, st>>>(*p, static_cast<const float2*>(src), pre, ptab, ktab,
+                                                         rtab, make_float2(hi, lo), Bp, ns, status);
+        }
+    }
+    if (!ringed) {  // one thread per (frequency, radius) reading its planes directly
         const size_t s1 =
             sizeof(float) * (((size_t)p->n_z * (MM + 4) + 1) / 2 * 2) + sizeof(float2) * (size_t)p->n_z;
         if (s1 > 200 * 1024) return MMA_ERR_TOO_LARGE;
@@ -710,21 +741,47 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
 }  // namespace
 
 // FF[rho, w] = sum_k tau_k P_k[rho, w] (the z trapezoid) from plane transforms already computed:
-// planes[slot[k]][rho][w], one thread per (rho, w), coalesced over w.
-__global__ void ff_from_planes_kernel(mma_hankel_problem P, const double* zg, const int64_t* slot,
-                                      const double2* planes, double2* ff)
+// planes[slot[k]][rho][w], one thread per (rho, w), coalesced over w.  The CTA stages the planes'
+// offsets and weights in shared memory, and each thread keeps eight plane loads in flight (the
+// kernel streams all planes once, so it is HBM-bound).
+constexpr int kFfChunk = 512;
+__global__ void __launch_bounds__(kThreads) ff_from_planes_kernel(mma_hankel_problem P, const double* zg,
+                                                                 const int64_t* slot, const double2* planes,
+                                                                 double2* ff)
 {
-    const int64_t Nz = P.n_z, No = P.n_omega, n = P.n_rho * No;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-        double re = 0.0, im = 0.0;
-        for (int64_t k = 0; k < Nz; k++) {
-            const double tau = trap_w(zg, k, Nz);
-            const double2 v = planes[slot[k] * n + e];
-            re = fma(tau, v.x, re);
-            im = fma(tau, v.y, im);
+    __shared__ int64_t s_off[kFfChunk];
+    __shared__ double s_tau[kFfChunk];
+    const int64_t Nz = P.n_z, n = P.n_rho * P.n_omega;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double re = 0.0, im = 0.0;
+    for (int64_t k0 = 0; k0 < Nz; k0 += kFfChunk) {
+        const int nk = (int)(Nz - k0 < kFfChunk ? Nz - k0 : kFfChunk);
+        __syncthreads();
+        for (int q = threadIdx.x; q < nk; q += blockDim.x) {
+            s_off[q] = slot[k0 + q] * n;
+            s_tau[q] = trap_w(zg, k0 + q, Nz);
         }
-        ff[e] = make_double2(re, im);
+        __syncthreads();
+        if (e < n) {
+            int q = 0;
+            for (; q + 8 <= nk; q += 8) {
+                double2 v[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) v[u] = __ldcs(planes + s_off[q + u] + e);
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    re = fma(s_tau[q + u], v[u].x, re);
+                    im = fma(s_tau[q + u], v[u].y, im);
+                }
+            }
+            for (; q < nk; q++) {
+                const double2 v = __ldcs(planes + s_off[q] + e);
+                re = fma(s_tau[q], v.x, re);
+                im = fma(s_tau[q], v.y, im);
+            }
+        }
     }
+    if (e < n) ff[e] = make_double2(re, im);
 }
 
 extern "C" int mma_hankel_ff_from_planes(const mma_hankel_problem* p, const double* zgrid, const int64_t* plane_slot,
@@ -733,7 +790,8 @@ extern "C" int mma_hankel_ff_from_planes(const mma_hankel_problem* p, const doub
     if (!valid(p) || !zgrid || !plane_slot || !planes || !ff) return MMA_ERR_ARG;
     const int64_t n = p->n_rho * p->n_omega;
     const int64_t b = (n + kThreads - 1) / kThreads;
-    ff_from_planes_kernel<<<(unsigned)(b < 65536 ? b : 65536), kThreads, 0, (cudaStream_t)stream>>>(
+    if (b > INT32_MAX) return MMA_ERR_TOO_LARGE;
+    ff_from_planes_kernel<<<(unsigned)b, kThreads, 0, (cudaStream_t)stream>>>(
         *p, zgrid, plane_slot, reinterpret_cast<const double2*>(planes), reinterpret_cast<double2*>(ff));
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }

@@ -394,7 +394,7 @@ __global__ void rho_table(const double* og, const double* rho, double inv_cd, in
 constexpr int PREP_THREADS = 256;
 constexpr int PREP_PAIRS = 2;  // rpad <= 2 * 2 * 256 = 1024
 
-__global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, float2 u_ref, const double* og,
+__global__ void __launch_bounds__(PREP_THREADS, 2) prep_b(mma_hankel_problem P, float2 u_ref, const double* og,
                                                        const double* rg, const float4* dinv, const void* src,
                                                        const double2* pre,
                                                        __half* Bh, __half* Bl, float* alpha, int64_t rpad,
@@ -450,22 +450,33 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, flo
 #pragma unroll
     for (int i = 0; i < 2 * PREP_PAIRS; i++) kmax = fmaxf(kmax, fabsf(kr2h[i]));
     const bool small = __syncthreads_and(kmax * __uint_as_float(s_dumax) <= 0.12f);
-    constexpr int PB = 4;  // planes per iteration: their loads are in flight together, one barrier for all
-    for (int64_t kz0 = 0; kz0 < zpad; kz0 += PB) {
-        float2 a[PB][2 * PREP_PAIRS];
-        float mx[PB];
+    // planes per iteration: their loads are in flight together, one barrier for all; the next
+    // iteration's loads are issued before this one's arithmetic, barrier and stores
+    constexpr int PB = 4;
+    auto load_planes = [&](float2 (&dst)[PB][2 * PREP_PAIRS], int64_t k0) {
 #pragma unroll
         for (int u = 0; u < PB; u++) {
-            const int64_t kz = kz0 + u;
+            const int64_t kz = k0 + u;
             const bool live = kz < P.n_z;
 #pragma unroll
             for (int i = 0; i < 2 * PREP_PAIRS; i++) {
                 const int64_t r = 2 * (t + (int64_t)PREP_THREADS * (i / 2)) + (i & 1);
-                a[u][i] = (live && r < Nr) ? load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r,
-                                                        P.source_c128)
-                                           : make_float2(0.f, 0.f);
+                dst[u][i] = (live && r < Nr) ? load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r,
+                                                          P.source_c128)
+                                             : make_float2(0.f, 0.f);
             }
         }
+    };
+    float2 nx[PB][2 * PREP_PAIRS];
+    load_planes(nx, 0);
+    for (int64_t kz0 = 0; kz0 < zpad; kz0 += PB) {
+        float2 a[PB][2 * PREP_PAIRS];
+        float mx[PB];
+#pragma unroll
+        for (int u = 0; u < PB; u++)
+#pragma unroll
+            for (int i = 0; i < 2 * PREP_PAIRS; i++) a[u][i] = nx[u][i];
+        load_planes(nx, kz0 + PB);  // planes beyond n_z load as zeros
 #pragma unroll
         for (int u = 0; u < PB; u++) {
             const int64_t kz = kz0 + u;

@@ -75,9 +75,7 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort,
                                           uint64_t limit_ns)
 {
-#pragma unroll 1
-    for (int i = 0; i < 64; i++)  // the common short wait: no timer read
-        if (mbar_test(bar, parity)) return true;
+    if (mbar_test(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (uint32_t i = 1;; i++) {
         if (mbar_test(bar, parity)) return true;
@@ -96,6 +94,17 @@ __device__ __forceinline__ void bulk_load_1d(void* dst, const void* src, uint32_
                      smem_u32(dst)),
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
+}
+
+// mbar_wait for waits that are usually short and frequent (once per ring stage per thread): up to
+// 64 tests before the first read of the global timer
+__device__ __forceinline__ bool mbar_wait_spin(uint64_t* bar, uint32_t parity, const volatile int* abort,
+                                               uint64_t limit_ns)
+{
+#pragma unroll 1
+    for (int i = 0; i < 64; i++)
+        if (mbar_test(bar, parity)) return true;
+    return mbar_wait(bar, parity, abort, limit_ns);
 }
 
 // L1 prefetch hint for an address inside an allocation

@@ -284,11 +284,12 @@ class TDSEBatchPlan:
 
     ``launch()`` issues the whole device pipeline -- Fourier interpolation of the
     fields (one batched DFT pair per field length), the persistent propagation kernel
-    (one launch for the whole batch: the FP64 and float-float kernels take any grid
-    width, and complex64 batches of several 256-thread table widths run the
-    width-dispatching kernel; ``c64_one_launch=False`` or grids with other CTA sizes give
-    one complex64 launch per table shape), the output spectra (one batch per series
-    length) -- on one
+    (the FP64 and float-float kernels take any grid width, so one launch runs the whole
+    batch; complex64 batches run one launch per table shape, or, with
+    ``c64_one_launch=True`` and 256-thread tables for every grid, one launch of the
+    width-dispatching kernel, which is correct but slower: its register-resident widths
+    spill more as called functions than as their own kernels), the output spectra (one
+    batch per series length) -- on one
     stream, with no host synchronisation, so ``capture()`` can record it as a CUDA
     graph and ``replay()`` re-runs it on new fields written by ``load_fields``.
 
@@ -298,7 +299,7 @@ class TDSEBatchPlan:
     """
 
     def __init__(self, grids, n_field, dt_field, grid_ids=None, dt_req=None, tmin=0.0, precision="fp64",
-                 spectra=True, psi_final=False, snap_every=0, tmax=None, grid_ctas=0, c64_one_launch=True):
+                 spectra=True, psi_final=False, snap_every=0, tmax=None, grid_ctas=0, c64_one_launch=False):
         lib = _sig()
         self.lib = lib
         if precision not in PRECISIONS:
