@@ -53,6 +53,7 @@ constexpr uint32_t B_BYTES = NCOL * KB * 2; // hi or lo: 16 KB
 constexpr uint32_t B_OFF = 2 * A_BYTES;
 constexpr uint32_t STAGE_BYTES = B_OFF + 2 * B_BYTES;  // 48 KB
 constexpr uint64_t WAIT_NS = 2000000000ull;             // 2 s per wait
+constexpr uint64_t kPrepWaitNs = 2000000000ull;         // 2 s per ring wait of the B preparation
 
 struct Params {
     int64_t n_omega, n_r, n_z, n_rho;
@@ -394,7 +395,7 @@ __global__ void rho_table(const double* og, const double* rho, double inv_cd, in
 constexpr int PREP_THREADS = 256;
 constexpr int PREP_PAIRS = 2;  // rpad <= 2 * 2 * 256 = 1024
 
-__global__ void __launch_bounds__(PREP_THREADS, 2) prep_b(mma_hankel_problem P, float2 u_ref, const double* og,
+__global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, float2 u_ref, const double* og,
                                                        const double* rg, const float4* dinv, const void* src,
                                                        const double2* pre,
                                                        __half* Bh, __half* Bl, float* alpha, int64_t rpad,
@@ -450,33 +451,22 @@ __global__ void __launch_bounds__(PREP_THREADS, 2) prep_b(mma_hankel_problem P, 
 #pragma unroll
     for (int i = 0; i < 2 * PREP_PAIRS; i++) kmax = fmaxf(kmax, fabsf(kr2h[i]));
     const bool small = __syncthreads_and(kmax * __uint_as_float(s_dumax) <= 0.12f);
-    // planes per iteration: their loads are in flight together, one barrier for all; the next
-    // iteration's loads are issued before this one's arithmetic, barrier and stores
-    constexpr int PB = 4;
-    auto load_planes = [&](float2 (&dst)[PB][2 * PREP_PAIRS], int64_t k0) {
-#pragma unroll
-        for (int u = 0; u < PB; u++) {
-            const int64_t kz = k0 + u;
-            const bool live = kz < P.n_z;
-#pragma unroll
-            for (int i = 0; i < 2 * PREP_PAIRS; i++) {
-                const int64_t r = 2 * (t + (int64_t)PREP_THREADS * (i / 2)) + (i & 1);
-                dst[u][i] = (live && r < Nr) ? load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r,
-                                                          P.source_c128)
-                                             : make_float2(0.f, 0.f);
-            }
-        }
-    };
-    float2 nx[PB][2 * PREP_PAIRS];
-    load_planes(nx, 0);
+    constexpr int PB = 4;  // planes per iteration: their loads are in flight together, one barrier for all
     for (int64_t kz0 = 0; kz0 < zpad; kz0 += PB) {
         float2 a[PB][2 * PREP_PAIRS];
         float mx[PB];
 #pragma unroll
-        for (int u = 0; u < PB; u++)
+        for (int u = 0; u < PB; u++) {
+            const int64_t kz = kz0 + u;
+            const bool live = kz < P.n_z;
 #pragma unroll
-            for (int i = 0; i < 2 * PREP_PAIRS; i++) a[u][i] = nx[u][i];
-        load_planes(nx, kz0 + PB);  // planes beyond n_z load as zeros
+            for (int i = 0; i < 2 * PREP_PAIRS; i++) {
+                const int64_t r = 2 * (t + (int64_t)PREP_THREADS * (i / 2)) + (i & 1);
+                a[u][i] = (live && r < Nr) ? load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r,
+                                                        P.source_c128)
+                                           : make_float2(0.f, 0.f);
+            }
+        }
 #pragma unroll
         for (int u = 0; u < PB; u++) {
             const int64_t kz = kz0 + u;
@@ -542,6 +532,217 @@ __global__ void __launch_bounds__(PREP_THREADS, 2) prep_b(mma_hankel_problem P, 
                     const int64_t idx = ((o * 2 * zpad + 2 * kz + c) * rpad + r0) / 2;
                     reinterpret_cast<__half2*>(Bh)[idx] = __halves2half2(h0, h1);
                     reinterpret_cast<__half2*>(Bl)[idx] = __halves2half2(l0, l1);
+                }
+            }
+        }
+    }
+}
+
+// The same B operand for complex64 sources whose plane rows start on 16-byte boundaries (an even
+// number of radii at even strides) and pre-factors per (plane, frequency): thread 0 streams the
+// frequency's rows into a shared-memory ring (one 1-D bulk copy per plane, kPrepG planes per
+// stage, one mbarrier per stage), so the loads stay in flight across the per-stage barrier that
+// the row scales need.  Each thread owns two radius pairs and carries every per-radius quantity
+// as a pair, so the arithmetic runs in packed FP32x2 instructions: the same operations in the
+// same order as prep_b, hence the same B operand bit for bit.  The wait for a stage is bounded;
+// on a timeout the CTA sets *status, lets its copies land and writes NaN row scales.
+constexpr int kPrepG = 4;  // planes per ring stage
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__global__ void __launch_bounds__(PREP_THREADS, 2)
+    prep_b_ring(mma_hankel_problem P, float2 u_ref, const double* og, const double* rg, const float4* dinv,
+                const float2* __restrict__ src, const double2* __restrict__ pre, __half* Bh, __half* Bl,
+                float* alpha, int64_t rpad, int64_t zpad, int ns, int* status)
+{
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ float wmax[2][kPrepG][PREP_THREADS / 32];  // double-buffered by stage parity
+    __shared__ unsigned s_dumax;
+    const int64_t o = blockIdx.x, Nr = P.n_r, No = P.n_omega;
+    const int Nz = (int)P.n_z;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    float2* ring = reinterpret_cast<float2*>(smem_raw);                      // ns x kPrepG x rpad
+    float4* pinfo = reinterpret_cast<float4*>(ring + (size_t)ns * kPrepG * rpad);  // zpad: (pre, du, 0)
+    uint64_t* full = reinterpret_cast<uint64_t*>(pinfo + zpad);
+    const int n_st = (int)((zpad + kPrepG - 1) / kPrepG);  // stages over the padded planes
+    const int n_live = (Nz + kPrepG - 1) / kPrepG;         // stages with source rows to copy
+    const uint32_t row_bytes = (uint32_t)Nr * 8u;
+    const float2* row0 = src + o * P.omega_stride;
+    auto issue = [&](int j, int slot) {
+        const int k0 = j * kPrepG, np = Nz - k0 < kPrepG ? Nz - k0 : kPrepG;
+        tc::mbar_arrive_expect_tx(&full[slot], row_bytes * (uint32_t)np);
+        for (int g = 0; g < np; g++)
+            tc::bulk_load_1d(ring + ((size_t)slot * kPrepG + g) * rpad, row0 + (int64_t)(k0 + g) * P.plane_stride,
+                             row_bytes, &full[slot]);
+    };
+    if (t == 0) {
+        for (int q = 0; q < ns; q++) tc::mbar_init(&full[q], 1);
+        s_dumax = 0u;
+        tc::fence_barrier_init();
+        for (int j = 0; j < n_live && j < ns; j++) issue(j, j);
+    }
+    __syncthreads();
+    {
+        unsigned mx = 0u;
+        for (int64_t kz = t; kz < zpad; kz += PREP_THREADS) {
+            const bool live = kz < Nz;
+            const double2 pf = (live && pre) ? pre[kz * No + o] : make_double2(1.0, 0.0);
+            const float du = live ? dinv[kz].z : 0.f;
+            pinfo[kz] = make_float4((float)pf.x, (float)pf.y, du, 0.f);
+            mx = max(mx, __float_as_uint(fabsf(du)));
+        }
+        atomicMax(&s_dumax, mx);
+    }
+    float kh, kl;
+    split_d(og[o] / kC, kh, kl);
+    // per radius pair (r0, r0 + 1), r0 = 2 (t + 256 pp): k r^2 as float-float, r w_r, and the
+    // reference phase e^{-i k r^2 u_ref} = (bre, bim)
+    float2 kr2h[PREP_PAIRS], kr2l[PREP_PAIRS], wr[PREP_PAIRS], bre[PREP_PAIRS], bim[PREP_PAIRS];
+    float kmax = 0.f;
+#pragma unroll
+    for (int pp = 0; pp < PREP_PAIRS; pp++) {
+        float v[5][2];
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int64_t r = 2 * (t + (int64_t)PREP_THREADS * pp) + q;
+            v[0][q] = v[1][q] = v[2][q] = 0.f;
+            v[3][q] = 1.f;
+            v[4][q] = 0.f;
+            if (r < Nr) {
+                const double rr = rg[r];
+                float r2h, r2l;
+                split_d(rr * rr, r2h, r2l);
+                v[0][q] = kh * r2h;
+                v[1][q] = fmaf(kh, r2h, -v[0][q]) + fmaf(kh, r2l, kl * r2h);
+                v[2][q] = (float)(trap_w(rg, r, Nr) * rr);
+                const float th = v[0][q] * u_ref.x;
+                const float te = fmaf(v[0][q], u_ref.x, -th) + fmaf(v[0][q], u_ref.y, v[1][q] * u_ref.x);
+                float sn, cs;
+                sincos_reduced(reduce_2pi(th, te), sn, cs);
+                v[3][q] = cs;
+                v[4][q] = -sn;
+            }
+            kmax = fmaxf(kmax, fabsf(v[0][q]));
+        }
+        kr2h[pp] = make_float2(v[0][0], v[0][1]);
+        kr2l[pp] = make_float2(v[1][0], v[1][1]);
+        wr[pp] = make_float2(v[2][0], v[2][1]);
+        bre[pp] = make_float2(v[3][0], v[3][1]);
+        bim[pp] = make_float2(v[4][0], v[4][1]);
+    }
+    __syncthreads();  // pinfo and s_dumax complete
+    // the phase e^{-i k r^2 u_k} = base e^{-i delta}, delta = k r^2 (u_k - u_ref): Taylor polynomials
+    // when every |delta| of this CTA is within 0.12, else the exact float-float reduction
+    const bool small = __syncthreads_and(kmax * __uint_as_float(s_dumax) <= 0.12f);
+    const bool near = P.near_field != 0;
+    int s = 0;
+    uint32_t ph = 0;
+    int issued = n_live < ns ? n_live : ns;
+    for (int j = 0; j < n_st; j++) {
+        const int k0 = j * kPrepG;
+        bool ok = true;
+        if (j < n_live) ok = tc::mbar_wait_spin(&full[s], ph, nullptr, kPrepWaitNs);
+        float2 are[kPrepG][PREP_PAIRS], aim[kPrepG][PREP_PAIRS];
+        float mx[kPrepG];
+#pragma unroll
+        for (int u = 0; u < kPrepG; u++) {
+            const int kz = k0 + u;
+            const bool live = kz < Nz;
+            const float4 pf = pinfo[kz < zpad ? kz : 0];
+            const float2 prx = bc2(pf.x), pry = bc2(pf.y);
+            mx[u] = 0.f;
+#pragma unroll
+            for (int pp = 0; pp < PREP_PAIRS; pp++) {
+                const int64_t r0 = 2 * (t + (int64_t)PREP_THREADS * pp);
+                float4 sv4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (live && r0 < Nr) sv4 = *reinterpret_cast<const float4*>(ring + ((size_t)s * kPrepG + u) * rpad + r0);
+                const float2 sre = make_float2(sv4.x, sv4.z), sim = make_float2(sv4.y, sv4.w);
+                // v = pre S
+                float2 vre = __ffma2_rn(prx, sre, neg2(__fmul2_rn(pry, sim)));
+                float2 vim = __ffma2_rn(prx, sim, __fmul2_rn(pry, sre));
+                if (near) {
+                    if (small) {  // e = base e^{-i delta}, then v e
+                        const float2 d = __fmul2_rn(kr2h[pp], bc2(pf.z));
+                        const float2 p2 = __fmul2_rn(d, d);
+                        const float2 sn = __fmul2_rn(
+                            d, __ffma2_rn(p2, __ffma2_rn(p2, bc2(8.33333333e-3f), bc2(-1.66666667e-1f)), bc2(1.0f)));
+                        const float2 cs =
+                            __ffma2_rn(p2, __ffma2_rn(p2, bc2(4.16666667e-2f), bc2(-0.5f)), bc2(1.0f));
+                        const float2 ere = __ffma2_rn(bre[pp], cs, __fmul2_rn(bim[pp], sn));
+                        const float2 eim = __ffma2_rn(bim[pp], cs, neg2(__fmul2_rn(bre[pp], sn)));
+                        const float2 nre = __ffma2_rn(vre, ere, neg2(__fmul2_rn(vim, eim)));
+                        const float2 nim = __ffma2_rn(vre, eim, __fmul2_rn(vim, ere));
+                        vre = nre;
+                        vim = nim;
+                    } else {  // exact angle k r^2 / (2 D_k), per radius
+                        const float4 di = live ? dinv[kz] : make_float4(0.f, 0.f, 0.f, 0.f);
+                        float xr[2] = {vre.x, vre.y}, xi[2] = {vim.x, vim.y};
+                        const float kh2[2] = {kr2h[pp].x, kr2h[pp].y}, kl2[2] = {kr2l[pp].x, kr2l[pp].y};
+#pragma unroll
+                        for (int q = 0; q < 2; q++) {
+                            const float th = kh2[q] * di.x;
+                            const float te = fmaf(kh2[q], di.x, -th) + fmaf(kh2[q], di.y, kl2[q] * di.x);
+                            float sn, cs;
+                            sincos_reduced(reduce_2pi(th, te), sn, cs);  // e^{-i theta}
+                            const float a = fmaf(xr[q], cs, xi[q] * sn), b = fmaf(xi[q], cs, -xr[q] * sn);
+                            xr[q] = a;
+                            xi[q] = b;
+                        }
+                        vre = make_float2(xr[0], xr[1]);
+                        vim = make_float2(xi[0], xi[1]);
+                    }
+                }
+                are[u][pp] = __fmul2_rn(vre, wr[pp]);  // zero beyond n_r (wr = 0, source 0)
+                aim[u][pp] = __fmul2_rn(vim, wr[pp]);
+                mx[u] = fmaxf(mx[u], fmaxf(fmaxf(fabsf(are[u][pp].x), fabsf(aim[u][pp].x)),
+                                           fmaxf(fabsf(are[u][pp].y), fabsf(aim[u][pp].y))));
+            }
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) mx[u] = fmaxf(mx[u], __shfl_xor_sync(0xffffffffu, mx[u], d));
+        }
+        const int par = j & 1;
+        if (lane == 0)
+#pragma unroll
+            for (int u = 0; u < kPrepG; u++) wmax[par][u][w] = mx[u];
+        // every warp has read the stage (its slot can be refilled) and written its maxima
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) {
+                atomicCAS(status, 0, 1);
+                for (int q = j; q < issued; q++)  // let the copies in flight land
+                    tc::mbar_wait(&full[q % ns], (uint32_t)(q / ns) & 1u, nullptr, kPrepWaitNs);
+            }
+            for (int64_t kz = t; kz < zpad; kz += PREP_THREADS) alpha[o * zpad + kz] = __int_as_float(0x7fc00000);
+            return;
+        }
+        if (t == 0 && issued < n_live) {
+            issue(issued, s);  // stage j + ns into this stage's slot
+            issued++;
+        }
+        if (j < n_live && ++s == ns) {
+            s = 0;
+            ph ^= 1u;
+        }
+#pragma unroll
+        for (int u = 0; u < kPrepG; u++) {
+            const int64_t kz = k0 + u;
+            if (kz >= zpad) break;
+            float al = 0.f;
+#pragma unroll
+            for (int q = 0; q < PREP_THREADS / 32; q++) al = fmaxf(al, wmax[par][u][q]);
+            const float sc = al > 0.f ? 1.0f / al : 0.f;
+            if (t == 0) alpha[o * zpad + kz] = al;
+#pragma unroll
+            for (int pp = 0; pp < PREP_PAIRS; pp++) {
+                const int64_t r0 = 2 * (t + (int64_t)PREP_THREADS * pp);
+                if (r0 >= rpad) continue;
+#pragma unroll
+                for (int c = 0; c < 2; c++) {
+                    const float2 x = __fmul2_rn(c ? aim[u][pp] : are[u][pp], bc2(sc));
+                    const __half2 h = __float22half2_rn(x);
+                    const float2 hb = __half22float2(h);
+                    const __half2 l = __float22half2_rn(__fadd2_rn(x, neg2(hb)));
+                    const int64_t idx = ((o * 2 * zpad + 2 * kz + c) * rpad + r0) / 2;
+                    reinterpret_cast<__half2*>(Bh)[idx] = h;
+                    reinterpret_cast<__half2*>(Bl)[idx] = l;
                 }
             }
         }
@@ -731,6 +932,24 @@ bool layout(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, Lay
 
 size_t planes_smem() { return 1024 + STAGES * STAGE_BYTES + 256; }  // alignment slack, stages, barriers
 
+// Ring stages of the B preparation that fit two CTAs per SM (0: the ring form does not apply).
+size_t prep_ring_smem(const Layout& L, int ns)
+{
+    return (size_t)ns * kPrepG * L.rpad * sizeof(float2) + (size_t)L.zpad * sizeof(float4) + (size_t)ns * 8;
+}
+int prep_ring_stages(const mma_hankel_problem* p, const void* src, const Layout& L)
+{
+    if (p->source_c128 || p->pre_radial || (p->n_r & 1) || (p->omega_stride & 1) || (p->plane_stride & 1) ||
+        (reinterpret_cast<uintptr_t>(src) & 15))
+        return 0;
+    const size_t budget = 110 * 1024;
+    const size_t stage = (size_t)kPrepG * L.rpad * sizeof(float2) + 8;
+    const size_t fixed = (size_t)L.zpad * sizeof(float4);
+    if (fixed + 2 * stage > budget) return 0;
+    const size_t ns = (budget - fixed) / stage;
+    return (int)(ns > 8 ? 8 : ns);
+}
+
 template <int MM>
 int launch_planes(const CUtensorMap& th, const CUtensorMap& tl, const Params& P, cudaStream_t st)
 {
@@ -790,16 +1009,30 @@ extern "C" int mma_hankel_planes_tc_prepare(const mma_hankel_problem* p, const m
                                                                reinterpret_cast<float4*>(sc + L.off_dinv),
                                                                reinterpret_cast<float*>(sc + L.off_ftab),
                                                                reinterpret_cast<float2*>(sc + L.off_rgf));
-    const size_t sp = sizeof(float2) * (size_t)L.zpad;
-    if (sp > 48 * 1024 &&
-        cudaFuncSetAttribute(prep_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp) != cudaSuccess)
-        return MMA_ERR_CUDA;
     float uh, ul;  // u_ref = 1/(2 d_ref) as a float pair
     {
         const double u = 1.0 / (2.0 * plan->d_ref);
         uh = (float)u;
         ul = (float)(u - (double)uh);
     }
+    int* status = reinterpret_cast<int*>(sc + L.off_status) + 1;  // the preparation's own status word
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
+    const int ns = prep_ring_stages(p, source, L);
+    if (ns > 0) {
+        const size_t sr = prep_ring_smem(L, ns);
+        if (cudaFuncSetAttribute(prep_b_ring, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr) != cudaSuccess)
+            return MMA_ERR_CUDA;
+        prep_b_ring<<<(unsigned)p->n_omega, PREP_THREADS, sr, st>>>(
+            *p, make_float2(uh, ul), ogrid, rgrid, reinterpret_cast<const float4*>(sc + L.off_dinv),
+            static_cast<const float2*>(source), reinterpret_cast<const double2*>(pre),
+            reinterpret_cast<__half*>(sc + L.off_bh), reinterpret_cast<__half*>(sc + L.off_bl),
+            reinterpret_cast<float*>(sc + L.off_alpha), L.rpad, L.zpad, ns, status);
+        return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
+    }
+    const size_t sp = sizeof(float2) * (size_t)L.zpad;
+    if (sp > 48 * 1024 &&
+        cudaFuncSetAttribute(prep_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp) != cudaSuccess)
+        return MMA_ERR_CUDA;
     prep_b<<<(unsigned)p->n_omega, PREP_THREADS, sp, st>>>(
         *p, make_float2(uh, ul), ogrid, rgrid, reinterpret_cast<const float4*>(sc + L.off_dinv), source,
         reinterpret_cast<const double2*>(pre), reinterpret_cast<__half*>(sc + L.off_bh),
@@ -881,12 +1114,12 @@ extern "C" int mma_hankel_planes_tc_status(const mma_hankel_problem* p, const mm
 {
     Layout L;
     if (!p || !plan || !scratch || !layout(p, plan, L)) return MMA_ERR_ARG;
-    int h = 0;
-    if (cudaMemcpyAsync(&h, static_cast<const char*>(scratch) + L.off_status, sizeof(int), cudaMemcpyDeviceToHost,
+    int h[2] = {0, 0};  // the tensor-core kernel's and the B preparation's status words
+    if (cudaMemcpyAsync(h, static_cast<const char*>(scratch) + L.off_status, sizeof(h), cudaMemcpyDeviceToHost,
                         (cudaStream_t)stream) != cudaSuccess ||
         cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
         return MMA_ERR_CUDA;
-    return h == 0 ? MMA_OK : MMA_ERR_TIMEOUT;
+    return (h[0] == 0 && h[1] == 0) ? MMA_OK : MMA_ERR_TIMEOUT;
 }
 
 extern "C" int mma_tc_selftest(const void* A, const void* B, float* D, int use_tma, int* status, void* stream)

@@ -99,6 +99,23 @@ def test_all_planes_vs_plain(gpu_lib, tol, rho_max, terms):
     assert worst < TOL
 
 
+def test_ring_fed_b_operand_matches_direct_loads(gpu_lib):
+    """A complex64 source with an even number of radii goes through the ring-fed B preparation
+    (bulk copies into shared memory, packed pair arithmetic); the same values as complex128 go
+    through the preparation that loads each value itself.  Both compute the same operations in the
+    same order, so the planes agree bit for bit."""
+    from mma_gb300 import hankel as H
+
+    zg, rg, og, rho, S = _problem(n_omega=16, n_z=40)
+    planes = list(range(len(zg)))
+    pre = np.exp(1j * np.linspace(0, 1, len(zg)))[:, None] * np.ones((1, len(og)))
+    _, p64, _ = H.far_field(og, rg, zg, rho, S, 1.0, pre, True, planes=planes, form="fast", planes_via="tc")
+    _, p128, _ = H.far_field(og, rg, zg, rho, S.to(torch.complex128), 1.0, pre, True, planes=planes, form="fast",
+                             planes_via="tc")
+    for k in planes:
+        assert torch.equal(p64[k], p128[k]), k
+
+
 def test_selected_planes_only(gpu_lib):
     """Planes not requested are not written; requested ones match the direct FP32 form."""
     from mma_gb300 import hankel as H
