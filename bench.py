@@ -227,13 +227,14 @@ def run_hankel(args, device):
     del S
     z = target.zgrid
     pre, _ = H.pre_factor_table(z, target.ogrid, "Ar", 1.0)
+    pre_d = torch.as_tensor(pre, device=device)  # resident like the source (the e2e pass uploads the host table)
     Nz, No, Nr = target.source.shape
     terms = float(No) * Nz * len(rho) * Nr
     stream = torch.cuda.current_stream()
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=device)
 
     def run(form, planes=(0, -1)):
-        return H.far_field(target.ogrid, target.rgrid, z, rho, target.source, 1.0, pre, True, planes=planes,
+        return H.far_field(target.ogrid, target.rgrid, z, rho, target.source, 1.0, pre_d, True, planes=planes,
                            form=form)
 
     out = {}
@@ -282,7 +283,7 @@ def run_hankel(args, device):
     t_e2e = float(np.median(t_runs))
     h2d_bytes, d2h_bytes = host_src.numel() * 8, host_ff.numel() * 16
     del host_src
-    allp = run_all_planes(args, target, z, rho, pre, flush, stream)
+    allp = run_all_planes(args, target, z, rho, pre_d, flush, stream)
     out = {"workload": "config3: N_r=512, N_z=256 (255 planes integrated), N_omega=2048, N_rho=256, D=1 m, "
                        "complex64 source, constant XUV index n=1-1e-5+1e-7i, near-field factor on",
            "terms": terms, "flop_per_term": HANKEL_FLOP_PER_TERM,

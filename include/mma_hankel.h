@@ -63,8 +63,10 @@ typedef struct mma_hankel_fast_plan_t {
  *   B_m[w, r]   = sum_k tau_k v_k^m A_k[w, r],  v_k = (1 - lambda_k^2)/sigma     (HBM-bound)
  *   FF[rho, w]  = sum_{r, m} K_m(k r rho / d_ref) B_m[w, r],
  *   K_m(y) = (sigma y / 2)^m J_m(y) / m!, by a division-free recurrence from J0, J1. (FP32)
- * FP32 arithmetic, float-float phases, compensated sums; planes requested through
- * plane_slot are evaluated directly (FP32, one J0 per term).
+ * FP32 arithmetic, float-float phases, compensated sums.  Planes requested through plane_slot:
+ * up to two (n_planes <= 2, e.g. the entry and exit planes) come from the same series in the
+ * second stage, P_k[rho, w] = sum_r A_k[w, r] sum_m v_k^m K_m(y), sharing its K_m evaluations;
+ * more are evaluated directly (FP32, one J0 per term).
  * The host fills `plan` with mma_hankel_fast_plan (zgrid on the host). */
 int mma_hankel_fast_plan(const double *zgrid_host, int64_t n_z, double distance, double omega_max, double r_max,
                          double rho_max, double tol, mma_hankel_fast_plan_t *plan);

@@ -109,6 +109,9 @@ __global__ void fast_plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F,
     }
 }
 
+__device__ __forceinline__ float2 f2b(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 f2n(float2 a) { return make_float2(-a.x, -a.y); }
+
 // Per-frequency and per-radius constants of stage 1 as floats: ktab[w] = k_w = w/c as (hi, lo);
 // rtab[r] = (r^2 as (hi, lo), trapezoid weight * r, 0).
 __global__ void fast_wr_tables(mma_hankel_problem P, const double* og, const double* rg, float2* ktab, float4* rtab)
@@ -426,15 +429,29 @@ __global__ void __launch_bounds__(kThreads) fast_stage1(mma_hankel_problem P, co
 //   K_{m+1} = sigma m/(m+1) K_m - (sigma y/2)^2 / (m (m+1)) K_{m-1}
 // (J_{m+1} = (2m/y) J_m - J_{m-1} rescaled by (sigma y/2)^m/m!: no division by y).
 // One thread per (w, rho); B and k r / d_ref staged in shared memory in tiles of r.
-template <int MM>
-__global__ void __launch_bounds__(kThreads) fast_stage2(mma_hankel_problem P, mma_hankel_fast_plan_t F,
+// With SER the same K_m(y) also give up to kSeriesPlanes single planes, the fast form's entry and
+// exit planes: P_k[rho, w] = sum_r A_k[w, r] sum_m v_k^m K_m(y) (J0(lambda_k y) by the same
+// series), with A_k from series_plane_a and the pairs (v_k0^m, v_k1^m) from series_plane_tables;
+// the planes' sums run as FP32x2 pairs (one lane per plane) beside the far field's.
+constexpr int kSeriesPlanes = 2;
+template <int MM, bool SER>
+__global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_problem P, mma_hankel_fast_plan_t F,
                                                         const double* og, const double* rg, const double* rho,
-                                                        const float2* Bp, double2* ff, int rtile)
+                                                        const float2* Bp, double2* ff, int rtile,
+                                                        const float2* asel, const float2* vsel, int n_sel,
+                                                        double2* planes)
 {
-    extern __shared__ float smem[];
+    extern __shared__ __align__(16) float smem[];
     const int64_t o = blockIdx.y, Nr = P.n_r, Nrho = P.n_rho, No = P.n_omega;
-    float2* B = reinterpret_cast<float2*>(smem);  // MM * rtile
+    float2* B = reinterpret_cast<float2*>(smem);  // MM * rtile (rtile even)
     float2* kr = B + MM * rtile;                  // rtile
+    float2* As = kr + rtile;                      // SER: kSeriesPlanes * rtile, A_k of the selected planes
+    float2* Vs = As + kSeriesPlanes * rtile;      // SER: MM pairs (v_k0^m, v_k1^m)
+    if (SER)
+        for (int q = threadIdx.x; q < MM; q += blockDim.x) Vs[q] = vsel[q];
+    float2 ppart[kSeriesPlanes], phi[kSeriesPlanes], plo[kSeriesPlanes];  // the planes' compensated sums
+#pragma unroll
+    for (int i = 0; i < kSeriesPlanes; i++) ppart[i] = phi[i] = plo[i] = make_float2(0.f, 0.f);
     const double kap = (og[o] / kC) / F.d_ref;
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float rh = 0.f, rl = 0.f;
@@ -453,13 +470,81 @@ __global__ void __launch_bounds__(kThreads) fast_stage2(mma_hankel_problem P, mm
             float h, l;
             split_d(kap * rg[r0 + q], h, l);
             kr[q] = make_float2(h, l);
+            if (SER)
+#pragma unroll
+                for (int i = 0; i < kSeriesPlanes; i++) As[i * rtile + q] = asel[((int64_t)i * No + o) * Nr + r0 + q];
         }
         __syncthreads();
         if (j < Nrho) {
-            // two radii per iteration: their seed and m-recurrence chains are independent, so the
-            // scheduler can interleave them (the loop is otherwise bound by dependent FMA latency)
-#pragma unroll 2
-            for (int64_t q = 0; q < nt; q++) {
+            // radius pairs: each per-radius quantity is a pair, so the y products, K_1, the
+            // m-recurrence and the contraction run as packed FP32x2 instructions (each lane the
+            // single-radius operations in the same order); the two radii's J0/J1 seeds are
+            // independent chains the scheduler interleaves.  The row stride rtile is even, so a
+            // pair's B values and k r / d_ref entries are one 16-byte load each.
+            const float4* B4 = reinterpret_cast<const float4*>(B);
+            const float4* kr4 = reinterpret_cast<const float4*>(kr);
+            // one radius's terms: the far field's, and with SER the planes' A_k[r] sum_m v_k^m K_m
+            auto add_in = [&](float2 in, int64_t q, float2 sv) {
+                part = __fadd2_rn(part, in);
+                if (SER) {
+                    ppart[0] = __ffma2_rn(As[q], f2b(sv.x), ppart[0]);
+                    ppart[1] = __ffma2_rn(As[rtile + q], f2b(sv.y), ppart[1]);
+                }
+                if (++cnt == 16) {
+                    ff_acc(hi.x, lo.x, part.x);
+                    ff_acc(hi.y, lo.y, part.y);
+                    part = make_float2(0.f, 0.f);
+                    if (SER)
+#pragma unroll
+                        for (int i = 0; i < kSeriesPlanes; i++) {
+                            ff_acc(phi[i].x, plo[i].x, ppart[i].x);
+                            ff_acc(phi[i].y, plo[i].y, ppart[i].y);
+                            ppart[i] = make_float2(0.f, 0.f);
+                        }
+                    cnt = 0;
+                }
+            };
+            int64_t q = 0;
+            for (; q + 1 < nt; q += 2) {
+                const float4 kk = kr4[q / 2];
+                const float2 kh = make_float2(kk.x, kk.z), kl = make_float2(kk.y, kk.w);
+                const float2 yh = __fmul2_rn(kh, f2b(rh));
+                const float2 yl = __fadd2_rn(__ffma2_rn(kh, f2b(rh), f2n(yh)), __ffma2_rn(kh, f2b(rl), __fmul2_rn(kl, f2b(rh))));
+                float J0a, J1a, J0b, J1b;
+                bessel01<true>(yh.x, yl.x, J0a, J1a);
+                bessel01<true>(yh.y, yl.y, J0b, J1b);
+                const float2 y = __fadd2_rn(yh, yl);
+                float2 K0 = make_float2(J0a, J0b);
+                float2 K1 = __fmul2_rn(__fmul2_rn(f2b(0.5f * s), y), make_float2(J1a, J1b));
+                const float2 q2 = __fmul2_rn(__fmul2_rn(f2b(0.25f * s * s), y), y);
+                const float4 b0 = B4[q / 2], b1 = B4[(rtile + q) / 2];
+                float2 ia = __ffma2_rn(make_float2(b0.x, b0.y), f2b(K0.x), __fmul2_rn(make_float2(b1.x, b1.y), f2b(K1.x)));
+                float2 ib = __ffma2_rn(make_float2(b0.z, b0.w), f2b(K0.y), __fmul2_rn(make_float2(b1.z, b1.w), f2b(K1.y)));
+                // SER: per radius the pair (sum_m v_k0^m K_m, sum_m v_k1^m K_m)
+                float2 sa = make_float2(0.f, 0.f), sb = sa;
+                if (SER) {
+                    sa = __ffma2_rn(Vs[1], f2b(K1.x), f2b(K0.x));  // v^0 = 1
+                    sb = __ffma2_rn(Vs[1], f2b(K1.y), f2b(K0.y));
+                }
+#pragma unroll
+                for (int m = 1; m + 1 < MM; m++) {
+                    const float2 K2 = __ffma2_rn(f2b(s * ((float)m / (float)(m + 1))), K1,
+                                                 __fmul2_rn(f2n(__fmul2_rn(q2, f2b(1.0f / (float)(m * (m + 1))))), K0));
+                    const float4 b = B4[((m + 1) * rtile + q) / 2];
+                    ia = __ffma2_rn(make_float2(b.x, b.y), f2b(K2.x), ia);
+                    ib = __ffma2_rn(make_float2(b.z, b.w), f2b(K2.y), ib);
+                    if (SER) {
+                        const float2 v = Vs[m + 1];
+                        sa = __ffma2_rn(v, f2b(K2.x), sa);
+                        sb = __ffma2_rn(v, f2b(K2.y), sb);
+                    }
+                    K0 = K1;
+                    K1 = K2;
+                }
+                add_in(ia, q, sa);
+                add_in(ib, q + 1, sb);
+            }
+            if (q < nt) {  // an odd last radius
                 const float2 kk = kr[q];
                 const float yh = kk.x * rh;
                 const float yl = fmaf(kk.x, rh, -yh) + fmaf(kk.x, rl, kk.y * rh);
@@ -470,23 +555,19 @@ __global__ void __launch_bounds__(kThreads) fast_stage2(mma_hankel_problem P, mm
                 const float q2 = 0.25f * s * s * y * y;
                 float2 b0 = B[q], b1 = B[rtile + q];
                 float2 in = make_float2(fmaf(b0.x, K0, b1.x * K1), fmaf(b0.y, K0, b1.y * K1));
+                float2 sa = make_float2(0.f, 0.f);
+                if (SER) sa = __ffma2_rn(Vs[1], f2b(K1), f2b(K0));
 #pragma unroll
                 for (int m = 1; m + 1 < MM; m++) {
                     const float K2 = fmaf(s * ((float)m / (float)(m + 1)), K1, -(q2 * (1.0f / (float)(m * (m + 1)))) * K0);
                     const float2 b = B[(m + 1) * rtile + q];
                     in.x = fmaf(b.x, K2, in.x);
                     in.y = fmaf(b.y, K2, in.y);
+                    if (SER) sa = __ffma2_rn(Vs[m + 1], f2b(K2), sa);
                     K0 = K1;
                     K1 = K2;
                 }
-                part.x += in.x;
-                part.y += in.y;
-                if (++cnt == 16) {
-                    ff_acc(hi.x, lo.x, part.x);
-                    ff_acc(hi.y, lo.y, part.y);
-                    part = make_float2(0.f, 0.f);
-                    cnt = 0;
-                }
+                add_in(in, q, sa);
             }
         }
     }
@@ -494,7 +575,70 @@ __global__ void __launch_bounds__(kThreads) fast_stage2(mma_hankel_problem P, mm
         ff_acc(hi.x, lo.x, part.x);
         ff_acc(hi.y, lo.y, part.y);
         ff[j * No + o] = make_double2((double)hi.x + (double)lo.x, (double)hi.y + (double)lo.y);
+        if (SER)
+#pragma unroll
+            for (int i = 0; i < kSeriesPlanes; i++) {
+                ff_acc(phi[i].x, plo[i].x, ppart[i].x);
+                ff_acc(phi[i].y, plo[i].y, ppart[i].y);
+                if (i < n_sel)
+                    planes[((int64_t)i * Nrho + j) * No + o] =
+                        make_double2((double)phi[i].x + (double)plo[i].x, (double)phi[i].y + (double)plo[i].y);
+            }
     }
+}
+
+// Tables of the planes that stage 2 evaluates by the series: for output slot i < n_sel the plane
+// k with slot[k] == i (slot i >= n_sel repeats slot 0), sel_kz[i] = k and, per term m,
+// vsel[m] = (v_k0^m, v_k1^m), v_k = (1 - lambda_k^2) / sigma (in FP64, rounded once).
+__global__ void series_plane_tables(mma_hankel_problem P, mma_hankel_fast_plan_t F, const double* zg,
+                                    const int64_t* slot, int n_sel, int mm, int* sel_kz, float2* vsel)
+{
+    double v[kSeriesPlanes];
+    for (int i = 0; i < kSeriesPlanes; i++) {
+        int64_t kz = 0;
+        for (int64_t q = 0; q < P.n_z; q++)
+            if (slot[q] == (i < n_sel ? i : 0)) kz = q;
+        if (threadIdx.x == 0) sel_kz[i] = (int)kz;
+        const double lam = F.d_ref / (P.distance - zg[kz]);
+        v[i] = (1.0 - lam * lam) / F.sigma;
+    }
+    for (int m = threadIdx.x; m < mm; m += blockDim.x) {
+        double c0 = 1.0, c1 = 1.0;
+        for (int q = 0; q < m; q++) {
+            c0 *= v[0];
+            c1 *= v[1];
+        }
+        vsel[m] = make_float2((float)c0, (float)c1);
+    }
+}
+
+// A_k[w, r] = pre_k(w) e^{-i k r^2/(2 D_k)} r w_r S_k[w, r] of the series planes, in FP32 with the
+// phase angle as float-float (k r^2 from ktab and rtab, 1/(2 D_k) from the plane table) reduced
+// mod 2 pi: asel[i][w][r].  Grid (radius blocks, frequencies, kSeriesPlanes).
+template <int MM>
+__global__ void series_plane_a(mma_hankel_problem P, const float2* ktab, const float4* rtab, const float* ptab,
+                              const void* src, const double2* pre, const int* sel_kz, float2* asel)
+{
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, o = blockIdx.y, i = blockIdx.z;
+    if (r >= P.n_r) return;
+    const int64_t kz = sel_kz[i];
+    const double2 pd = pre_at(P, pre, kz, o, r);
+    const float2 sv = load_src_f(src, kz * P.plane_stride + o * P.omega_stride + r, P.source_c128);
+    const float2 pf = make_float2((float)pd.x, (float)pd.y);
+    float2 a = make_float2(fmaf(pf.x, sv.x, -pf.y * sv.y), fmaf(pf.x, sv.y, pf.y * sv.x));
+    const float4 rt = rtab[r];
+    if (P.near_field) {
+        const float2 kk = ktab[o];
+        const float kr2h = kk.x * rt.x;
+        const float kr2l = fmaf(kk.x, rt.x, -kr2h) + fmaf(kk.x, rt.y, kk.y * rt.x);
+        const float ih = ptab[kz * (MM + 4) + MM], il = ptab[kz * (MM + 4) + MM + 1];
+        const float th = kr2h * ih;
+        const float te = fmaf(kr2h, ih, -th) + fmaf(kr2h, il, kr2l * ih);
+        float sn, cs;
+        sincos_reduced(reduce_2pi(th, te), sn, cs);  // e^{-i theta} = (cs, -sn)
+        a = make_float2(fmaf(a.x, cs, a.y * sn), fmaf(a.y, cs, -a.x * sn));
+    }
+    asel[(i * P.n_omega + o) * P.n_r + r] = make_float2(a.x * rt.z, a.y * rt.z);
 }
 
 // ------------------------------------------------------------------------ fast form, single planes
@@ -661,10 +805,20 @@ static size_t status_off(const mma_hankel_problem* p, const mma_hankel_fast_plan
     return rtab_off(p, plan) + up256(sizeof(float4) * (size_t)p->n_r);
 }
 
+// after the status word: the series planes' tables (sel_kz, vsel) and A_k rows (asel)
+static size_t sel_off(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
+{
+    return status_off(p, plan) + 256;
+}
+static size_t asel_off(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
+{
+    return sel_off(p, plan) + up256(64 + sizeof(float2) * (size_t)plan->n_terms);
+}
+
 extern "C" size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan)
 {
     if (!p || !plan) return 0;
-    return status_off(p, plan) + 256;
+    return asel_off(p, plan) + up256(sizeof(float2) * 2 * (size_t)p->n_omega * (size_t)p->n_r);
 }
 
 extern "C" int mma_hankel_fast_status(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
@@ -699,8 +853,10 @@ int ring_stages(const mma_hankel_problem* p, const void* src)
 template <int MM>
 int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, const double* og, const double* rg,
                 const double* zg, const double* rho, const void* src, const double2* pre, double2* ff,
-                float2* Bp, float* ptab, float2* ktab, float4* rtab, int* status, cudaStream_t st)
+                float2* Bp, float* ptab, float2* ktab, float4* rtab, int* status, const int64_t* slot, int n_sel,
+                double2* planes, int* sel_kz, float2* vsel, float2* asel, cudaStream_t st)
 {
+    const bool ser = n_sel > 0 && n_sel <= kSeriesPlanes;  // planes by the series inside stage 2
     fast_plane_table<MM><<<(unsigned)((p->n_z + 127) / 128), 128, 0, st>>>(*p, *plan, zg, ptab);
     bool ringed = false;
     if constexpr (MM % 4 == 0 && MM <= 16) {
@@ -730,29 +886,56 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
         dim3 g1((unsigned)((p->n_r + kThreads - 1) / kThreads), (unsigned)p->n_omega);
         fast_stage1<MM><<<g1, kThreads, s1, st>>>(*p, og, rg, src, pre, ptab, Bp);
     }
+    if (ser) {
+        if (!ringed) {
+            const int64_t nt = p->n_omega > p->n_r ? p->n_omega : p->n_r;
+            fast_wr_tables<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(*p, og, rg, ktab, rtab);
+        }
+        series_plane_tables<<<1, 64, 0, st>>>(*p, *plan, zg, slot, n_sel, MM, sel_kz, vsel);
+        dim3 ga((unsigned)((p->n_r + 255) / 256), (unsigned)p->n_omega, (unsigned)kSeriesPlanes);
+        series_plane_a<MM><<<ga, 256, 0, st>>>(*p, ktab, rtab, ptab, src, pre, sel_kz, asel);
+    }
+    // stage 2: B, k r / d_ref and (series planes) their A_k rows per tile of rtile radii
+    const int rows = MM + 1 + (ser ? kSeriesPlanes : 0);
+    const size_t budget = (ser ? 72 : 96) * 1024;
     int rtile = (int)(p->n_r < 512 ? p->n_r : 512);
-    while ((size_t)(MM + 1) * rtile * sizeof(float2) > 96 * 1024 && rtile > 32) rtile /= 2;
-    const size_t s2 = (size_t)(MM + 1) * rtile * sizeof(float2);
-    cudaFuncSetAttribute(fast_stage2<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
+    rtile += rtile & 1;  // even row stride: stage 2 loads radius pairs as 16-byte words
+    while ((size_t)rows * rtile * sizeof(float2) + MM * sizeof(float2) > budget && rtile > 32) rtile /= 2;
+    const size_t s2 = (size_t)rows * rtile * sizeof(float2) + (ser ? MM * sizeof(float2) : 0);
     dim3 g2((unsigned)((p->n_rho + kThreads - 1) / kThreads), (unsigned)p->n_omega);
-    fast_stage2<MM><<<g2, kThreads, s2, st>>>(*p, *plan, og, rg, rho, Bp, ff, rtile);
+    if (ser) {
+        cudaFuncSetAttribute(fast_stage2<MM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
+        fast_stage2<MM, true><<<g2, kThreads, s2, st>>>(*p, *plan, og, rg, rho, Bp, ff, rtile, asel, vsel, n_sel,
+                                                         planes);
+    } else {
+        cudaFuncSetAttribute(fast_stage2<MM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
+        fast_stage2<MM, false><<<g2, kThreads, s2, st>>>(*p, *plan, og, rg, rho, Bp, ff, rtile, nullptr, nullptr, 0,
+                                                          nullptr);
+    }
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }
 }  // namespace
 
 // FF[rho, w] = sum_k tau_k P_k[rho, w] (the z trapezoid) from plane transforms already computed:
-// planes[slot[k]][rho][w], one thread per (rho, w), coalesced over w.  The CTA stages the planes'
-// offsets and weights in shared memory, and each thread keeps eight plane loads in flight (the
-// kernel streams all planes once, so it is HBM-bound).
-constexpr int kFfChunk = 512;
+// planes[slot[k]][rho][w], coalesced over w.  The kernel streams every plane once (HBM-bound).
+// A CTA takes 64 elements; its four thread groups sum a quarter of the planes each (eight loads
+// in flight per thread) and the quarters are added in a fixed order, so the result does not
+// depend on scheduling.  Small work units keep the last wave of CTAs short (config 3: 8192 CTAs).
+constexpr int kFfChunk = 512;  // planes whose offsets and weights are staged at a time
+constexpr int kFfElems = 64;   // elements per CTA
 __global__ void __launch_bounds__(kThreads) ff_from_planes_kernel(mma_hankel_problem P, const double* zg,
                                                                  const int64_t* slot, const double2* planes,
                                                                  double2* ff)
 {
+    constexpr int kGroups = kThreads / kFfElems;
     __shared__ int64_t s_off[kFfChunk];
     __shared__ double s_tau[kFfChunk];
+    __shared__ double2 s_part[kGroups][kFfElems];
     const int64_t Nz = P.n_z, n = P.n_rho * P.n_omega;
-    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int g = threadIdx.x / kFfElems;
+    const int64_t e = blockIdx.x * (int64_t)kFfElems + threadIdx.x % kFfElems;
+    const bool live = e < n;
+    const int64_t a = live ? e : 0;  // clamped: every load stays in bounds
     double re = 0.0, im = 0.0;
     for (int64_t k0 = 0; k0 < Nz; k0 += kFfChunk) {
         const int nk = (int)(Nz - k0 < kFfChunk ? Nz - k0 : kFfChunk);
@@ -762,26 +945,35 @@ __global__ void __launch_bounds__(kThreads) ff_from_planes_kernel(mma_hankel_pro
             s_tau[q] = trap_w(zg, k0 + q, Nz);
         }
         __syncthreads();
-        if (e < n) {
-            int q = 0;
-            for (; q + 8 <= nk; q += 8) {
-                double2 v[8];
+        const int per = (nk + kGroups - 1) / kGroups, q0 = g * per, q1 = q0 + per < nk ? q0 + per : nk;
+        int q = q0;
+        for (; q + 8 <= q1; q += 8) {
+            double2 x[8];
 #pragma unroll
-                for (int u = 0; u < 8; u++) v[u] = __ldcs(planes + s_off[q + u] + e);
+            for (int u = 0; u < 8; u++) x[u] = __ldcs(planes + s_off[q + u] + a);
 #pragma unroll
-                for (int u = 0; u < 8; u++) {
-                    re = fma(s_tau[q + u], v[u].x, re);
-                    im = fma(s_tau[q + u], v[u].y, im);
-                }
-            }
-            for (; q < nk; q++) {
-                const double2 v = __ldcs(planes + s_off[q] + e);
-                re = fma(s_tau[q], v.x, re);
-                im = fma(s_tau[q], v.y, im);
+            for (int u = 0; u < 8; u++) {
+                re = fma(s_tau[q + u], x[u].x, re);
+                im = fma(s_tau[q + u], x[u].y, im);
             }
         }
+        for (; q < q1; q++) {
+            const double2 x = __ldcs(planes + s_off[q] + a);
+            re = fma(s_tau[q], x.x, re);
+            im = fma(s_tau[q], x.y, im);
+        }
     }
-    if (e < n) ff[e] = make_double2(re, im);
+    s_part[g][threadIdx.x % kFfElems] = make_double2(re, im);
+    __syncthreads();
+    if (g == 0 && live) {
+        double2 acc = s_part[0][threadIdx.x];
+#pragma unroll
+        for (int q = 1; q < kGroups; q++) {
+            acc.x += s_part[q][threadIdx.x].x;
+            acc.y += s_part[q][threadIdx.x].y;
+        }
+        ff[e] = acc;
+    }
 }
 
 extern "C" int mma_hankel_ff_from_planes(const mma_hankel_problem* p, const double* zgrid, const int64_t* plane_slot,
@@ -789,7 +981,7 @@ extern "C" int mma_hankel_ff_from_planes(const mma_hankel_problem* p, const doub
 {
     if (!valid(p) || !zgrid || !plane_slot || !planes || !ff) return MMA_ERR_ARG;
     const int64_t n = p->n_rho * p->n_omega;
-    const int64_t b = (n + kThreads - 1) / kThreads;
+    const int64_t b = (n + kFfElems - 1) / kFfElems;
     if (b > INT32_MAX) return MMA_ERR_TOO_LARGE;
     ff_from_planes_kernel<<<(unsigned)b, kThreads, 0, (cudaStream_t)stream>>>(
         *p, zgrid, plane_slot, reinterpret_cast<const double2*>(planes), reinterpret_cast<double2*>(ff));
@@ -814,10 +1006,15 @@ extern "C" int mma_hankel_fast(const mma_hankel_problem* p, const mma_hankel_fas
     float2* ktab = reinterpret_cast<float2*>(sc + ktab_off(p, plan));
     float4* rtab = reinterpret_cast<float4*>(sc + rtab_off(p, plan));
     int* status = reinterpret_cast<int*>(sc + status_off(p, plan));
+    int* sel_kz = reinterpret_cast<int*>(sc + sel_off(p, plan));
+    float2* vsel = reinterpret_cast<float2*>(sc + sel_off(p, plan) + 64);
+    float2* asel = reinterpret_cast<float2*>(sc + asel_off(p, plan));
+    double2* planes2 = reinterpret_cast<double2*>(planes);
     int rc;
-#define MMA_FAST_CASE(T)                                                                                             \
-    case T:                                                                                                          \
-        rc = launch_fast<T>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, ktab, rtab, status, st); \
+#define MMA_FAST_CASE(T)                                                                                         \
+    case T:                                                                                                      \
+        rc = launch_fast<T>(p, plan, ogrid, rgrid, zgrid, rho, source, pre2, ff2, Bp, ptab, ktab, rtab, status,  \
+                            plane_slot, n_planes, planes2, sel_kz, vsel, asel, st);                              \
         break;
     switch (plan->n_terms) {
         MMA_FAST_CASE(8)
@@ -832,7 +1029,7 @@ extern "C" int mma_hankel_fast(const mma_hankel_problem* p, const mma_hankel_fas
     }
 #undef MMA_FAST_CASE
     if (rc != MMA_OK) return rc;
-    if (n_planes > 0) {
+    if (n_planes > kSeriesPlanes) {  // more planes than the series pass takes: one J0 per term
         const int rtile = (int)(p->n_r < 1024 ? p->n_r : 1024);
         const size_t sp = 2 * sizeof(float2) * (size_t)rtile;
         dim3 gp((unsigned)((p->n_rho + kThreads - 1) / kThreads), (unsigned)p->n_omega, (unsigned)n_planes);

@@ -419,6 +419,8 @@ def pre_factor_table(zgrid, ogrid, preset_gas="vacuum", pressure=1.0, absorption
 
 # ------------------------------------------------------------------------------ kernels
 def _dev(a, device):
+    if torch.is_tensor(a):  # already a tensor (on the device: no copy)
+        return a.to(device=device, dtype=torch.float64).contiguous()
     a = np.ascontiguousarray(a, dtype=np.float64)
     if not a.flags.writeable:  # e.g. a view of a read-only archive buffer: torch wants writable memory
         a = a.copy()
@@ -426,6 +428,7 @@ def _dev(a, device):
 
 
 TC_MIN_PLANES = 16  # from this many requested planes the fast form computes them on the tensor cores
+SERIES_PLANES = 2  # up to this many planes the fast pass evaluates inside its series stage
 
 
 def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_field=True, planes=(), form="plain",
@@ -434,9 +437,11 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
     tensor is copied there first).
     Returns (FF [Nrho, No] complex128 tensor, {plane: [Nrho, No] tensor}, fast plan dict or None).
 
-    With form="fast", requested planes are computed either directly (one FP32 J0 per term,
-    planes_via="direct") or by the tensor-core split-precision GEMM (planes_via="tc");
-    "auto" takes the tensor cores from TC_MIN_PLANES planes on, where the problem fits them.
+    With form="fast", requested planes are computed in the fast pass (planes_via="direct": up to
+    two planes, such as the entry and exit planes, by the same multiplication-theorem series inside
+    its second stage, sharing its Bessel evaluations; more by one FP32 J0 per term) or by the
+    tensor-core split-precision GEMM (planes_via="tc"); "auto" takes the tensor cores from
+    TC_MIN_PLANES planes on, where the problem fits them.
     FF_integrated comes from the fast form's z-first series (ff_via="fast"), or, when every plane
     is computed on the tensor cores, as the z trapezoid of those planes (ff_via="planes": the
     quantity the cumulative results end on, at the planes' accuracy, without the series pass);
@@ -456,8 +461,9 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
                          int(S.dtype == torch.complex128), No * Nr, Nr, int(radial))
     og, rg, zg, rh = (_dev(a, dev) for a in (ogrid, rgrid, zgrid, rho))
     pre = None
-    if pre_table is not None:
-        pre = torch.as_tensor(np.ascontiguousarray(pre_table, dtype=np.complex128), device=dev)
+    if pre_table is not None:  # a device tensor is used in place; a host table is copied once per call
+        pre = pre_table.to(device=dev, dtype=torch.complex128).contiguous() if torch.is_tensor(pre_table) else \
+            torch.as_tensor(np.ascontiguousarray(pre_table, dtype=np.complex128), device=dev)
     ff = torch.zeros(len(rho), No, dtype=torch.complex128, device=dev)
     planes = sorted(set(int(p) % Nz for p in planes))
     slot = None
@@ -467,7 +473,8 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
         for i, p in enumerate(planes):
             s[p] = i
         slot = torch.as_tensor(s, device=dev)
-        pl = torch.zeros(len(planes), len(rho), No, dtype=torch.complex128, device=dev)
+        # every element of a requested plane is written by each form's kernels
+        pl = torch.empty(len(planes), len(rho), No, dtype=torch.complex128, device=dev)
     st = ctypes.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
     ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
     plan_d = None
@@ -519,7 +526,8 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
             _check(lib.mma_hankel_planes_tc_status(ctypes.byref(prob), ctypes.byref(plan), tcs.data_ptr(), st),
                    "mma_hankel_planes_tc (kernel status)")
         plan_d = plan.as_dict()
-        plan_d["planes_via"] = ("tc" if use_tc else "direct") if planes else None
+        plan_d["planes_via"] = ("tc" if use_tc else ("series" if len(planes) <= SERIES_PLANES else "direct")) \
+            if planes else None
         plan_d["ff_via"] = "planes" if ff_planes else "fast"
     else:
         raise ValueError("form must be 'plain' or 'fast'")

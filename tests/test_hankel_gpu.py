@@ -120,3 +120,32 @@ def test_radially_modulated_medium(gpu_lib):
             assert per_harmonic(h.entry_plane_transform, ref["entry"]) < FAST_TOL
             for k in range(ref["cumulative"].shape[0]):
                 assert per_harmonic(h.cumulative_field_no_norm[k], ref["cumulative"][k]) < FAST_TOL, k
+
+
+@pytest.mark.parametrize("n_r,source", [(200, "c64"), (201, "c128")], ids=["even r, complex64", "odd r, complex128"])
+def test_series_planes_match_direct_planes(gpu_lib, n_r, source):
+    """Up to two requested planes (the entry and exit planes) come out of the fast form's series
+    stage, from the same K_m(y) as the far field; three or more go through one FP32 J0 per term.
+    Both evaluate J0(k r rho / D_k): per-harmonic agreement within 1e-6, and the far field itself is
+    bit-identical whichever way the planes went (the series adds independent sums only)."""
+    from mma_gb300 import hankel as H
+
+    omega0 = 0.057 / 2.4188843265857e-17
+    rg = np.linspace(0.0, 200e-6, n_r)
+    zg = np.linspace(-5e-3, 5e-3, 30)
+    og = np.linspace(10 * omega0, 42 * omega0, 12)
+    rho = np.linspace(0.0, 5e-3, 40)
+    rng = np.random.default_rng(n_r)
+    S = np.exp(-(rg / 50e-6) ** 2)[None, None, :] * np.exp(1j * rng.uniform(0, 6.28, (len(zg), len(og))))[:, :, None]
+    S = torch.tensor(S, dtype=torch.complex64 if source == "c64" else torch.complex128, device="cuda")
+    pre = np.exp(1j * np.linspace(0, 1, len(zg)))[:, None] * np.ones((1, len(og)))
+    ff2, p2, plan2 = H.far_field(og, rg, zg, rho, S, 1.0, pre, True, planes=(0, -1), form="fast",
+                                 planes_via="direct")
+    ff3, p3, plan3 = H.far_field(og, rg, zg, rho, S, 1.0, pre, True, planes=(0, 7, -1), form="fast",
+                                 planes_via="direct")
+    assert plan2["planes_via"] == "series" and plan3["planes_via"] == "direct"
+    assert torch.equal(ff2, ff3)
+    for k in (0, len(zg) - 1):
+        assert per_harmonic(p2[k].cpu().numpy(), p3[k].cpu().numpy()) < 1e-6, k
+    _, p1, _ = H.far_field(og, rg, zg, rho, S, 1.0, pre, True, planes=(7,), form="fast", planes_via="direct")
+    assert per_harmonic(p1[7].cpu().numpy(), p3[7].cpu().numpy()) < 1e-6

@@ -116,6 +116,37 @@ def test_ring_fed_b_operand_matches_direct_loads(gpu_lib):
         assert torch.equal(p64[k], p128[k]), k
 
 
+@pytest.mark.parametrize("nz,nrho,no", [(40, 50, 24), (600, 3, 37)], ids=["40 planes", "600 planes, ragged"])
+def test_z_trapezoid_of_planes(gpu_lib, nz, nrho, no):
+    """mma_hankel_ff_from_planes (FF_integrated from every plane, Hankel_transform.py:661) against
+    the trapezoid in numpy: planes stored in a permuted slot order, a non-uniform z grid, more
+    planes than one staged chunk (512) and element counts that leave a ragged last CTA."""
+    import ctypes
+
+    from mma_gb300 import hankel as H
+
+    lib = H._sig()
+    rng = np.random.default_rng(nz)
+    z = np.sort(rng.uniform(-5e-3, 5e-3, nz))
+    slot = rng.permutation(nz).astype(np.int64)
+    planes = rng.standard_normal((nz, nrho, no)) + 1j * rng.standard_normal((nz, nrho, no))
+    w = np.zeros(nz)
+    w[:-1] += 0.5 * np.diff(z)
+    w[1:] += 0.5 * np.diff(z)
+    ref = np.einsum("k,kab->ab", w, planes[slot])  # plane k is stored at slot[k]
+    prob = H.HankelProblem(no, 2, nz, nrho, 1.0, 1, 0, no * 2, 2, 0)
+    dz = torch.tensor(z, device="cuda")
+    ds = torch.tensor(slot, device="cuda")
+    dp = torch.tensor(planes, dtype=torch.complex128, device="cuda")
+    ff = torch.full((nrho, no), complex("nan"), dtype=torch.complex128, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.mma_hankel_ff_from_planes(ctypes.byref(prob), dz.data_ptr(), ds.data_ptr(), dp.data_ptr(),
+                                         ff.data_ptr(), st) == 0
+    torch.cuda.synchronize()
+    got = ff.cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
 def test_selected_planes_only(gpu_lib):
     """Planes not requested are not written; requested ones match the direct FP32 form."""
     from mma_gb300 import hankel as H
