@@ -41,6 +41,10 @@ namespace tcf {
 
 using namespace mma::tc;
 
+// packed FP32x2 helpers: a negated pair, a broadcast scalar
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+
 constexpr int KB = 32;       // r per K-block: 32 FP16 = one 64-byte swizzled row
 constexpr int NP = 128;      // planes per tile
 constexpr int NCOL = 2 * NP; // accumulator columns of a tile (re, im per plane)
@@ -258,34 +262,33 @@ __global__ void __launch_bounds__(THREADS, 1)
             uint8_t* sa[4];
 #pragma unroll
             for (int c = 0; c < 4; c++) sa[c] = base + ((((k0 >> 3) ^ c) & 3) << 4);
-            const float y0h = kh * rv.x, y0l = fmaf(kh, rv.x, -y0h) + fmaf(kh, rv.y, kl * rv.x);
-            const float y1h = kh * rv.z, y1l = fmaf(kh, rv.z, -y1h) + fmaf(kh, rv.w, kl * rv.z);
+            // the lane's two radii as FP32x2 pairs: y = k rho r / d_ref in float-float
+            const float2 rh = make_float2(rv.x, rv.z), rl = make_float2(rv.y, rv.w);
+            const float2 yh = __fmul2_rn(bc2(kh), rh);
+            const float2 yl = __fadd2_rn(__ffma2_rn(bc2(kh), rh, neg2(yh)), __ffma2_rn(bc2(kh), rl, __fmul2_rn(bc2(kl), rh)));
             float J00, J10, J01, J11;
-            bessel01<true>(y0h, y0l, J00, J10);
-            bessel01<true>(y1h, y1l, J01, J11);
+            bessel01<true>(yh.x, yl.x, J00, J10);
+            bessel01<true>(yh.y, yl.y, J01, J11);
             // K^_m = u^m J_m(y), u = y / y_max <= 1:  K^_{m+1} = (2m / y_max) K^_m - u^2 K^_{m-1}
-            const float u0 = (y0h + y0l) * iy, u1 = (y1h + y1l) * iy;
-            const float w0 = u0 * u0, w1 = u1 * u1;
-            auto put2 = [&](int m, float x0, float x1) {
-                const __half2 h = __floats2half2_rn(x0, x1);
+            const float2 u = __fmul2_rn(__fadd2_rn(yh, yl), bc2(iy));
+            const float2 w = __fmul2_rn(u, u);
+            auto put2 = [&](int m, float2 x) {  // FP16 hi and lo of the pair
+                const __half2 h = __float22half2_rn(x);
                 const float2 f = __half22float2(h);
-                const __half2 l = __floats2half2_rn(x0 - f.x, x1 - f.y);
+                const __half2 l = __float22half2_rn(__fadd2_rn(x, neg2(f)));
                 uint8_t* const pa = sa[(m >> 1) & 3] + (m >> 3) * 512 + (m & 7) * 64;
                 *reinterpret_cast<__half2*>(pa) = h;
                 *reinterpret_cast<__half2*>(pa + A_BYTES) = l;
             };
-            float a0 = J00, b0 = u0 * J10, a1 = J01, b1 = u1 * J11;
-            put2(0, a0, a1);
-            put2(1, b0, b1);
+            float2 a = make_float2(J00, J01), b = __fmul2_rn(u, make_float2(J10, J11));
+            put2(0, a);
+            put2(1, b);
 #pragma unroll
             for (int m = 1; m + 1 < MM; m++) {
-                const float c = (float)m * tw;
-                const float n0 = fmaf(c, b0, -w0 * a0), n1 = fmaf(c, b1, -w1 * a1);
-                put2(m + 1, n0, n1);
-                a0 = b0;
-                b0 = n0;
-                a1 = b1;
-                b1 = n1;
+                const float2 n = __ffma2_rn(bc2((float)m * tw), b, neg2(__fmul2_rn(w, a)));
+                put2(m + 1, n);
+                a = b;
+                b = n;
             }
             fence_async_smem();
             __syncwarp();
@@ -547,15 +550,13 @@ __global__ void __launch_bounds__(PREP_THREADS) prep_b(mma_hankel_problem P, flo
 // same order as prep_b, hence the same B operand bit for bit.  The wait for a stage is bounded;
 // on a timeout the CTA sets *status, lets its copies land and writes NaN row scales.
 constexpr int kPrepG = 4;  // planes per ring stage
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
 __global__ void __launch_bounds__(PREP_THREADS, 2)
     prep_b_ring(mma_hankel_problem P, float2 u_ref, const double* og, const double* rg, const float4* dinv,
                 const float2* __restrict__ src, const double2* __restrict__ pre, __half* Bh, __half* Bl,
                 float* alpha, int64_t rpad, int64_t zpad, int ns, int* status)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    __shared__ float wmax[2][kPrepG][PREP_THREADS / 32];  // double-buffered by stage parity
+    __shared__ __align__(16) float wmax[2][kPrepG][PREP_THREADS / 32];  // double-buffered by stage parity
     __shared__ unsigned s_dumax;
     const int64_t o = blockIdx.x, Nr = P.n_r, No = P.n_omega;
     const int Nz = (int)P.n_z;
@@ -566,6 +567,7 @@ __global__ void __launch_bounds__(PREP_THREADS, 2)
     const int n_st = (int)((zpad + kPrepG - 1) / kPrepG);  // stages over the padded planes
     const int n_live = (Nz + kPrepG - 1) / kPrepG;         // stages with source rows to copy
     const uint32_t row_bytes = (uint32_t)Nr * 8u;
+    const int rph = (int)(rpad / 2);  // half2 words per B row
     const float2* row0 = src + o * P.omega_stride;
     auto issue = [&](int j, int slot) {
         const int k0 = j * kPrepG, np = Nz - k0 < kPrepG ? Nz - k0 : kPrepG;
@@ -721,28 +723,31 @@ __global__ void __launch_bounds__(PREP_THREADS, 2)
             s = 0;
             ph ^= 1u;
         }
+        // the stage's rows start at row 2 k0 of this frequency; a row is rph half2 words and the
+        // thread's pair pp sits at word t + 256 pp
+        const int64_t row0 = (o * 2 * zpad + 2 * (int64_t)k0) * rph + t;
+        __half2* bh = reinterpret_cast<__half2*>(Bh) + row0;
+        __half2* bl = reinterpret_cast<__half2*>(Bl) + row0;
+        const float4* wm = reinterpret_cast<const float4*>(&wmax[par][0][0]);
 #pragma unroll
         for (int u = 0; u < kPrepG; u++) {
-            const int64_t kz = k0 + u;
-            if (kz >= zpad) break;
-            float al = 0.f;
-#pragma unroll
-            for (int q = 0; q < PREP_THREADS / 32; q++) al = fmaxf(al, wmax[par][u][q]);
+            if (k0 + u >= zpad) break;
+            const float4 w0 = wm[2 * u], w1 = wm[2 * u + 1];  // the 8 warps' maxima
+            const float al = fmaxf(fmaxf(fmaxf(w0.x, w0.y), fmaxf(w0.z, w0.w)), fmaxf(fmaxf(w1.x, w1.y), fmaxf(w1.z, w1.w)));
             const float sc = al > 0.f ? 1.0f / al : 0.f;
-            if (t == 0) alpha[o * zpad + kz] = al;
+            if (t == 0) alpha[o * zpad + k0 + u] = al;
 #pragma unroll
             for (int pp = 0; pp < PREP_PAIRS; pp++) {
-                const int64_t r0 = 2 * (t + (int64_t)PREP_THREADS * pp);
-                if (r0 >= rpad) continue;
+                if (2 * (t + PREP_THREADS * pp) >= rpad) continue;
 #pragma unroll
                 for (int c = 0; c < 2; c++) {
                     const float2 x = __fmul2_rn(c ? aim[u][pp] : are[u][pp], bc2(sc));
                     const __half2 h = __float22half2_rn(x);
                     const float2 hb = __half22float2(h);
                     const __half2 l = __float22half2_rn(__fadd2_rn(x, neg2(hb)));
-                    const int64_t idx = ((o * 2 * zpad + 2 * kz + c) * rpad + r0) / 2;
-                    reinterpret_cast<__half2*>(Bh)[idx] = h;
-                    reinterpret_cast<__half2*>(Bl)[idx] = l;
+                    const int off = (2 * u + c) * rph + PREP_THREADS * pp;
+                    bh[off] = h;
+                    bl[off] = l;
                 }
             }
         }
