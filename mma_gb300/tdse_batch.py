@@ -429,14 +429,21 @@ class TDSEBatchPlan:
     def load_fields(self, fields):
         """Copy the raw fields (a [n_inst, n_f] tensor or a list of 1-D tensors) into the
         plan's device buffer (on the current stream; no host synchronisation)."""
-        rows = [fields[i] for i in range(fields.shape[0])] if torch.is_tensor(fields) and fields.dim() == 2 \
-            else list(fields)
+        uniform = torch.is_tensor(fields) and fields.dim() == 2
+        rows = [fields[i] for i in range(fields.shape[0])] if uniform else list(fields)
         if len(rows) != self.n_inst:
             raise ValueError("expected %d fields" % self.n_inst)
+        if uniform:  # one copy of the whole tensor (asynchronous from pinned host memory), then
+            # each length group from it on the device: a slice when its instances are consecutive
+            src = fields.to(self.device, torch.float64, non_blocking=True)
         for L, idx, raw_off, _ in self.len_groups:
             dst = self.raw[raw_off:raw_off + len(idx) * L].view(len(idx), L)
-            if torch.is_tensor(fields) and fields.dim() == 2:
-                dst.copy_(fields[torch.as_tensor(idx, device=fields.device)].to(torch.float64), non_blocking=True)
+            if uniform:
+                i0 = int(idx[0])
+                if np.array_equal(np.asarray(idx), np.arange(i0, i0 + len(idx))):
+                    dst.copy_(src[i0:i0 + len(idx)], non_blocking=True)
+                else:
+                    dst.copy_(src[torch.as_tensor(idx, device=self.device)], non_blocking=True)
             else:
                 for j, i in enumerate(idx):
                     if rows[i].numel() != L:
