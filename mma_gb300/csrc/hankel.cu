@@ -510,12 +510,11 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
                 const float2 kh = make_float2(kk.x, kk.z), kl = make_float2(kk.y, kk.w);
                 const float2 yh = __fmul2_rn(kh, f2b(rh));
                 const float2 yl = __fadd2_rn(__ffma2_rn(kh, f2b(rh), f2n(yh)), __ffma2_rn(kh, f2b(rl), __fmul2_rn(kl, f2b(rh))));
-                float J0a, J1a, J0b, J1b;
-                bessel01<true>(yh.x, yl.x, J0a, J1a);
-                bessel01<true>(yh.y, yl.y, J0b, J1b);
+                float2 J0, J1;
+                bessel01x2<true>(yh, yl, J0, J1);
                 const float2 y = __fadd2_rn(yh, yl);
-                float2 K0 = make_float2(J0a, J0b);
-                float2 K1 = __fmul2_rn(__fmul2_rn(f2b(0.5f * s), y), make_float2(J1a, J1b));
+                float2 K0 = J0;
+                float2 K1 = __fmul2_rn(__fmul2_rn(f2b(0.5f * s), y), J1);
                 const float2 q2 = __fmul2_rn(__fmul2_rn(f2b(0.25f * s * s), y), y);
                 const float4 b0 = B4[q / 2], b1 = B4[(rtile + q) / 2];
                 float2 ia = __ffma2_rn(make_float2(b0.x, b0.y), f2b(K0.x), __fmul2_rn(make_float2(b1.x, b1.y), f2b(K1.x)));

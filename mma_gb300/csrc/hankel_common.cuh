@@ -125,6 +125,82 @@ __device__ __forceinline__ void bessel01(float yh, float yl, float& J0, float& J
     }
 }
 
+// The same J0 and J1 for two arguments at once (x = (yh + yl).x and .y).  When both are >= 3 the
+// modulus/phase branch runs as packed FP32x2 instructions, each lane the operations of bessel01 in
+// the same order (the same bits); otherwise each lane takes bessel01.
+__device__ __forceinline__ float2 b2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 poly6(float2 t, float c6, float c5, float c4, float c3, float c2, float c1, float c0)
+{
+    return __ffma2_rn(t, __ffma2_rn(t, __ffma2_rn(t, __ffma2_rn(t, __ffma2_rn(t, __ffma2_rn(t, b2(c6), b2(c5)), b2(c4)),
+                                                              b2(c3)), b2(c2)), b2(c1)), b2(c0));
+}
+__device__ __forceinline__ float2 poly5(float2 t, float c5, float c4, float c3, float c2, float c1, float c0)
+{
+    return __ffma2_rn(t, __ffma2_rn(t, __ffma2_rn(t, __ffma2_rn(t, __ffma2_rn(t, b2(c5), b2(c4)), b2(c3)), b2(c2)),
+                                    b2(c1)), b2(c0));
+}
+__device__ __forceinline__ void sincos_small2(float2 p, float2& s, float2& c)
+{
+    const float2 p2 = __fmul2_rn(p, p);
+    s = __fmul2_rn(p, __ffma2_rn(p2, __ffma2_rn(p2, b2(8.33333333e-3f), b2(-1.66666667e-1f)), b2(1.0f)));
+    c = __ffma2_rn(p2, __ffma2_rn(p2, b2(4.16666667e-2f), b2(-0.5f)), b2(1.0f));
+}
+template <bool WANT_J1>
+__device__ __forceinline__ void bessel01x2(float2 yh, float2 yl, float2& J0, float2& J1)
+{
+    if (!(yh.x >= 3.0f && yh.y >= 3.0f)) {
+        bessel01<WANT_J1>(yh.x, yl.x, J0.x, J1.x);
+        bessel01<WANT_J1>(yh.y, yl.y, J0.y, J1.y);
+        return;
+    }
+    const float2 t = make_float2(__fdividef(3.0f, yh.x), __fdividef(3.0f, yh.y));
+    // reduce_2pi, lane by lane
+    const float2 kk = make_float2(rintf(yh.x * 0.159154943f), rintf(yh.y * 0.159154943f));
+    const float2 nk = make_float2(-kk.x, -kk.y);
+    float2 red = __ffma2_rn(nk, b2(6.28125f), yh);
+    red = __ffma2_rn(nk, b2(1.93500518798828125e-3f), red);
+    red = __ffma2_rn(nk, b2(3.0199159819370158e-07f), red);
+    red = __fadd2_rn(red, yl);
+    const float2 sq = make_float2(rsqrtf(yh.x), rsqrtf(yh.y));
+    // sincos_reduced, lane by lane
+    const float2 k = make_float2(rintf(red.x * 0.636619772f), rintf(red.y * 0.636619772f));
+    const float2 mk = make_float2(-k.x, -k.y);
+    float2 r = __ffma2_rn(mk, b2(1.5703125f), red);
+    r = __ffma2_rn(mk, b2(4.83826794896619e-4f), r);
+    const float2 r2 = __fmul2_rn(r, r);
+    const float2 ps = __fmul2_rn(
+        r, __ffma2_rn(r2, __ffma2_rn(r2, __ffma2_rn(r2, __ffma2_rn(r2, b2(2.75573192e-6f), b2(-1.98412698e-4f)),
+                                                    b2(8.33333333e-3f)), b2(-1.66666667e-1f)), b2(1.0f)));
+    const float2 pc = __ffma2_rn(r2, __ffma2_rn(r2, __ffma2_rn(r2, __ffma2_rn(r2, b2(2.48015873e-5f), b2(-1.38888889e-3f)),
+                                                              b2(4.16666667e-2f)), b2(-0.5f)), b2(1.0f));
+    float2 sr, cr;
+    {
+        const int qx = (int)k.x & 3, qy = (int)k.y & 3;
+        const float ssx = (qx & 1) ? pc.x : ps.x, ccx = (qx & 1) ? ps.x : pc.x;
+        const float ssy = (qy & 1) ? pc.y : ps.y, ccy = (qy & 1) ? ps.y : pc.y;
+        sr = make_float2((qx & 2) ? -ssx : ssx, (qy & 2) ? -ssy : ssy);
+        cr = make_float2(((qx + 1) & 2) ? -ccx : ccx, ((qy + 1) & 2) ? -ccy : ccy);
+    }
+    const float2 a = __fadd2_rn(cr, sr), b = __fadd2_rn(cr, make_float2(-sr.x, -sr.y));
+    const float2 f0 = poly6(t, 0.00014476f, -0.00072805f, 0.00137237f, -0.00009512f, -0.00552740f, -0.00000077f,
+                            0.79788456f);
+    const float2 p0 = __fmul2_rn(t, poly5(t, 0.00013558f, -0.00029333f, -0.00054125f, 0.00262573f, -0.00003954f,
+                                          -0.04166397f));
+    float2 s0, c0;
+    sincos_small2(p0, s0, c0);
+    J0 = __fmul2_rn(__fmul2_rn(f0, sq), __fmul2_rn(b2(0.707106781f), __ffma2_rn(c0, a, __fmul2_rn(s0, b))));
+    if (WANT_J1) {
+        const float2 f1 = poly6(t, -0.00020033f, 0.00113653f, -0.00249511f, 0.00017105f, 0.01659667f, 0.00000156f,
+                                0.79788456f);
+        const float2 p1 = __fmul2_rn(t, poly5(t, -0.00029166f, 0.00079824f, 0.00074348f, -0.00637879f, 0.00005650f,
+                                              0.12499612f));
+        float2 s1, c1;
+        sincos_small2(p1, s1, c1);
+        const float2 cb = __fmul2_rn(c1, b);
+        J1 = __fmul2_rn(__fmul2_rn(f1, sq), __fmul2_rn(b2(0.707106781f), __ffma2_rn(s1, a, make_float2(-cb.x, -cb.y))));
+    }
+}
+
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 {
     s = a + b;

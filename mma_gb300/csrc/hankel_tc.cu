@@ -266,9 +266,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             const float2 rh = make_float2(rv.x, rv.z), rl = make_float2(rv.y, rv.w);
             const float2 yh = __fmul2_rn(bc2(kh), rh);
             const float2 yl = __fadd2_rn(__ffma2_rn(bc2(kh), rh, neg2(yh)), __ffma2_rn(bc2(kh), rl, __fmul2_rn(bc2(kl), rh)));
-            float J00, J10, J01, J11;
-            bessel01<true>(yh.x, yl.x, J00, J10);
-            bessel01<true>(yh.y, yl.y, J01, J11);
+            float2 J0, J1;
+            bessel01x2<true>(yh, yl, J0, J1);
             // K^_m = u^m J_m(y), u = y / y_max <= 1:  K^_{m+1} = (2m / y_max) K^_m - u^2 K^_{m-1}
             const float2 u = __fmul2_rn(__fadd2_rn(yh, yl), bc2(iy));
             const float2 w = __fmul2_rn(u, u);
@@ -280,7 +279,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 *reinterpret_cast<__half2*>(pa) = h;
                 *reinterpret_cast<__half2*>(pa + A_BYTES) = l;
             };
-            float2 a = make_float2(J00, J01), b = __fmul2_rn(u, make_float2(J10, J11));
+            float2 a = J0, b = __fmul2_rn(u, J1);
             put2(0, a);
             put2(1, b);
 #pragma unroll
