@@ -23,6 +23,10 @@ int mma_probe_fma_peak(int precision, double *flops_per_s);
  * *status becomes 1, and the kernel frees its tensor memory and returns without writing D;
  * the context stays usable. */
 int mma_tc_selftest(const void *A, const void *B, float *D, int use_tma, int *status, void *stream);
+/* One tcgen05.mma kind::tf32 (M 128, N 16, K 8) from K-major core-matrix tiles without swizzle,
+ * the operand layout of the tensor-core stage 1 of the fast far field: D[128][16] = A[128][8]
+ * B[16][8]^T (row-major FP32, device pointers); *status = 2 if the bounded wait for the MMA ran out. */
+int mma_s1tc_selftest(const float *A, const float *B, float *D, int *status, void *stream);
 
 #ifdef __cplusplus
 }

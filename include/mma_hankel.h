@@ -76,6 +76,14 @@ size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem *p, const mma_hank
  * for all n_z planes; complex128 planes [slot][n_rho][n_omega], ff [n_rho][n_omega]). */
 int mma_hankel_ff_from_planes(const mma_hankel_problem *p, const double *zgrid, const int64_t *plane_slot,
                               const double *planes, double *ff, void *stream);
+/* Stage 1 of mma_hankel_fast (the z contraction B_m): mode 1 (default) runs it on the CUDA cores
+ * (FP32 FMAs, the streamed ring form); mode 0 runs it on the tensor cores where it applies -- 16
+ * series terms, a complex64 source with rows on 16-byte boundaries (even n_r and strides),
+ * pre-factors per (plane, frequency), at most about 1000 planes -- as a TF32 split-precision GEMM
+ * (tcgen05, FP32 accumulation in TMEM).  On config 3 the tensor-core form is slower and less
+ * accurate (per-harmonic error 6.6e-6 against 3.4e-7).  Process-wide setting; MMA_ERR_ARG for
+ * other modes. */
+int mma_hankel_set_stage1(int mode);
 /* Status of the last mma_hankel_fast call on this scratch (synchronises the stream): MMA_OK, or
  * MMA_ERR_TIMEOUT if a bounded wait of its streamed stage 1 gave up (that call's far field is then
  * NaN).  The streamed stage 1 runs for complex64 sources with rows on 16-byte boundaries (even

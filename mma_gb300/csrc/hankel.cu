@@ -12,6 +12,7 @@
 #include "../../include/mma_hankel.h"
 #include "../../include/mma_tdse.h"
 #include "hankel_common.cuh"
+#include "s1tc.cuh"
 #include "tc_sm100.cuh"
 
 namespace mma {
@@ -716,6 +717,12 @@ constexpr int kTerms[] = {8, 12, 16, 20, 24, 32, 40, 48};
 
 using namespace mma::hk;
 
+// Stage 1 of the fast form: 1 (default) = the CUDA-core ring; 0 = on the tensor cores where it
+// applies (16 terms, complex64 rows on 16-byte boundaries), else the CUDA-core ring.  The
+// tensor-core form measured slower and less accurate on config 3 (TF32 split precision, N = 16
+// MMAs that keep the tensor pipe about 20% busy), so it is not the default.
+static int g_stage1_mode = 1;
+
 extern "C" int mma_hankel_plain(const mma_hankel_problem* p, const double* ogrid, const double* rgrid,
                                 const double* zgrid, const double* rho, const void* source, const double* pre,
                                 double* ff, const int64_t* plane_slot, int n_planes, double* planes, void* stream)
@@ -820,6 +827,13 @@ extern "C" size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem* p, con
     return asel_off(p, plan) + up256(sizeof(float2) * 2 * (size_t)p->n_omega * (size_t)p->n_r);
 }
 
+extern "C" int mma_hankel_set_stage1(int mode)
+{
+    if (mode != 0 && mode != 1) return MMA_ERR_ARG;
+    g_stage1_mode = mode;
+    return MMA_OK;
+}
+
 extern "C" int mma_hankel_fast_status(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
                                       const void* scratch, void* stream)
 {
@@ -860,10 +874,22 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
     bool ringed = false;
     if constexpr (MM % 4 == 0 && MM <= 16) {
         const int ns = ring_stages<MM>(p, src);
-        if (ns > 0) {  // stage 1 through the shared-memory ring
+        int tc_done = 0;  // 1: stage 1 ran on the tensor cores
+        if (ns > 0) {  // stage 1 through the shared-memory ring: on the tensor cores, or the CUDA cores
             ringed = true;
             const int64_t nt = p->n_omega > p->n_r ? p->n_omega : p->n_r;
             fast_wr_tables<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(*p, og, rg, ktab, rtab);
+            if (g_stage1_mode == 0) {
+                float uh, ul;
+                const double u = 1.0 / (2.0 * plan->d_ref);
+                uh = (float)u;
+                ul = (float)(u - (double)uh);
+                tc_done = mma::s1tc::stage1_tc_launch(*p, src, pre, ptab, ktab, rtab, make_float2(uh, ul), Bp, MM,
+                                                      status, st);
+                if (tc_done < 0) return tc_done;
+            }
+        }
+        if (ns > 0 && tc_done == 0) {
             if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
             const size_t sr = (size_t)ns * kG * kRingR * 8 + (size_t)MM * 8 * kRingR +
                               (size_t)p->n_z * (MM * 4 + 16) + 2 * (size_t)ns * 8 + 16;

@@ -215,6 +215,44 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_
         : "memory");
 }
 
+// Instruction descriptor, kind::tf32: TF32 A and B (both K-major), FP32 accumulator, M x N.
+__host__ __device__ constexpr uint32_t idesc_tf32_f32(int M, int N)
+{
+    return (1u << 4)                          // D format: F32
+           | (2u << 7) | (2u << 10)           // A, B format: TF32
+           | ((uint32_t)(N >> 3) << 17)       // N / 8
+           | ((uint32_t)(M >> 4) << 24);      // M / 16
+}
+
+// Shared-memory matrix descriptor, K-major without swizzle: core matrices of 8 rows x 16 bytes
+// (128 contiguous bytes), `lbo` bytes between core matrices adjacent in K, `sbo` bytes between
+// core matrices adjacent in M (or N).
+__device__ __forceinline__ uint64_t sdesc_plain(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4)   // start address / 16
+           | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16)
+           | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32)
+           | ((uint64_t)1u << 46);               // descriptor version (tcgen05); layout: no swizzle
+}
+
+// byte offset of element (row, k) of a K-major TF32 tile stored as core matrices: 8-row groups
+// `sbo` bytes apart, 4-element (16-byte) K groups `lbo` bytes apart
+__host__ __device__ constexpr uint32_t plain_offset(uint32_t row, uint32_t k, uint32_t lbo, uint32_t sbo)
+{
+    return (row >> 3) * sbo + (k >> 2) * lbo + (row & 7u) * 16u + (k & 3u) * 4u;
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T with TF32 operands (K = 8 per instruction), issued by one thread
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
 // the mbarrier receives one arrival when all tcgen05.mma issued so far by this thread completed
 __device__ __forceinline__ void mma_commit(uint64_t* bar)
 {

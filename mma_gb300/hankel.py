@@ -85,6 +85,8 @@ def _sig():
     lib.mma_hankel_planes_tc_run.restype = c_int
     lib.mma_hankel_planes_tc_status.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p]
     lib.mma_hankel_planes_tc_status.restype = c_int
+    lib.mma_hankel_set_stage1.argtypes = [c_int]
+    lib.mma_hankel_set_stage1.restype = c_int
     lib.mma_hankel_ff_from_planes.argtypes = [P, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
     lib.mma_hankel_ff_from_planes.restype = c_int
     lib.mma_hankel_fast_status.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p]
@@ -429,6 +431,17 @@ def _dev(a, device):
 
 TC_MIN_PLANES = 16  # from this many requested planes the fast form computes them on the tensor cores
 SERIES_PLANES = 2  # up to this many planes the fast pass evaluates inside its series stage
+
+
+def set_stage1_form(form):
+    """Stage 1 of the fast form (the z contraction): "cuda" (default) runs it on the CUDA cores
+    (FP32 FMAs); "tc" runs it on the tensor cores where it applies (16 series terms, complex64
+    source rows on 16-byte boundaries, pre-factors per (plane, frequency)) as a TF32
+    split-precision GEMM, which on config 3 is slower and about 20 times less accurate.  Other
+    problems always take the CUDA cores."""
+    if form not in ("tc", "cuda"):
+        raise ValueError("stage-1 form must be 'tc' or 'cuda'")
+    _check(_sig().mma_hankel_set_stage1(0 if form == "tc" else 1), "mma_hankel_set_stage1")
 
 
 def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_field=True, planes=(), form="plain",

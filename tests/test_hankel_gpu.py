@@ -149,3 +149,37 @@ def test_series_planes_match_direct_planes(gpu_lib, n_r, source):
         assert per_harmonic(p2[k].cpu().numpy(), p3[k].cpu().numpy()) < 1e-6, k
     _, p1, _ = H.far_field(og, rg, zg, rho, S, 1.0, pre, True, planes=(7,), form="fast", planes_via="direct")
     assert per_harmonic(p1[7].cpu().numpy(), p3[7].cpu().numpy()) < 1e-6
+
+
+@pytest.mark.parametrize("n_r,near", [(512, True), (300, False)], ids=["512 r, near field", "300 r, far only"])
+def test_stage1_tensor_cores_match_cuda_cores(gpu_lib, n_r, near):
+    """Stage 1 of the fast form on the tensor cores (TF32 split precision, 16 series terms) against
+    the CUDA-core ring (FP32 FMAs) on the same complex64 source, and both against the plain FP64
+    form: the two forms agree within 2e-5 per harmonic (TF32 split precision) and both stay within
+    the fast form's bound against FP64.  300 radii leave a partial CTA block."""
+    from mma_gb300 import hankel as H
+
+    omega0 = 0.057 / 2.4188843265857e-17
+    rg = np.linspace(0.0, 200e-6, n_r)
+    zg = np.linspace(-5e-3, 5e-3, 61)
+    og = np.linspace(10 * omega0, 42 * omega0, 12)
+    rho = np.linspace(0.0, 5e-3, 48)
+    rng = np.random.default_rng(n_r)
+    S = np.exp(-(rg / 50e-6) ** 2)[None, None, :] * np.exp(1j * rng.uniform(0, 6.28, (len(zg), len(og))))[:, :, None]
+    S = torch.tensor(S, dtype=torch.complex64, device="cuda")
+    pre = np.exp(1j * np.linspace(0, 1, len(zg)))[:, None] * np.exp(-0.1j * np.arange(len(og)))[None, :]
+    out = {}
+    try:
+        for form in ("tc", "cuda"):
+            H.set_stage1_form(form)
+            out[form] = H.far_field(og, rg, zg, rho, S, 1.0, pre, near, planes=(0, -1), form="fast", tol=1e-9)
+    finally:
+        H.set_stage1_form("cuda")
+    assert out["tc"][2]["n_terms"] == 16
+    ff64, p64, _ = H.far_field(og, rg, zg, rho, S, 1.0, pre, near, planes=(0, -1), form="plain")
+    ff_tc, ff_cc = out["tc"][0].cpu().numpy(), out["cuda"][0].cpu().numpy()
+    assert not np.array_equal(ff_tc, ff_cc)  # the two forms really ran
+    assert per_harmonic(ff_tc, ff_cc) < 2e-5
+    assert per_harmonic(ff_tc, ff64.cpu().numpy()) < FAST_TOL
+    for k in (0, len(zg) - 1):
+        assert per_harmonic(out["tc"][1][k].cpu().numpy(), p64[k].cpu().numpy()) < FAST_TOL

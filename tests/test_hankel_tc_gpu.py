@@ -69,6 +69,26 @@ def test_tcgen05_bounded_wait_runs_out(gpu_lib):
     assert bool((D == 32.0).all())
 
 
+def test_tf32_tile_layout(gpu_lib):
+    """One tcgen05.mma kind::tf32 (M 128, N 16, K 8) from K-major core-matrix tiles without
+    swizzle, the operand layout of the tensor-core stage 1: integer operands are exact in TF32, so
+    D = A B^T is exact."""
+    lib = gpu_lib
+    lib.mma_s1tc_selftest.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_void_p]
+    lib.mma_s1tc_selftest.restype = ctypes.c_int
+    rng = np.random.default_rng(7)
+    A = rng.integers(-8, 9, (128, 8)).astype(np.float32)
+    B = rng.integers(-8, 9, (16, 8)).astype(np.float32)
+    dA, dB = torch.tensor(A, device="cuda"), torch.tensor(B, device="cuda")
+    dD = torch.full((128, 16), float("nan"), dtype=torch.float32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.mma_s1tc_selftest(dA.data_ptr(), dB.data_ptr(), dD.data_ptr(), status.data_ptr(), st) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert np.array_equal(dD.cpu().numpy(), A @ B.T)
+
+
 def _problem(n_omega=24, n_r=200, n_z=40, n_rho=50, seed=0, rho_max=5e-3):
     omega0 = 0.057 / 2.4188843265857e-17
     rgrid = np.linspace(0.0, 200e-6, n_r)
