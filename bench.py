@@ -157,6 +157,65 @@ def run_config2(args, device):
     return out
 
 
+def run_config0(args, device):
+    """Config 0: one 8001-site instance (10-cycle 800 nm sin^2 pulse, E0 = 0.0534 a.u.) through the
+    PythonCTDSE surface -- the legacy C-ABI in the FP64 plain form, ground state, propagation and
+    spectra, host arrays in and out -- timed wall-clock per call; the same instance in the
+    float-float form through the batched API; and the oracle port on one host core.  The field is
+    the one the reference DLL was run on for tests/golden/tdse_config0.npz, so each form's
+    relative L2 error against the reference's own outputs is reported beside its time."""
+    import torch
+
+    from mma_gb300.tdse import TDSE_DLL, run_single
+    from mma_gb300.tdse_batch import TDSEGrids, run_batch
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "tdse_config0.npz"))
+    t, E = g["t"], g["E"]
+    num_r, dx, a = int(g["params"][0]), float(g["params"][1]), float(g["params"][2])
+    series = ("sourceterm", "PopTot", "PopInt", "expval", "Fsourceterm")
+
+    def errs(res):
+        return {k: float(np.linalg.norm(np.asarray(res[k]) - g[k]) / np.linalg.norm(g[k])) for k in series}
+
+    dll = TDSE_DLL()
+    run_single(dll, t, E, num_r=num_r, dx=dx, trg_a=a, CV=1e-15)  # warm-up (DFT plan, module load)
+    secs = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        r = run_single(dll, t, E, num_r=num_r, dx=dx, trg_a=a, CV=1e-15)
+        secs.append(time.perf_counter() - t0)
+    site_steps = float((num_r + 1) * r["Nt"])
+    out = {"instances": 1, "sites": num_r + 1, "steps": int(r["Nt"]), "site_steps": site_steps,
+           "legacy_fp64": {"seconds_per_call": float(np.median(secs)), "calls": len(secs),
+                           "site_steps_per_s": site_steps / float(np.median(secs)),
+                           "rel_l2_vs_reference": errs(r),
+                           "note": "wall clock of the PythonCTDSE-surface call: ground state, one CTA "
+                                   "propagating, spectra, host copies"}}
+    dtf = float(t[1] - t[0])
+    grids = TDSEGrids([dict(num_r=num_r, dx=dx, trg_a=a)], dt=dtf, df64=True)
+    Ed = torch.tensor(E[None, :], device=device)
+    for prec in ("fp64", "df64"):
+        run_batch(grids, Ed, dt_field=dtf, tmax=float(t[-1] - t[0]), precision=prec)  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        res = run_batch(grids, Ed, dt_field=dtf, tmax=float(t[-1] - t[0]), precision=prec)
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) * 1e-3
+        host = {k: res[k][0].cpu().numpy() for k in series}
+        out["batch_" + prec] = {"seconds": sec, "site_steps_per_s": site_steps / sec,
+                                "rel_l2_vs_reference": errs(host)}
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        _cpu_instance(("port", None, t, E, num_r, dx, a))
+        cpu = time.perf_counter() - t0
+        out["cpu_port_1_core"] = {"seconds": cpu, "site_steps_per_s": site_steps / cpu,
+                                  "note": "the oracle's C restatement, one instance on one host core"}
+        out["legacy_speedup_vs_1_core"] = cpu / out["legacy_fp64"]["seconds_per_call"]
+    return out
+
+
 def run_config4(args, device):
     """Adjoint: 256 instances on the config-1 grid (every 8th instance of the config-1 focus),
     L = harmonic yield over [21, 31] omega0, checkpoints every 256 steps; timing of the
@@ -625,6 +684,7 @@ def l2_flush(buf):
 
 WORKLOADS = {
     # name: (n_r, n_z, n_cycles, hankel n_omega)
+    "config0": (64, 32, 10, 2048),  # one instance through the PythonCTDSE surface (run_config0)
     "config1": (64, 32, 10, 2048),
     "config2": (64, 32, 10, 2048),  # uneven batch (run_config2), reported on its own line
     "config4": (64, 32, 10, 2048),  # adjoint gradients (run_config4), reported on its own line
@@ -856,13 +916,14 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
-    if args.workload in ("config2", "config3", "config4", "analysis", "small_wide", "small_adjoint", "small_ff"):
+    if args.workload in ("config0", "config2", "config3", "config4", "analysis", "small_wide", "small_adjoint",
+                         "small_ff"):
         import torch
 
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
         torch.cuda.set_device(dev)
-        fn = {"config2": run_config2, "config3": run_hankel, "small_ff": run_hankel, "config4": run_config4,
-              "analysis": run_analysis, "small_wide": run_profile_case,
+        fn = {"config0": run_config0, "config2": run_config2, "config3": run_hankel, "small_ff": run_hankel,
+              "config4": run_config4, "analysis": run_analysis, "small_wide": run_profile_case,
               "small_adjoint": run_profile_case}[args.workload]
         print(json.dumps({"workload": args.workload, "result": fn(args, dev)}))
         return
@@ -952,6 +1013,7 @@ def main():
         # the uneven batch (config 2: 4096 instances, one launch per form) and the adjoint
         # (config 4: 256 instances, central finite differences at 4 samples per instance here;
         # `--workload config4` checks 32)
+        line["config0"] = run_config0(args, dev)
         line["config2"] = run_config2(args, dev)
         if args.fd_samples is None:
             args.fd_samples = 4

@@ -112,6 +112,15 @@ __global__ void fast_plane_table(mma_hankel_problem P, mma_hankel_fast_plan_t F,
 
 __device__ __forceinline__ float2 f2b(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 f2n(float2 a) { return make_float2(-a.x, -a.y); }
+// 16-byte shared-memory load kept where it stands (a volatile asm is neither hoisted out of the
+// loop nor merged): the per-term tables are re-read per radius pair instead of being held in
+// registers across the loop, which would spill
+__device__ __forceinline__ float4 lds4(uint32_t saddr)
+{
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(saddr));
+    return v;
+}
 
 // Per-frequency and per-radius constants of stage 1 as floats: ktab[w] = k_w = w/c as (hi, lo);
 // rtab[r] = (r^2 as (hi, lo), trapezoid weight * r, 0).
@@ -444,12 +453,27 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
 {
     extern __shared__ __align__(16) float smem[];
     const int64_t o = blockIdx.y, Nr = P.n_r, Nrho = P.n_rho, No = P.n_omega;
-    float2* B = reinterpret_cast<float2*>(smem);  // MM * rtile (rtile even)
-    float2* kr = B + MM * rtile;                  // rtile
-    float2* As = kr + rtile;                      // SER: kSeriesPlanes * rtile, A_k of the selected planes
-    float2* Vs = As + kSeriesPlanes * rtile;      // SER: MM pairs (v_k0^m, v_k1^m)
-    if (SER)
-        for (int q = threadIdx.x; q < MM; q += blockDim.x) Vs[q] = vsel[q];
+    // B_m of the tile's radius pairs: row m, pair p = (Re B_m[2p], Re B_m[2p+1], Im B_m[2p], Im B_m[2p+1])
+    float4* B4 = reinterpret_cast<float4*>(smem);  // MM * rtile / 2 (rtile even)
+    float2* kr = reinterpret_cast<float2*>(B4 + MM * (rtile / 2));  // rtile
+    float2* As = kr + rtile;                       // SER: kSeriesPlanes * rtile, A_k of the selected planes
+    float2* Vs = As + kSeriesPlanes * rtile;       // SER: MM pairs (v_k0^m, v_k1^m)
+    // per term m the recurrence's constants as broadcast pairs (s m/(m+1), -1/(m(m+1))) and, with
+    // SER, the planes' (v_k0^m, v_k1^m) as broadcast pairs: read whole by one 16-byte load
+    float4* Cm = reinterpret_cast<float4*>(kr + rtile + (SER ? kSeriesPlanes * rtile + MM : 0));
+    float4* Vb = Cm + MM;  // SER
+    const uint32_t cm_s = (uint32_t)__cvta_generic_to_shared(Cm), vb_s = cm_s + 16u * MM;
+    const float s = (float)F.sigma;
+    for (int m = threadIdx.x; m < MM; m += blockDim.x) {
+        const float c1 = s * __fdiv_rn((float)m, (float)(m + 1));
+        const float c2 = m > 0 ? -__fdiv_rn(1.0f, (float)(m * (m + 1))) : 0.f;
+        Cm[m] = make_float4(c1, c1, c2, c2);
+        if (SER) {
+            const float2 v = vsel[m];
+            Vs[m] = v;
+            Vb[m] = make_float4(v.x, v.x, v.y, v.y);
+        }
+    }
     float2 ppart[kSeriesPlanes], phi[kSeriesPlanes], plo[kSeriesPlanes];  // the planes' compensated sums
 #pragma unroll
     for (int i = 0; i < kSeriesPlanes; i++) ppart[i] = phi[i] = plo[i] = make_float2(0.f, 0.f);
@@ -457,7 +481,6 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float rh = 0.f, rl = 0.f;
     if (j < Nrho) split_d(rho[j], rh, rl);
-    const float s = (float)F.sigma;
     float2 part = make_float2(0.f, 0.f), hi = part, lo = part;
     int cnt = 0;
     for (int64_t r0 = 0; r0 < Nr; r0 += rtile) {
@@ -465,7 +488,10 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
         __syncthreads();
         for (int64_t q = threadIdx.x; q < MM * nt; q += blockDim.x) {
             const int64_t m = q / nt, rr = q % nt;
-            B[m * rtile + rr] = Bp[(o * MM + m) * Nr + r0 + rr];
+            const float2 v = Bp[(o * MM + m) * Nr + r0 + rr];
+            float* w = reinterpret_cast<float*>(B4 + m * (rtile / 2) + rr / 2) + (rr & 1);
+            w[0] = v.x;
+            w[2] = v.y;
         }
         for (int64_t q = threadIdx.x; q < nt; q += blockDim.x) {
             float h, l;
@@ -482,7 +508,6 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
             // single-radius operations in the same order); the two radii's J0/J1 seeds are
             // independent chains the scheduler interleaves.  The row stride rtile is even, so a
             // pair's B values and k r / d_ref entries are one 16-byte load each.
-            const float4* B4 = reinterpret_cast<const float4*>(B);
             const float4* kr4 = reinterpret_cast<const float4*>(kr);
             // one radius's terms: the far field's, and with SER the planes' A_k[r] sum_m v_k^m K_m
             auto add_in = [&](float2 in, int64_t q, float2 sv) {
@@ -517,32 +542,35 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
                 float2 K0 = J0;
                 float2 K1 = __fmul2_rn(__fmul2_rn(f2b(0.5f * s), y), J1);
                 const float2 q2 = __fmul2_rn(__fmul2_rn(f2b(0.25f * s * s), y), y);
-                const float4 b0 = B4[q / 2], b1 = B4[(rtile + q) / 2];
-                float2 ia = __ffma2_rn(make_float2(b0.x, b0.y), f2b(K0.x), __fmul2_rn(make_float2(b1.x, b1.y), f2b(K1.x)));
-                float2 ib = __ffma2_rn(make_float2(b0.z, b0.w), f2b(K0.y), __fmul2_rn(make_float2(b1.z, b1.w), f2b(K1.y)));
-                // SER: per radius the pair (sum_m v_k0^m K_m, sum_m v_k1^m K_m)
-                float2 sa = make_float2(0.f, 0.f), sb = sa;
+                // lanes = the two radii throughout: the real and the imaginary parts of the far
+                // field's sum, and (SER) the planes' sums sum_m v_k0^m K_m and sum_m v_k1^m K_m
+                const float4 b0 = B4[q / 2], b1 = B4[rtile / 2 + q / 2];
+                float2 sre = __ffma2_rn(make_float2(b0.x, b0.y), K0, __fmul2_rn(make_float2(b1.x, b1.y), K1));
+                float2 sim = __ffma2_rn(make_float2(b0.z, b0.w), K0, __fmul2_rn(make_float2(b1.z, b1.w), K1));
+                float2 s0 = make_float2(0.f, 0.f), s1 = s0;
                 if (SER) {
-                    sa = __ffma2_rn(Vs[1], f2b(K1.x), f2b(K0.x));  // v^0 = 1
-                    sb = __ffma2_rn(Vs[1], f2b(K1.y), f2b(K0.y));
+                    const float4 v = lds4(vb_s + 16u);
+                    s0 = __ffma2_rn(make_float2(v.x, v.y), K1, K0);  // v^0 = 1
+                    s1 = __ffma2_rn(make_float2(v.z, v.w), K1, K0);
                 }
 #pragma unroll
                 for (int m = 1; m + 1 < MM; m++) {
-                    const float2 K2 = __ffma2_rn(f2b(s * ((float)m / (float)(m + 1))), K1,
-                                                 __fmul2_rn(f2n(__fmul2_rn(q2, f2b(1.0f / (float)(m * (m + 1))))), K0));
-                    const float4 b = B4[((m + 1) * rtile + q) / 2];
-                    ia = __ffma2_rn(make_float2(b.x, b.y), f2b(K2.x), ia);
-                    ib = __ffma2_rn(make_float2(b.z, b.w), f2b(K2.y), ib);
+                    const float4 c = lds4(cm_s + 16u * m);
+                    const float2 K2 = __ffma2_rn(make_float2(c.x, c.y), K1,
+                                                 __fmul2_rn(__fmul2_rn(q2, make_float2(c.z, c.w)), K0));
+                    const float4 b = B4[(m + 1) * (rtile / 2) + q / 2];
+                    sre = __ffma2_rn(make_float2(b.x, b.y), K2, sre);
+                    sim = __ffma2_rn(make_float2(b.z, b.w), K2, sim);
                     if (SER) {
-                        const float2 v = Vs[m + 1];
-                        sa = __ffma2_rn(v, f2b(K2.x), sa);
-                        sb = __ffma2_rn(v, f2b(K2.y), sb);
+                        const float4 v = lds4(vb_s + 16u * (m + 1));
+                        s0 = __ffma2_rn(make_float2(v.x, v.y), K2, s0);
+                        s1 = __ffma2_rn(make_float2(v.z, v.w), K2, s1);
                     }
                     K0 = K1;
                     K1 = K2;
                 }
-                add_in(ia, q, sa);
-                add_in(ib, q + 1, sb);
+                add_in(make_float2(sre.x, sim.x), q, make_float2(s0.x, s1.x));
+                add_in(make_float2(sre.y, sim.y), q + 1, make_float2(s0.y, s1.y));
             }
             if (q < nt) {  // an odd last radius
                 const float2 kk = kr[q];
@@ -553,16 +581,15 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
                 const float y = yh + yl;
                 float K0 = J0, K1 = 0.5f * s * y * J1;
                 const float q2 = 0.25f * s * s * y * y;
-                float2 b0 = B[q], b1 = B[rtile + q];
-                float2 in = make_float2(fmaf(b0.x, K0, b1.x * K1), fmaf(b0.y, K0, b1.y * K1));
+                const float* bq = reinterpret_cast<const float*>(B4 + q / 2) + (q & 1);  // row m at + 2 m rtile
+                float2 in = make_float2(fmaf(bq[0], K0, bq[2 * rtile] * K1), fmaf(bq[2], K0, bq[2 * rtile + 2] * K1));
                 float2 sa = make_float2(0.f, 0.f);
                 if (SER) sa = __ffma2_rn(Vs[1], f2b(K1), f2b(K0));
 #pragma unroll
                 for (int m = 1; m + 1 < MM; m++) {
                     const float K2 = fmaf(s * ((float)m / (float)(m + 1)), K1, -(q2 * (1.0f / (float)(m * (m + 1)))) * K0);
-                    const float2 b = B[(m + 1) * rtile + q];
-                    in.x = fmaf(b.x, K2, in.x);
-                    in.y = fmaf(b.y, K2, in.y);
+                    in.x = fmaf(bq[(m + 1) * 2 * rtile], K2, in.x);
+                    in.y = fmaf(bq[(m + 1) * 2 * rtile + 2], K2, in.y);
                     if (SER) sa = __ffma2_rn(Vs[m + 1], f2b(K2), sa);
                     K0 = K1;
                     K1 = K2;
@@ -923,10 +950,11 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
     // stage 2: B, k r / d_ref and (series planes) their A_k rows per tile of rtile radii
     const int rows = MM + 1 + (ser ? kSeriesPlanes : 0);
     const size_t budget = (ser ? 72 : 96) * 1024;
+    const size_t consts = (ser ? MM * (sizeof(float2) + 2 * sizeof(float4)) : MM * sizeof(float4));
     int rtile = (int)(p->n_r < 512 ? p->n_r : 512);
     rtile += rtile & 1;  // even row stride: stage 2 loads radius pairs as 16-byte words
-    while ((size_t)rows * rtile * sizeof(float2) + MM * sizeof(float2) > budget && rtile > 32) rtile /= 2;
-    const size_t s2 = (size_t)rows * rtile * sizeof(float2) + (ser ? MM * sizeof(float2) : 0);
+    while ((size_t)rows * rtile * sizeof(float2) + consts > budget && rtile > 32) rtile /= 2;
+    const size_t s2 = (size_t)rows * rtile * sizeof(float2) + consts;
     dim3 g2((unsigned)((p->n_rho + kThreads - 1) / kThreads), (unsigned)p->n_omega);
     if (ser) {
         cudaFuncSetAttribute(fast_stage2<MM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
