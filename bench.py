@@ -280,6 +280,7 @@ def run_hankel(args, device):
 
     from mma_gb300 import hankel as H
 
+    H.set_stage1_form(getattr(args, "stage1", "cuda"))
     H.XUV_index.set_constant_index(complex(1 - 1e-5, 1e-7))
     zgrid, rgrid, ogrid, rho, S = config3_inputs(device, n_omega=WORKLOADS[args.workload][3])
     target = H.FSources_provider(zgrid, rgrid, ogrid, FSource=S, device=device)
@@ -883,6 +884,8 @@ def main():
     ap.add_argument("--fd-samples", type=int, default=None,
                     help="finite-difference samples per instance of the adjoint check (config 4: 32)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config1")
+    ap.add_argument("--stage1", choices=("cuda", "tc"), default="cuda",
+                    help="stage 1 of the fast far field: CUDA cores (default) or TF32 tensor cores")
     ap.add_argument("--forms", choices=["all", "both", "fp64", "c64", "df64"], default="all",
                     help="all: FP64, complex64 and float-float; both: FP64 and complex64")
     ap.add_argument("--c64-threads", default="auto",
