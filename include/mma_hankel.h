@@ -91,6 +91,13 @@ int mma_hankel_set_stage1(int mode);
  * which has no waits. */
 int mma_hankel_fast_status(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan, const void *scratch,
                            void *stream);
+/* Copy of the frequency block [n_z][w0:w1][n_r] of a source between host and device (either
+ * direction; the two sides laid out alike): n_z rows of block_bytes, plane_bytes apart on both
+ * sides, as one asynchronous copy on `stream`.  The far field of a pinned host source uploads it
+ * block by block with this and runs each block's fast form while the next block is in flight
+ * (the fast form's per-frequency work is independent, so the result equals the one-shot call). */
+int mma_hankel_copy_block(void *dst, const void *src, int64_t n_z, int64_t plane_bytes, int64_t block_bytes,
+                          void *stream);
 int mma_hankel_fast(const mma_hankel_problem *p, const mma_hankel_fast_plan_t *plan, const double *ogrid,
                     const double *rgrid, const double *zgrid, const double *rho, const void *source, const double *pre,
                     double *ff, const int64_t *plane_slot, int n_planes, double *planes, void *scratch,

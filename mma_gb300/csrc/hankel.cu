@@ -1041,6 +1041,19 @@ extern "C" int mma_hankel_ff_from_planes(const mma_hankel_problem* p, const doub
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }
 
+// A block of frequencies [n_z][w0:w1][n_r] copied between two sources laid out alike (host and
+// device, either direction): n_z rows of block_bytes, the rows plane_bytes apart on both sides.
+// One asynchronous 2-D copy on `stream`.
+extern "C" int mma_hankel_copy_block(void* dst, const void* src, int64_t n_z, int64_t plane_bytes, int64_t block_bytes,
+                                     void* stream)
+{
+    if (!dst || !src || n_z <= 0 || block_bytes <= 0 || plane_bytes < block_bytes) return MMA_ERR_ARG;
+    return cudaMemcpy2DAsync(dst, (size_t)plane_bytes, src, (size_t)plane_bytes, (size_t)block_bytes, (size_t)n_z,
+                             cudaMemcpyDefault, (cudaStream_t)stream) == cudaSuccess
+               ? MMA_OK
+               : MMA_ERR_CUDA;
+}
+
 extern "C" int mma_hankel_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan, const double* ogrid,
                                const double* rgrid, const double* zgrid, const double* rho, const void* source,
                                const double* pre, double* ff, const int64_t* plane_slot, int n_planes,

@@ -87,6 +87,8 @@ def _sig():
     lib.mma_hankel_planes_tc_status.restype = c_int
     lib.mma_hankel_set_stage1.argtypes = [c_int]
     lib.mma_hankel_set_stage1.restype = c_int
+    lib.mma_hankel_copy_block.argtypes = [c_void_p, c_void_p, c_int64, c_int64, c_int64, c_void_p]
+    lib.mma_hankel_copy_block.restype = c_int
     lib.mma_hankel_ff_from_planes.argtypes = [P, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
     lib.mma_hankel_ff_from_planes.restype = c_int
     lib.mma_hankel_fast_status.argtypes = [P, POINTER(FastPlan), c_void_p, c_void_p]
@@ -444,10 +446,16 @@ def set_stage1_form(form):
     _check(_sig().mma_hankel_set_stage1(0 if form == "tc" else 1), "mma_hankel_set_stage1")
 
 
+STREAM_BLOCK = 256  # frequencies per block when a pinned host source is uploaded while computing
+
+
 def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_field=True, planes=(), form="plain",
-              tol=1e-9, stream=None, planes_via="auto", ff_via="auto", _events=None):
-    """Run the far-field kernels.  source: torch complex tensor [Nz, No, Nr] (on the GPU; a host
-    tensor is copied there first).
+              tol=1e-9, stream=None, planes_via="auto", ff_via="auto", _events=None, _omega_max=None):
+    """Run the far-field kernels.  source: torch complex tensor [Nz, No, Nr] with r contiguous (on
+    the GPU, or on the host: a host tensor is copied there first; a pinned host tensor, for the
+    fast form with at most two planes, is uploaded in blocks of STREAM_BLOCK frequencies on a
+    second stream while the blocks already on the device are computed -- the same result as the
+    one-shot call, since every frequency is independent and all blocks share one plan).
     Returns (FF [Nrho, No] complex128 tensor, {plane: [Nrho, No] tensor}, fast plan dict or None).
 
     With form="fast", requested planes are computed in the fast pass (planes_via="direct": up to
@@ -461,17 +469,22 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
     "auto" takes "planes" in that case and "fast" otherwise."""
     lib = _sig()
     if not source.is_cuda:  # the kernels take device pointers only: a host source is copied first
+        if (form == "fast" and source.is_pinned() and source.is_contiguous() and source.dim() == 3
+                and source.shape[1] > STREAM_BLOCK and len(set(planes)) <= SERIES_PLANES):
+            return _far_field_streamed(ogrid, rgrid, zgrid, rho, source, distance, pre_table, near_field, planes,
+                                       tol, stream, planes_via, ff_via)
         source = source.to(torch.device("cuda", torch.cuda.current_device()))
     dev = source.device
     Nz, No, Nr = source.shape
     if len(zgrid) != Nz or len(ogrid) != No or len(rgrid) != Nr:
         raise ValueError("source shape does not match the grids")
-    S = source.contiguous()
+    # planes and frequencies may be strided (a frequency block of a larger source); r is contiguous
+    S = source if source.stride(2) == 1 and source.stride(1) >= Nr and source.stride(0) >= 0 else source.contiguous()
     radial = pre_table is not None and np.ndim(pre_table) == 3
     if pre_table is not None and tuple(np.shape(pre_table)) not in ((Nz, No), (Nz, No, Nr)):
         raise ValueError("pre-factor must be [Nz, No] or [Nz, No, Nr]")
     prob = HankelProblem(No, Nr, Nz, len(rho), float(distance), int(bool(near_field)),
-                         int(S.dtype == torch.complex128), No * Nr, Nr, int(radial))
+                         int(S.dtype == torch.complex128), S.stride(0), S.stride(1), int(radial))
     og, rg, zg, rh = (_dev(a, dev) for a in (ogrid, rgrid, zgrid, rho))
     pre = None
     if pre_table is not None:  # a device tensor is used in place; a host table is copied once per call
@@ -496,11 +509,12 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
                                     S.data_ptr(), ptr(pre), ff.data_ptr(), ptr(slot), len(planes), ptr(pl), st),
                "mma_hankel_plain")
     elif form == "fast":
-        zh = np.ascontiguousarray(zgrid, dtype=np.float64)
+        zh = np.ascontiguousarray(_np(zgrid), dtype=np.float64)
         plan = FastPlan()
+        om = float(np.max(np.abs(_np(ogrid)))) if _omega_max is None else float(_omega_max)
         _check(lib.mma_hankel_fast_plan(zh.ctypes.data_as(POINTER(c_double)), Nz, float(distance),
-                                        float(np.max(np.abs(ogrid))), float(np.max(np.abs(rgrid))),
-                                        float(np.max(np.abs(rho))), float(tol), ctypes.byref(plan)),
+                                        om, float(np.max(np.abs(_np(rgrid)))),
+                                        float(np.max(np.abs(_np(rho)))), float(tol), ctypes.byref(plan)),
                "mma_hankel_fast_plan")
         nb = lib.mma_hankel_fast_scratch_bytes(ctypes.byref(prob), ctypes.byref(plan))
         scratch = torch.empty(int(nb), dtype=torch.uint8, device=dev)
@@ -546,6 +560,62 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
         raise ValueError("form must be 'plain' or 'fast'")
     out_planes = {p: pl[i] for i, p in enumerate(planes)} if planes else {}
     return ff, out_planes, plan_d
+
+
+def _np(a):
+    return a.detach().cpu().numpy() if torch.is_tensor(a) else np.asarray(a)
+
+
+def _far_field_streamed(ogrid, rgrid, zgrid, rho, source, distance, pre_table, near_field, planes, tol, stream,
+                        planes_via, ff_via):
+    """far_field of a pinned host source [Nz, No, Nr]: blocks of STREAM_BLOCK frequencies are
+    copied to the device on a second stream (mma_hankel_copy_block, one 2-D copy per block) and
+    each block's fast form runs on `stream` as soon as its copy has landed, with the plan of the
+    whole frequency range.  Returns once every block's copy has completed (the host source may
+    then be released); the far field itself is ordered on `stream`."""
+    lib = _sig()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    comp = stream or torch.cuda.current_stream(dev)
+    Nz, No, Nr = source.shape
+    if len(zgrid) != Nz or len(ogrid) != No or len(rgrid) != Nr:
+        raise ValueError("source shape does not match the grids")
+    with torch.cuda.stream(comp):
+        S = torch.empty(source.shape, dtype=source.dtype, device=dev)
+        og = _dev(ogrid, dev)
+        pre = None
+        if pre_table is not None:
+            pre = pre_table.to(device=dev, dtype=torch.complex128) if torch.is_tensor(pre_table) else \
+                torch.as_tensor(np.ascontiguousarray(pre_table, dtype=np.complex128), device=dev)
+    copy_s = torch.cuda.Stream(device=dev)
+    copy_s.wait_stream(comp)  # S is allocated on comp
+    S.record_stream(copy_s)
+    esz = source.element_size()
+    bounds = list(range(0, No, STREAM_BLOCK)) + [No]
+    landed = []
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        off = a * Nr * esz
+        _check(lib.mma_hankel_copy_block(S.data_ptr() + off, source.data_ptr() + off, Nz, No * Nr * esz,
+                                         (b - a) * Nr * esz, copy_s.cuda_stream), "mma_hankel_copy_block")
+        ev = torch.cuda.Event()
+        ev.record(copy_s)
+        landed.append(ev)
+    omax = float(np.max(np.abs(_np(ogrid))))
+    ff = out_planes = plan = None
+    with torch.cuda.stream(comp):
+        for (a, b), ev in zip(zip(bounds[:-1], bounds[1:]), landed):
+            comp.wait_event(ev)
+            pre_b = None if pre is None else pre[:, a:b]
+            ffb, plb, plan = far_field(og[a:b], rgrid, zgrid, rho, S[:, a:b], distance, pre_b, near_field, planes,
+                                       form="fast", tol=tol, stream=comp, planes_via=planes_via, ff_via=ff_via,
+                                       _omega_max=omax)
+            if ff is None:
+                ff = torch.empty(ffb.shape[0], No, dtype=ffb.dtype, device=dev)
+                out_planes = {p: torch.empty(v.shape[0], No, dtype=v.dtype, device=dev) for p, v in plb.items()}
+            ff[:, a:b] = ffb
+            for p, v in plb.items():
+                out_planes[p][:, a:b] = v
+    landed[-1].synchronize()  # every block is on the device: the host source is no longer read
+    return ff, out_planes, plan
 
 
 def HankelTransform(ogrid, rgrid, FField, distance, rgrid_FF, integrator=trapezoidal_integrator,

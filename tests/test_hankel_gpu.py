@@ -183,3 +183,35 @@ def test_stage1_tensor_cores_match_cuda_cores(gpu_lib, n_r, near):
     assert per_harmonic(ff_tc, ff64.cpu().numpy()) < FAST_TOL
     for k in (0, len(zg) - 1):
         assert per_harmonic(out["tc"][1][k].cpu().numpy(), p64[k].cpu().numpy()) < FAST_TOL
+
+
+@pytest.mark.parametrize("n_omega,n_r", [(600, 256), (513, 130)], ids=["600 frequencies", "513 frequencies, odd block"])
+def test_streamed_host_source_matches_device_source(gpu_lib, monkeypatch, n_omega, n_r):
+    """A pinned host source is uploaded in blocks of STREAM_BLOCK frequencies on a second stream
+    while the blocks already on the device are computed; every frequency is independent and all
+    blocks share the plan of the whole range, so the far field and the series planes equal the
+    one-shot call on the same source on the device, bit for bit.  600 and 513 frequencies leave
+    a short last block (88 and 1)."""
+    from mma_gb300 import hankel as H
+
+    omega0 = 0.057 / 2.4188843265857e-17
+    rg = np.linspace(0.0, 200e-6, n_r)
+    zg = np.linspace(-5e-3, 5e-3, 21)
+    og = np.linspace(10 * omega0, 42 * omega0, n_omega)
+    rho = np.linspace(0.0, 5e-3, 40)
+    rng = np.random.default_rng(n_omega)
+    S = np.exp(-(rg / 50e-6) ** 2)[None, None, :] * np.exp(1j * rng.uniform(0, 6.28, (len(zg), n_omega)))[:, :, None]
+    host = torch.tensor(S, dtype=torch.complex64).pin_memory()
+    pre = np.exp(1j * np.linspace(0, 1, len(zg)))[:, None] * np.exp(-0.1j * np.arange(n_omega) / n_omega)[None, :]
+    calls = []
+    real = H._far_field_streamed
+    monkeypatch.setattr(H, "_far_field_streamed", lambda *a, **k: calls.append(1) or real(*a, **k))
+    ff_h, pl_h, plan_h = H.far_field(og, rg, zg, rho, host, 1.0, pre, True, planes=(0, -1), form="fast")
+    assert calls, "the streamed path did not run"
+    ff_d, pl_d, plan_d = H.far_field(og, rg, zg, rho, host.cuda(), 1.0, pre, True, planes=(0, -1), form="fast")
+    torch.cuda.synchronize()
+    assert plan_h["n_terms"] == plan_d["n_terms"]
+    assert torch.equal(ff_h, ff_d)
+    assert sorted(pl_h) == sorted(pl_d)
+    for k in pl_d:
+        assert torch.equal(pl_h[k], pl_d[k])
