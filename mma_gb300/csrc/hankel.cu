@@ -142,13 +142,15 @@ __global__ void fast_wr_tables(mma_hankel_problem P, const double* og, const dou
 
 // Stage 1 through a shared-memory ring, for complex64 sources whose rows start on 16-byte
 // boundaries (rows of an even number of radii at even strides) and pre-factors per (plane,
-// frequency).  One CTA per (frequency, 256 radii), one radius per thread, two CTAs per SM.
-// Thread 0 streams the source with 1-D bulk copies (one per plane: the plane's row of radii,
-// 2 KB) into a ring of `ns` stages of kG planes each, one mbarrier per stage, so that tens of KB
-// per SM are in flight whatever the register count; the stage kSlack stages back is refilled
-// once every warp has released it, which lets the warps drift that far apart.  A thread waits
-// once per stage and then accumulates its kG planes (independent chains the scheduler can
-// interleave):
+// frequency).  One CTA per (frequency, 256 radii), two CTAs per SM: eight consumer warps, one
+// radius per thread, and a producer warp whose lane 0 streams the source with 1-D bulk copies
+// (one per plane: the plane's row of radii, 2 KB) into a ring of `ns` stages of kG planes each,
+// one full and one empty mbarrier per stage, so that tens of KB per SM are in flight whatever the
+// register count.  A consumer warp releases a stage as soon as it has read its values, and the
+// producer refills the slot with the stage ns later once all eight have; it does no other work,
+// so the refills do not wait for a consumer's arithmetic (with the producer in a consumer warp
+// the kernel took 139.8 against 108.3 us on the 268 MB small_ff case).  A consumer waits once per
+// stage and then accumulates its kG planes (independent chains the scheduler can interleave):
 //   B_m = e^{-i k r^2 u_ref} r w_r sum_k tau_k v_k^m pre_k e^{-i delta_k} S_k,
 //   delta_k = k r^2 (u_k - u_ref),  u = 1/(2 D),
 // i.e. the near-field phase e^{-i k r^2 u_k} split into a per-thread reference factor, applied
@@ -159,11 +161,10 @@ __global__ void fast_wr_tables(mma_hankel_problem P, const double* og, const dou
 // float4 quads from shared memory; every 16 planes they are added into FP32 totals kept in
 // shared memory (each thread its own column), which leaves the registers to the partial sums.
 // Every wait is bounded; on a timeout the CTA stops, sets *status and writes NaN into its B values.
-constexpr int kRingR = 256;  // radii per CTA, one per thread
+constexpr int kRingR = 256;  // radii per CTA, one per consumer thread
 constexpr int kG = 4;        // planes per ring stage
-constexpr int kSlack = 2;    // stages the warps may drift apart
 template <int MM>
-__global__ void __launch_bounds__(kRingR, 2)
+__global__ void __launch_bounds__(kRingR + 32, 2)
     fast_stage1_ring(mma_hankel_problem P, const float2* __restrict__ src, const double2* __restrict__ pre,
                      const float* __restrict__ ptab, const float2* __restrict__ ktab,
                      const float4* __restrict__ rtab, float2 u_ref, float2* Bp, int ns, int* status)
@@ -210,8 +211,9 @@ __global__ void __launch_bounds__(kRingR, 2)
         const float* row = ptab + (q / MQ) * RW + (q % MQ) * 4;
         coef[q] = make_float4(row[0], row[1], row[2], row[3]);
     }
+    if (t < kRingR)
 #pragma unroll
-    for (int q = 0; q < 2 * MQ; q++) tots[q * kRingR + t] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int q = 0; q < 2 * MQ; q++) tots[q * kRingR + t] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();  // s_dumax initialised
     {
         unsigned mx = 0u;  // max |u_k - u_ref| as float bits (non-negative floats order as integers)
@@ -224,7 +226,7 @@ __global__ void __launch_bounds__(kRingR, 2)
         atomicMax(&s_dumax, mx);
     }
     __syncthreads();
-    int issued = n_st < ns ? n_st : ns;  // stages whose copies thread 0 has issued
+    int issued = n_st < ns ? n_st : ns;  // stages issued: the first ns by thread 0, the rest by the producer
     // ---------------------------------------------------------------- per-thread constants
     const bool active = t < cnt;
     const int64_t r = r0 + (active ? t : 0);
@@ -268,26 +270,37 @@ __global__ void __launch_bounds__(kRingR, 2)
         }
     };
     bool ok = true;
-    // ring slot and phase parity of stage j (s, ph) and of stage j - kSlack (sp, php), counted
-    // incrementally (no divisions); stage `issued` = (j - kSlack) + ns reuses slot sp
-    int s = 0, sp = 0;
-    uint32_t ph = 0, php = 0;
-    for (int j = 0; j < n_st; j++) {
-        if (j >= kSlack) {
-            if (t == 0 && issued < n_st) {  // refill slot sp (stage j - kSlack, released by every warp)
-                if (tc::mbar_wait_spin(&empty[sp], php, abort_s, kRingWaitNs)) {
-                    issue(issued, sp);
-                    issued++;
-                } else if (!*abort_s) {
-                    *abort_s = 1;
-                    atomicCAS(status, 0, 1);
+    if (t >= kRingR) {
+        // the producer warp: lane 0 refills each slot with the stage ns later as soon as every
+        // consumer warp has released it, then waits until its last copies have landed (on an abort
+        // too: the ring must outlive the copies in flight)
+        if (lane == 0) {
+            int sp = 0;
+            uint32_t php = 0;
+            for (int jj = issued; jj < n_st; jj++) {
+                if (!tc::mbar_wait_spin(&empty[sp], php, abort_s, kRingWaitNs)) {
+                    if (!*abort_s) {
+                        *abort_s = 1;
+                        atomicCAS(status, 0, 1);
+                    }
+                    break;
+                }
+                issue(jj, sp);
+                issued = jj + 1;
+                if (++sp == ns) {
+                    sp = 0;
+                    php ^= 1u;
                 }
             }
-            if (++sp == ns) {
-                sp = 0;
-                php ^= 1u;
-            }
+            for (int j = (issued > ns ? issued - ns : 0); j < issued; j++)
+                tc::mbar_wait(&full[j % ns], (uint32_t)(j / ns) & 1u, nullptr, kRingWaitNs);
         }
+        return;
+    }
+    // ring slot and phase parity of stage j, counted incrementally (no divisions)
+    int s = 0;
+    uint32_t ph = 0;
+    for (int j = 0; j < n_st; j++) {
         if (!tc::mbar_wait_spin(&full[s], ph, abort_s, kRingWaitNs)) {
             *abort_s = 1;
             atomicCAS(status, 0, 2);
@@ -328,9 +341,6 @@ __global__ void __launch_bounds__(kRingR, 2)
             }
         }
     }
-    if (t == 0 && !ok)  // after an abort, let the copies already issued land before the CTA leaves
-        for (int j = (issued > ns ? issued - ns : 0); j < issued; j++)
-            tc::mbar_wait(&full[j % ns], (uint32_t)(j / ns) & 1u, nullptr, kRingWaitNs);
     if (!active) return;
     // the per-thread factor r w_r e^{-i k r^2 u_ref}
     float2 bw = make_float2(rt.z, 0.f);
@@ -885,7 +895,7 @@ int ring_stages(const mma_hankel_problem* p, const void* src)
     const size_t stage = (size_t)kG * kRingR * 8 + 16;
     const size_t tables = (size_t)p->n_z * (MM * 4 + 16) + (size_t)MM * 8 * kRingR + 64;
     const size_t budget = 110 * 1024;
-    if (tables + 3 * kSlack * stage > budget) return 0;
+    if (tables + 4 * stage > budget) return 0;  // at least four stages
     const size_t ns = (budget - tables) / stage;
     return (int)(ns > 16 ? 16 : ns);
 }
@@ -920,14 +930,14 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
             if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return MMA_ERR_CUDA;
             const size_t sr = (size_t)ns * kG * kRingR * 8 + (size_t)MM * 8 * kRingR +
                               (size_t)p->n_z * (MM * 4 + 16) + 2 * (size_t)ns * 8 + 16;
-            cudaFuncSetAttribute(fast_stage1_ring<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr);
             float hi, lo;  // u_ref = 1/(2 d_ref) as a float pair
             const double u = 1.0 / (2.0 * plan->d_ref);
             hi = (float)u;
             lo = (float)(u - (double)hi);
             dim3 g1((unsigned)((p->n_r + kRingR - 1) / kRingR), (unsigned)p->n_omega);
-            fast_stage1_ring<MM><<<g1, kRingR, sr, st>>>(*p, static_cast<const float2*>(src), pre, ptab, ktab,
-                                                         rtab, make_float2(hi, lo), Bp, ns, status);
+            cudaFuncSetAttribute(fast_stage1_ring<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr);
+            fast_stage1_ring<MM><<<g1, kRingR + 32, sr, st>>>(*p, static_cast<const float2*>(src), pre, ptab, ktab,
+                                                              rtab, make_float2(hi, lo), Bp, ns, status);
         }
     }
     if (!ringed) {  // one thread per (frequency, radius) reading its planes directly
