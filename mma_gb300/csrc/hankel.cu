@@ -246,17 +246,19 @@ __global__ void __launch_bounds__(kRingR + 32, 2)
     // one plane: a = pre S e^{-i delta}, then the MM partial sums
     auto plane = [&](const float2 sv, const int kz, const int md) {
         const float4 pf = pinfo[kz];
-        float2 a = make_float2(fmaf(pf.x, sv.x, -pf.y * sv.y), fmaf(pf.x, sv.y, pf.y * sv.x));
+        // pre S as a packed pair: lane re pre.re S.re + pre.im (-S.im), lane im pre.re S.im + pre.im S.re
+        float2 a = __ffma2_rn(f2b(pf.x), sv, __fmul2_rn(f2b(pf.y), make_float2(-sv.y, sv.x)));
         if (md != 0) {
             float sn, cs;
             if (md == 1) {
-                sincos_small(kr2h * pf.z, sn, cs);
+                sincos_small_p(kr2h * pf.z, sn, cs);
             } else {  // the angle k r^2 (u_k - u_ref) in float-float, reduced mod 2 pi
                 const float th = kr2h * pf.z;
                 const float te = fmaf(kr2h, pf.z, -th) + fmaf(kr2h, pf.w, kr2l * pf.z);
                 sincos_reduced(reduce_2pi(th, te), sn, cs);
             }
-            a = make_float2(fmaf(a.x, cs, a.y * sn), fmaf(a.y, cs, -a.x * sn));
+            // a e^{-i delta}: lane re a.re cs + sn a.im, lane im a.im cs + sn (-a.re)
+            a = __ffma2_rn(a, f2b(cs), __fmul2_rn(f2b(sn), make_float2(a.y, -a.x)));
         }
         const float2 ax = make_float2(a.x, a.x), ay = make_float2(a.y, a.y);
         const float4* c4 = coef + kz * MQ;
@@ -300,46 +302,70 @@ __global__ void __launch_bounds__(kRingR + 32, 2)
     // ring slot and phase parity of stage j, counted incrementally (no divisions)
     int s = 0;
     uint32_t ph = 0;
-    for (int j = 0; j < n_st; j++) {
+    // add the 16-plane partial sums into the totals
+    auto flush = [&]() {
+#pragma unroll
+        for (int q = 0; q < MQ; q++) {
+            float4* tr = tots + (2 * q) * kRingR + t;
+            float4* ti = tots + (2 * q + 1) * kRingR + t;
+            float4 vr = *tr, vi = *ti;
+            const float2 r01 = __fadd2_rn(make_float2(vr.x, vr.y), pr[2 * q]);
+            const float2 r23 = __fadd2_rn(make_float2(vr.z, vr.w), pr[2 * q + 1]);
+            const float2 i01 = __fadd2_rn(make_float2(vi.x, vi.y), pim[2 * q]);
+            const float2 i23 = __fadd2_rn(make_float2(vi.z, vi.w), pim[2 * q + 1]);
+            *tr = make_float4(r01.x, r01.y, r23.x, r23.y);
+            *ti = make_float4(i01.x, i01.y, i23.x, i23.y);
+            pr[2 * q] = pr[2 * q + 1] = pim[2 * q] = pim[2 * q + 1] = make_float2(0.f, 0.f);
+        }
+    };
+    // wait for stage j's slot, read this thread's kG values and release the slot
+    auto take = [&](float2 (&sv)[kG]) -> bool {
         if (!tc::mbar_wait_spin(&full[s], ph, abort_s, kRingWaitNs)) {
             *abort_s = 1;
             atomicCAS(status, 0, 2);
-            ok = false;
-            break;
+            return false;
         }
-        const int k0 = j * kG;
-        float2 sv[kG];
 #pragma unroll
-        for (int g = 0; g < kG; g++) sv[g] = ring[((size_t)s * kG + g) * kRingR + t];  // rows beyond cnt: unused
+        for (int g = 0; g < kG; g++) sv[g] = ring[(s * kG + g) * kRingR + t];  // rows beyond cnt: unused
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&empty[s]);
-        if (k0 + kG <= Nz && mode == 1) {  // the common case: kG independent chains, no control flow
-#pragma unroll
-            for (int g = 0; g < kG; g++) plane(sv[g], k0 + g, 1);
-        } else {  // no near field, exact angles, or the last, partial stage (static indices keep sv in registers)
-#pragma unroll
-            for (int g = 0; g < kG; g++)
-                if (k0 + g < Nz) plane(sv[g], k0 + g, mode);
-        }
         if (++s == ns) {
             s = 0;
             ph ^= 1u;
         }
-        if ((j & (16 / kG - 1)) == 16 / kG - 1 || j == n_st - 1) {  // add the 16-plane sums into the totals
+        return true;
+    };
+    constexpr int kGroup = 16 / kG;  // stages per 16 planes
+    int j = 0;
+    // the common case, small near-field angles: groups of kGroup full stages, kG independent chains
+    // per stage and the totals updated after each group, with no per-stage tests
+    const int n_grp = mode == 1 ? Nz / 16 : 0;
+    for (int gi = 0; gi < n_grp && ok; gi++) {
 #pragma unroll
-            for (int q = 0; q < MQ; q++) {
-                float4* tr = tots + (2 * q) * kRingR + t;
-                float4* ti = tots + (2 * q + 1) * kRingR + t;
-                float4 vr = *tr, vi = *ti;
-                const float2 r01 = __fadd2_rn(make_float2(vr.x, vr.y), pr[2 * q]);
-                const float2 r23 = __fadd2_rn(make_float2(vr.z, vr.w), pr[2 * q + 1]);
-                const float2 i01 = __fadd2_rn(make_float2(vi.x, vi.y), pim[2 * q]);
-                const float2 i23 = __fadd2_rn(make_float2(vi.z, vi.w), pim[2 * q + 1]);
-                *tr = make_float4(r01.x, r01.y, r23.x, r23.y);
-                *ti = make_float4(i01.x, i01.y, i23.x, i23.y);
-                pr[2 * q] = pr[2 * q + 1] = pim[2 * q] = pim[2 * q + 1] = make_float2(0.f, 0.f);
+        for (int u = 0; u < kGroup; u++) {
+            float2 sv[kG];
+            if (!take(sv)) {
+                ok = false;
+                break;
             }
+#pragma unroll
+            for (int g = 0; g < kG; g++) plane(sv[g], (j + u) * kG + g, 1);
         }
+        j += kGroup;
+        if (ok) flush();
+    }
+    // the rest: no near field, exact angles, and the last planes (static indices keep sv in registers)
+    for (; ok && j < n_st; j++) {
+        float2 sv[kG];
+        if (!take(sv)) {
+            ok = false;
+            break;
+        }
+        const int k0 = j * kG;
+#pragma unroll
+        for (int g = 0; g < kG; g++)
+            if (k0 + g < Nz) plane(sv[g], k0 + g, mode);
+        if (j % kGroup == kGroup - 1 || j == n_st - 1) flush();
     }
     if (!active) return;
     // the per-thread factor r w_r e^{-i k r^2 u_ref}

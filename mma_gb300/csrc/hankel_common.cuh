@@ -81,6 +81,18 @@ __device__ __forceinline__ void sincos_small(float p, float& s, float& c)
     c = fmaf(p2, fmaf(p2, 4.16666667e-2f, -0.5f), 1.0f);
 }
 
+// sincos_small with the two polynomials as one packed pair, (cos p, sin p / p): each lane the
+// operations of sincos_small in the same order (the same bits)
+__device__ __forceinline__ void sincos_small_p(float p, float& s, float& c)
+{
+    const float p2 = p * p;
+    const float2 q2 = make_float2(p2, p2);
+    float2 cs = __ffma2_rn(q2, make_float2(4.16666667e-2f, 8.33333333e-3f), make_float2(-0.5f, -1.66666667e-1f));
+    cs = __ffma2_rn(q2, cs, make_float2(1.0f, 1.0f));
+    c = cs.x;
+    s = p * cs.y;
+}
+
 // J0 and J1 in FP32 from the rational/asymptotic approximations of Abramowitz & Stegun
 // 9.4.1, 9.4.4 (x < 3) and 9.4.3, 9.4.6 (x >= 3; modulus and phase, |error| < 1e-7 absolute),
 // with the phase argument x reduced mod 2 pi in float-float (x = yh + yl).  For x >= 3 the two
