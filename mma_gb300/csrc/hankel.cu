@@ -656,20 +656,29 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
 __global__ void series_plane_tables(mma_hankel_problem P, mma_hankel_fast_plan_t F, const double* zg,
                                     const int64_t* slot, int n_sel, int mm, int* sel_kz, float2* vsel)
 {
-    double v[kSeriesPlanes];
-    for (int i = 0; i < kSeriesPlanes; i++) {
-        int64_t kz = 0;
-        for (int64_t q = 0; q < P.n_z; q++)
-            if (slot[q] == (i < n_sel ? i : 0)) kz = q;
-        if (threadIdx.x == 0) sel_kz[i] = (int)kz;
-        const double lam = F.d_ref / (P.distance - zg[kz]);
-        v[i] = (1.0 - lam * lam) / F.sigma;
+    __shared__ int s_kz[kSeriesPlanes];  // the last plane holding each slot (0 if none)
+    __shared__ double s_v[kSeriesPlanes];
+    if (threadIdx.x < kSeriesPlanes) s_kz[threadIdx.x] = 0;
+    __syncthreads();
+    for (int64_t q = threadIdx.x; q < P.n_z; q += blockDim.x) {
+        const int64_t sl = slot[q];
+#pragma unroll
+        for (int i = 0; i < kSeriesPlanes; i++)
+            if (sl == (i < n_sel ? i : 0)) atomicMax(&s_kz[i], (int)q);
     }
+    __syncthreads();
+    if (threadIdx.x < kSeriesPlanes) {
+        const int i = threadIdx.x, kz = s_kz[i];
+        sel_kz[i] = kz;
+        const double lam = F.d_ref / (P.distance - zg[kz]);
+        s_v[i] = (1.0 - lam * lam) / F.sigma;
+    }
+    __syncthreads();
     for (int m = threadIdx.x; m < mm; m += blockDim.x) {
         double c0 = 1.0, c1 = 1.0;
         for (int q = 0; q < m; q++) {
-            c0 *= v[0];
-            c1 *= v[1];
+            c0 *= s_v[0];
+            c1 *= s_v[1];
         }
         vsel[m] = make_float2((float)c0, (float)c1);
     }
@@ -979,7 +988,7 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
             const int64_t nt = p->n_omega > p->n_r ? p->n_omega : p->n_r;
             fast_wr_tables<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(*p, og, rg, ktab, rtab);
         }
-        series_plane_tables<<<1, 64, 0, st>>>(*p, *plan, zg, slot, n_sel, MM, sel_kz, vsel);
+        series_plane_tables<<<1, 256, 0, st>>>(*p, *plan, zg, slot, n_sel, MM, sel_kz, vsel);
         dim3 ga((unsigned)((p->n_r + 255) / 256), (unsigned)p->n_omega, (unsigned)kSeriesPlanes);
         series_plane_a<MM><<<ga, 256, 0, st>>>(*p, ktab, rtab, ptab, src, pre, sel_kz, asel);
     }

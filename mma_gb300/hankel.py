@@ -422,13 +422,17 @@ def pre_factor_table(zgrid, ogrid, preset_gas="vacuum", pressure=1.0, absorption
 
 
 # ------------------------------------------------------------------------------ kernels
-def _dev(a, device):
-    if torch.is_tensor(a):  # already a tensor (on the device: no copy)
-        return a.to(device=device, dtype=torch.float64).contiguous()
-    a = np.ascontiguousarray(a, dtype=np.float64)
+def _dev(a, device, dtype=torch.float64):
+    """A grid or table on the device.  Host data goes through pinned memory as an asynchronous copy
+    on the current stream, so the host does not wait for the stream's earlier work."""
+    if torch.is_tensor(a):
+        if a.is_cuda:  # already on the device: no copy
+            return a.to(device=device, dtype=dtype).contiguous()
+        return a.to(dtype).contiguous().pin_memory().to(device, non_blocking=True)
+    a = np.ascontiguousarray(a, dtype=np.dtype(str(dtype).replace("torch.", "")))
     if not a.flags.writeable:  # e.g. a view of a read-only archive buffer: torch wants writable memory
         a = a.copy()
-    return torch.as_tensor(a, device=device)
+    return torch.from_numpy(a).pin_memory().to(device, non_blocking=True)
 
 
 TC_MIN_PLANES = 16  # from this many requested planes the fast form computes them on the tensor cores
@@ -450,7 +454,7 @@ STREAM_BLOCK = 256  # frequencies per block when a pinned host source is uploade
 
 
 def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_field=True, planes=(), form="plain",
-              tol=1e-9, stream=None, planes_via="auto", ff_via="auto", _events=None, _omega_max=None):
+              tol=1e-9, stream=None, planes_via="auto", ff_via="auto", _events=None, _omega_max=None, _grids=None):
     """Run the far-field kernels.  source: torch complex tensor [Nz, No, Nr] with r contiguous (on
     the GPU, or on the host: a host tensor is copied there first; a pinned host tensor, for the
     fast form with at most two planes, is uploaded in blocks of STREAM_BLOCK frequencies on a
@@ -485,23 +489,38 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
         raise ValueError("pre-factor must be [Nz, No] or [Nz, No, Nr]")
     prob = HankelProblem(No, Nr, Nz, len(rho), float(distance), int(bool(near_field)),
                          int(S.dtype == torch.complex128), S.stride(0), S.stride(1), int(radial))
-    og, rg, zg, rh = (_dev(a, dev) for a in (ogrid, rgrid, zgrid, rho))
+    strm = stream or torch.cuda.current_stream(dev)
+    with torch.cuda.stream(strm):  # uploads and allocations on the call's stream
+        return _far_field_on(lib, strm, prob, S, ogrid, rgrid, zgrid, rho, distance, pre_table, planes, form, tol,
+                             planes_via, ff_via, _events, _omega_max, _grids)
+
+
+def _far_field_on(lib, strm, prob, S, ogrid, rgrid, zgrid, rho, distance, pre_table, planes, form, tol, planes_via,
+                  ff_via, _events, _omega_max, _grids):
+    dev = S.device
+    Nz, No, Nr = S.shape
+    # _grids: the grids already on the device (the host arrays still give the plan)
+    og, rg, zg, rh = _grids if _grids is not None else (_dev(a, dev) for a in (ogrid, rgrid, zgrid, rho))
     pre = None
     if pre_table is not None:  # a device tensor is used in place; a host table is copied once per call
-        pre = pre_table.to(device=dev, dtype=torch.complex128).contiguous() if torch.is_tensor(pre_table) else \
-            torch.as_tensor(np.ascontiguousarray(pre_table, dtype=np.complex128), device=dev)
+        pre = _dev(pre_table, dev, torch.complex128)
     ff = torch.zeros(len(rho), No, dtype=torch.complex128, device=dev)
     planes = sorted(set(int(p) % Nz for p in planes))
     slot = None
     pl = None
     if planes:
-        s = np.full(Nz, -1, dtype=np.int64)
-        for i, p in enumerate(planes):
-            s[p] = i
-        slot = torch.as_tensor(s, device=dev)
+        if len(planes) <= 8:  # built on the device: no copy to queue behind other transfers
+            slot = torch.full((Nz,), -1, dtype=torch.int64, device=dev)
+            for i, p in enumerate(planes):
+                slot[p] = i
+        else:
+            s = np.full(Nz, -1, dtype=np.int64)
+            for i, p in enumerate(planes):
+                s[p] = i
+            slot = _dev(s, dev, torch.int64)
         # every element of a requested plane is written by each form's kernels
         pl = torch.empty(len(planes), len(rho), No, dtype=torch.complex128, device=dev)
-    st = ctypes.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
+    st = ctypes.c_void_p(strm.cuda_stream)
     ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
     plan_d = None
     if form == "plain":
@@ -541,12 +560,12 @@ def far_field(ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_f
                                                     rg.data_ptr(), zg.data_ptr(), S.data_ptr(), ptr(pre),
                                                     tcs.data_ptr(), ntc, st), "mma_hankel_planes_tc_prepare")
             if _events is not None:  # (start, end) CUDA events around the tensor-core kernel
-                _events[0].record(stream or torch.cuda.current_stream())
+                _events[0].record(strm)
             _check(lib.mma_hankel_planes_tc_run(ctypes.byref(prob), ctypes.byref(plan), og.data_ptr(), rg.data_ptr(),
                                                 rh.data_ptr(), slot.data_ptr(), len(planes), pl.data_ptr(),
                                                 tcs.data_ptr(), ntc, st), "mma_hankel_planes_tc_run")
             if _events is not None:
-                _events[1].record(stream or torch.cuda.current_stream())
+                _events[1].record(strm)
             if ff_planes:
                 _check(lib.mma_hankel_ff_from_planes(ctypes.byref(prob), zg.data_ptr(), slot.data_ptr(), pl.data_ptr(),
                                                      ff.data_ptr(), st), "mma_hankel_ff_from_planes")
@@ -581,7 +600,11 @@ def _far_field_streamed(ogrid, rgrid, zgrid, rho, source, distance, pre_table, n
         raise ValueError("source shape does not match the grids")
     with torch.cuda.stream(comp):
         S = torch.empty(source.shape, dtype=source.dtype, device=dev)
-        og = _dev(ogrid, dev)
+        # the grids and the pre-factor first, as plain (synchronous) copies: they land before any
+        # block is queued, and the blocks' calls take them from the device
+        og, rg, zg, rh = (a.to(device=dev, dtype=torch.float64) if torch.is_tensor(a) else
+                          torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)
+                          for a in (ogrid, rgrid, zgrid, rho))
         pre = None
         if pre_table is not None:
             pre = pre_table.to(device=dev, dtype=torch.complex128) if torch.is_tensor(pre_table) else \
@@ -607,7 +630,7 @@ def _far_field_streamed(ogrid, rgrid, zgrid, rho, source, distance, pre_table, n
             pre_b = None if pre is None else pre[:, a:b]
             ffb, plb, plan = far_field(og[a:b], rgrid, zgrid, rho, S[:, a:b], distance, pre_b, near_field, planes,
                                        form="fast", tol=tol, stream=comp, planes_via=planes_via, ff_via=ff_via,
-                                       _omega_max=omax)
+                                       _omega_max=omax, _grids=(og[a:b], rg, zg, rh))
             if ff is None:
                 ff = torch.empty(ffb.shape[0], No, dtype=ffb.dtype, device=dev)
                 out_planes = {p: torch.empty(v.shape[0], No, dtype=v.dtype, device=dev) for p, v in plb.items()}
