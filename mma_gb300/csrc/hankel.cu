@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 
 #include "../../include/mma_hankel.h"
 #include "../../include/mma_tdse.h"
@@ -485,7 +486,7 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
                                                         const double* og, const double* rg, const double* rho,
                                                         const float2* Bp, double2* ff, int rtile,
                                                         const float2* asel, const float2* vsel, int n_sel,
-                                                        double2* planes)
+                                                        double2* planes, float x_cut8, float x_cut4)
 {
     extern __shared__ __align__(16) float smem[];
     const int64_t o = blockIdx.y, Nr = P.n_r, Nrho = P.n_rho, No = P.n_omega;
@@ -517,6 +518,12 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float rh = 0.f, rl = 0.f;
     if (j < Nrho) split_d(rho[j], rh, rl);
+    // the series length per (warp, chunk of kChunk radii): sigma y / 2 <= x_cut8 (x_cut4) lets MM - 8
+    // (MM - 4) terms meet the plan's truncation bound, y <= (k r / d_ref)_max of the chunk times
+    // the warp's largest rho
+    constexpr int kChunk = 32;
+    __shared__ float s_krm[64];  // per chunk of the tile: the largest k r / d_ref
+    const float rho_w = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(rh))));
     float2 part = make_float2(0.f, 0.f), hi = part, lo = part;
     int cnt = 0;
     for (int64_t r0 = 0; r0 < Nr; r0 += rtile) {
@@ -536,6 +543,13 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
             if (SER)
 #pragma unroll
                 for (int i = 0; i < kSeriesPlanes; i++) As[i * rtile + q] = asel[((int64_t)i * No + o) * Nr + r0 + q];
+        }
+        __syncthreads();
+        if (threadIdx.x < (nt + kChunk - 1) / kChunk) {
+            const int64_t c0 = threadIdx.x * kChunk, c1 = c0 + kChunk < nt ? c0 + kChunk : nt;
+            float mx = 0.f;
+            for (int64_t q = c0; q < c1; q++) mx = fmaxf(mx, fabsf(kr[q].x));
+            s_krm[threadIdx.x] = mx * 1.000001f;  // k r / d_ref's low part and rounding: a hair above
         }
         __syncthreads();
         if (j < Nrho) {
@@ -566,8 +580,10 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
                     cnt = 0;
                 }
             };
-            int64_t q = 0;
-            for (; q + 1 < nt; q += 2) {
+            // radius pairs q, q + 1 in [qa, qb) with ML series terms
+            auto pairs = [&](auto MLc, int64_t qa, int64_t qb) {
+              constexpr int ML = decltype(MLc)::value;
+              for (int64_t q = qa; q + 1 < qb; q += 2) {
                 const float4 kk = kr4[q / 2];
                 const float2 kh = make_float2(kk.x, kk.z), kl = make_float2(kk.y, kk.w);
                 const float2 yh = __fmul2_rn(kh, f2b(rh));
@@ -590,7 +606,7 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
                     s1 = __ffma2_rn(make_float2(v.z, v.w), K1, K0);
                 }
 #pragma unroll
-                for (int m = 1; m + 1 < MM; m++) {
+                for (int m = 1; m + 1 < ML; m++) {
                     const float4 c = lds4(cm_s + 16u * m);
                     const float2 K2 = __ffma2_rn(make_float2(c.x, c.y), K1,
                                                  __fmul2_rn(__fmul2_rn(q2, make_float2(c.z, c.w)), K0));
@@ -607,8 +623,21 @@ __global__ void __launch_bounds__(kThreads, SER ? 2 : 3) fast_stage2(mma_hankel_
                 }
                 add_in(make_float2(sre.x, sim.x), q, make_float2(s0.x, s1.x));
                 add_in(make_float2(sre.y, sim.y), q + 1, make_float2(s0.y, s1.y));
+              }
+            };
+            const float hs = 0.5f * s * rho_w;
+            for (int64_t c0 = 0; c0 + 1 < nt; c0 += kChunk) {
+                const int64_t c1 = c0 + kChunk < nt ? c0 + kChunk : nt;
+                const float xc = hs * s_krm[c0 / kChunk];  // warp-uniform
+                if (MM > 8 && xc <= x_cut8)
+                    pairs(std::integral_constant<int, (MM > 8 ? MM - 8 : MM)>{}, c0, c1);
+                else if (MM > 4 && xc <= x_cut4)
+                    pairs(std::integral_constant<int, (MM > 4 ? MM - 4 : MM)>{}, c0, c1);
+                else
+                    pairs(std::integral_constant<int, MM>{}, c0, c1);
             }
-            if (q < nt) {  // an odd last radius
+            const int64_t q = nt - 1;
+            if (nt & 1) {  // an odd last radius (all MM terms)
                 const float2 kk = kr[q];
                 const float yh = kk.x * rh;
                 const float yl = fmaf(kk.x, rh, -yh) + fmaf(kk.x, rl, kk.y * rh);
@@ -919,6 +948,27 @@ extern "C" int mma_hankel_fast_status(const mma_hankel_problem* p, const mma_han
 }
 
 namespace {
+// The largest x = sigma y / 2 at which m series terms still meet the plan's truncation bound,
+// x^m / m! e^x <= trunc_bound (bisection; the bound grows with x); -1 if m < 2 (never taken).
+// Stage 2 takes fewer terms where the chunk's largest y is small enough, so every term of the
+// sum keeps the plan's bound.
+static float series_cut(const mma_hankel_fast_plan_t* plan, int m)
+{
+    if (m < 2) return -1.f;
+    auto bound = [m](double x) {
+        double t = 1.0;
+        for (int q = 1; q <= m; q++) t *= x / q;
+        return t * std::exp(x);
+    };
+    double lo = 0.0, hi = 0.5 * plan->sigma * plan->y_max;
+    if (bound(hi) <= plan->trunc_bound) return (float)hi;
+    for (int it = 0; it < 80; it++) {
+        const double mid = 0.5 * (lo + hi);
+        (bound(mid) <= plan->trunc_bound ? lo : hi) = mid;
+    }
+    return (float)(lo * (1.0 - 1e-6));
+}
+
 // Ring stages of stage 1 that fit next to its tables (0: the ring form does not apply here).
 template <int MM>
 int ring_stages(const mma_hankel_problem* p, const void* src)
@@ -1001,14 +1051,15 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
     while ((size_t)rows * rtile * sizeof(float2) + consts > budget && rtile > 32) rtile /= 2;
     const size_t s2 = (size_t)rows * rtile * sizeof(float2) + consts;
     dim3 g2((unsigned)((p->n_rho + kThreads - 1) / kThreads), (unsigned)p->n_omega);
+    const float cut8 = series_cut(plan, MM - 8), cut4 = series_cut(plan, MM - 4);
     if (ser) {
         cudaFuncSetAttribute(fast_stage2<MM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
         fast_stage2<MM, true><<<g2, kThreads, s2, st>>>(*p, *plan, og, rg, rho, Bp, ff, rtile, asel, vsel, n_sel,
-                                                         planes);
+                                                         planes, cut8, cut4);
     } else {
         cudaFuncSetAttribute(fast_stage2<MM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
         fast_stage2<MM, false><<<g2, kThreads, s2, st>>>(*p, *plan, og, rg, rho, Bp, ff, rtile, nullptr, nullptr, 0,
-                                                          nullptr);
+                                                          nullptr, cut8, cut4);
     }
     return cudaGetLastError() == cudaSuccess ? MMA_OK : MMA_ERR_CUDA;
 }
