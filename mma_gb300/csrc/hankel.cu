@@ -948,27 +948,6 @@ extern "C" int mma_hankel_fast_status(const mma_hankel_problem* p, const mma_han
 }
 
 namespace {
-// The largest x = sigma y / 2 at which m series terms still meet the plan's truncation bound,
-// x^m / m! e^x <= trunc_bound (bisection; the bound grows with x); -1 if m < 2 (never taken).
-// Stage 2 takes fewer terms where the chunk's largest y is small enough, so every term of the
-// sum keeps the plan's bound.
-static float series_cut(const mma_hankel_fast_plan_t* plan, int m)
-{
-    if (m < 2) return -1.f;
-    auto bound = [m](double x) {
-        double t = 1.0;
-        for (int q = 1; q <= m; q++) t *= x / q;
-        return t * std::exp(x);
-    };
-    double lo = 0.0, hi = 0.5 * plan->sigma * plan->y_max;
-    if (bound(hi) <= plan->trunc_bound) return (float)hi;
-    for (int it = 0; it < 80; it++) {
-        const double mid = 0.5 * (lo + hi);
-        (bound(mid) <= plan->trunc_bound ? lo : hi) = mid;
-    }
-    return (float)(lo * (1.0 - 1e-6));
-}
-
 // Ring stages of stage 1 that fit next to its tables (0: the ring form does not apply here).
 template <int MM>
 int ring_stages(const mma_hankel_problem* p, const void* src)

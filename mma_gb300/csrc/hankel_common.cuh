@@ -1,5 +1,7 @@
 // hankel_common.cuh -- helpers shared by the far-field kernels (hankel.cu, hankel_tc.cu).
 #pragma once
+
+#include <cmath>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -40,6 +42,27 @@ __device__ __forceinline__ void split_d(double v, float& hi, float& lo)
 {
     hi = (float)v;
     lo = (float)(v - (double)hi);
+}
+
+// The largest x = sigma y / 2 at which m series terms still meet the plan's truncation bound,
+// x^m / m! e^x <= trunc_bound (bisection; the bound grows with x); -1 if m < 2 (never taken).
+// Stage 2 takes fewer terms where the chunk's largest y is small enough, so every term of the
+// sum keeps the plan's bound.
+inline float series_cut(const mma_hankel_fast_plan_t* plan, int m)
+{
+    if (m < 2) return -1.f;
+    auto bound = [m](double x) {
+        double t = 1.0;
+        for (int q = 1; q <= m; q++) t *= x / q;
+        return t * std::exp(x);
+    };
+    double lo = 0.0, hi = 0.5 * plan->sigma * plan->y_max;
+    if (bound(hi) <= plan->trunc_bound) return (float)hi;
+    for (int it = 0; it < 80; it++) {
+        const double mid = 0.5 * (lo + hi);
+        (bound(mid) <= plan->trunc_bound ? lo : hi) = mid;
+    }
+    return (float)(lo * (1.0 - 1e-6));
 }
 
 // (yh + yl) reduced mod 2 pi with 2 pi = C1 + C2 + C3 (C1, C2 short enough that k*C is exact)

@@ -28,6 +28,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "../../include/mma_diag.h"
 #include "../../include/mma_hankel.h"
@@ -76,6 +77,9 @@ struct Params {
     const float2* rgf;        // [rpad] r as float-float (0 beyond n_r)
     const float2* krho;       // [n_omega][n_rho] w rho / (c d_ref) as float-float
     float inv_ymax, two_over_ymax;
+    // y at or below which MM - 8 (MM - 4) series terms meet the plan's truncation bound: a K-block
+    // whose largest y is below stores the higher terms of its A operand as zeros
+    float ycut8, ycut4;
 };
 
 __device__ __forceinline__ void fail(volatile int* abort_s, int* status, int code)
@@ -282,13 +286,31 @@ __global__ void __launch_bounds__(THREADS, 1)
             float2 a = J0, b = __fmul2_rn(u, J1);
             put2(0, a);
             put2(1, b);
+            // terms up to ML - 1 by the recurrence, the rest zeros (ML warp-uniform)
+            auto terms = [&](auto MLc) {
+                constexpr int ML = decltype(MLc)::value;
 #pragma unroll
-            for (int m = 1; m + 1 < MM; m++) {
-                const float2 n = __ffma2_rn(bc2((float)m * tw), b, neg2(__fmul2_rn(w, a)));
-                put2(m + 1, n);
-                a = b;
-                b = n;
-            }
+                for (int m = 1; m + 1 < MM; m++) {
+                    if (m + 1 < ML) {
+                        const float2 n = __ffma2_rn(bc2((float)m * tw), b, neg2(__fmul2_rn(w, a)));
+                        put2(m + 1, n);
+                        a = b;
+                        b = n;
+                    } else {
+                        uint8_t* const pa = sa[((m + 1) >> 1) & 3] + ((m + 1) >> 3) * 512 + ((m + 1) & 7) * 64;
+                        *reinterpret_cast<uint32_t*>(pa) = 0u;
+                        *reinterpret_cast<uint32_t*>(pa + A_BYTES) = 0u;
+                    }
+                }
+            };
+            const float ymx =
+                __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(fmaxf(fabsf(yh.x), fabsf(yh.y)))));
+            if (MM > 8 && ymx <= P.ycut8)
+                terms(std::integral_constant<int, (MM > 8 ? MM - 8 : MM)>{});
+            else if (MM > 4 && ymx <= P.ycut4)
+                terms(std::integral_constant<int, (MM > 4 ? MM - 4 : MM)>{});
+            else
+                terms(std::integral_constant<int, MM>{});
             fence_async_smem();
             __syncwarp();
             if (lane == 0) mbar_arrive(&full[s]);
@@ -1093,6 +1115,11 @@ extern "C" int mma_hankel_planes_tc_run(const mma_hankel_problem* p, const mma_h
     }
     P.inv_ymax = plan->y_max > 0.0 ? (float)(1.0 / plan->y_max) : 0.f;
     P.two_over_ymax = plan->y_max > 0.0 ? (float)(2.0 / plan->y_max) : 0.f;
+    {   // x = sigma y / 2 cut-offs of the shorter series, as y (-1: never)
+        const float x8 = series_cut(plan, L.mm - 8), x4 = series_cut(plan, L.mm - 4);
+        P.ycut8 = x8 >= 0.f && plan->sigma > 0.0 ? (float)(2.0 * x8 / plan->sigma) : -1.f;
+        P.ycut4 = x4 >= 0.f && plan->sigma > 0.0 ? (float)(2.0 * x4 / plan->sigma) : -1.f;
+    }
     switch (L.mm) {
         case 8: return launch_planes<8>(th, tl, P, st);
         case 16: return launch_planes<16>(th, tl, P, st);
