@@ -28,6 +28,12 @@ int mma_tc_selftest(const void *A, const void *B, float *D, int use_tma, int *st
  * B[16][8]^T (row-major FP32, device pointers); *status = 2 if the bounded wait for the MMA ran out. */
 int mma_s1tc_selftest(const float *A, const float *B, float *D, int *status, void *stream);
 
+/* Test of the bounded waits of mma_hankel_fast's ring stage 1: while `on` is set, the ring's
+ * copies are never issued, so every wait of the stage runs out after its 2 s limit; the call
+ * returns, its far field is NaN and mma_hankel_fast_status reports MMA_ERR_TIMEOUT.  Process-wide;
+ * for tests only. */
+int mma_hankel_test_ring_timeout(int on);
+
 #ifdef __cplusplus
 }
 #endif

@@ -168,7 +168,7 @@ template <int MM>
 __global__ void __launch_bounds__(kRingR + 32, 2)
     fast_stage1_ring(mma_hankel_problem P, const float2* __restrict__ src, const double2* __restrict__ pre,
                      const float* __restrict__ ptab, const float2* __restrict__ ktab,
-                     const float4* __restrict__ rtab, float2 u_ref, float2* Bp, int ns, int* status)
+                     const float4* __restrict__ rtab, float2 u_ref, float2* Bp, int ns, int* status, int no_issue)
 {
     static_assert(MM % 4 == 0 && MM <= 16, "ring stage 1 takes 4, 8, 12 or 16 terms");
     extern __shared__ __align__(16) uint8_t smem_raw[];
@@ -206,7 +206,8 @@ __global__ void __launch_bounds__(kRingR + 32, 2)
         *abort_s = 0;
         s_dumax = 0u;
         tc::fence_barrier_init();
-        for (int j = 0; j < n_st && j < ns; j++) issue(j, j);  // the first stages, before the tables
+        if (!no_issue)  // (no_issue: the test of the bounded waits, nothing is ever copied)
+            for (int j = 0; j < n_st && j < ns; j++) issue(j, j);  // the first stages, before the tables
     }
     for (int q = t; q < Nz * MQ; q += blockDim.x) {
         const float* row = ptab + (q / MQ) * RW + (q % MQ) * 4;
@@ -227,7 +228,7 @@ __global__ void __launch_bounds__(kRingR + 32, 2)
         atomicMax(&s_dumax, mx);
     }
     __syncthreads();
-    int issued = n_st < ns ? n_st : ns;  // stages issued: the first ns by thread 0, the rest by the producer
+    int issued = no_issue ? 0 : (n_st < ns ? n_st : ns);  // stages issued: the first ns by thread 0, then the producer
     // ---------------------------------------------------------------- per-thread constants
     const bool active = t < cnt;
     const int64_t r = r0 + (active ? t : 0);
@@ -280,7 +281,7 @@ __global__ void __launch_bounds__(kRingR + 32, 2)
         if (lane == 0) {
             int sp = 0;
             uint32_t php = 0;
-            for (int jj = issued; jj < n_st; jj++) {
+            for (int jj = no_issue ? n_st : issued; jj < n_st; jj++) {
                 if (!tc::mbar_wait_spin(&empty[sp], php, abort_s, kRingWaitNs)) {
                     if (!*abort_s) {
                         *abort_s = 1;
@@ -823,6 +824,9 @@ using namespace mma::hk;
 // tensor-core form measured slower and less accurate on config 3 (TF32 split precision, N = 16
 // MMAs that keep the tensor pipe about 20% busy), so it is not the default.
 static int g_stage1_mode = 1;
+// Test of the ring's bounded waits: when set, the ring's copies are never issued (every wait of
+// the call runs out after kRingWaitNs; the far field is NaN and the status word reports it).
+static int g_ring_no_issue = 0;
 
 extern "C" int mma_hankel_plain(const mma_hankel_problem* p, const double* ogrid, const double* rgrid,
                                 const double* zgrid, const double* rho, const void* source, const double* pre,
@@ -928,6 +932,12 @@ extern "C" size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem* p, con
     return asel_off(p, plan) + up256(sizeof(float2) * 2 * (size_t)p->n_omega * (size_t)p->n_r);
 }
 
+extern "C" int mma_hankel_test_ring_timeout(int on)
+{
+    g_ring_no_issue = on ? 1 : 0;
+    return MMA_OK;
+}
+
 extern "C" int mma_hankel_set_stage1(int mode)
 {
     if (mode != 0 && mode != 1) return MMA_ERR_ARG;
@@ -1001,7 +1011,8 @@ int launch_fast(const mma_hankel_problem* p, const mma_hankel_fast_plan_t* plan,
             dim3 g1((unsigned)((p->n_r + kRingR - 1) / kRingR), (unsigned)p->n_omega);
             cudaFuncSetAttribute(fast_stage1_ring<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr);
             fast_stage1_ring<MM><<<g1, kRingR + 32, sr, st>>>(*p, static_cast<const float2*>(src), pre, ptab, ktab,
-                                                              rtab, make_float2(hi, lo), Bp, ns, status);
+                                                              rtab, make_float2(hi, lo), Bp, ns, status,
+                                                              g_ring_no_issue);
         }
     }
     if (!ringed) {  // one thread per (frequency, radius) reading its planes directly

@@ -4,6 +4,7 @@ and the oracle.
 Plain form (FP64, the reference's arithmetic): relative error <= 1e-10 of the largest
 value, per output.  Fast form (multiplication theorem, FP32): per-harmonic relative L2
 error over rho <= 2e-5 (the stated bound of the chosen form), planes <= 2e-5."""
+import ctypes
 import glob
 import os
 
@@ -215,3 +216,34 @@ def test_streamed_host_source_matches_device_source(gpu_lib, monkeypatch, n_omeg
     assert sorted(pl_h) == sorted(pl_d)
     for k in pl_d:
         assert torch.equal(pl_h[k], pl_d[k])
+
+
+def test_ring_bounded_waits_run_out(gpu_lib):
+    """With the ring's copies switched off (the test switch of stage 1's bounded waits), every wait
+    runs out after its 2 s limit: the call returns, its far field is NaN (the loud failure), and
+    the next call in the same context gives the normal result bit for bit."""
+    from mma_gb300 import hankel as H
+
+    lib = gpu_lib
+    lib.mma_hankel_test_ring_timeout.argtypes = [ctypes.c_int]
+    lib.mma_hankel_test_ring_timeout.restype = ctypes.c_int
+    omega0 = 0.057 / 2.4188843265857e-17
+    rg = np.linspace(0.0, 200e-6, 256)
+    zg = np.linspace(-5e-3, 5e-3, 9)
+    og = np.linspace(10 * omega0, 42 * omega0, 3)
+    rho = np.linspace(0.0, 5e-3, 16)
+    rng = np.random.default_rng(11)
+    S = np.exp(-(rg / 50e-6) ** 2)[None, None, :] * np.exp(1j * rng.uniform(0, 6.28, (len(zg), len(og))))[:, :, None]
+    S = torch.tensor(S, dtype=torch.complex64, device="cuda")
+    ref, _, _ = H.far_field(og, rg, zg, rho, S, 1.0, None, True, form="fast")
+    assert torch.isfinite(ref).all()
+    assert lib.mma_hankel_test_ring_timeout(1) == 0
+    try:
+        bad, _, _ = H.far_field(og, rg, zg, rho, S, 1.0, None, True, form="fast")
+        torch.cuda.synchronize()
+    finally:
+        lib.mma_hankel_test_ring_timeout(0)
+    assert torch.isnan(bad).all()
+    good, _, _ = H.far_field(og, rg, zg, rho, S, 1.0, None, True, form="fast")
+    torch.cuda.synchronize()
+    assert torch.equal(good, ref)
