@@ -512,7 +512,7 @@ def _far_field_on(lib, strm, prob, S, ogrid, rgrid, zgrid, rho, distance, pre_ta
         if len(planes) <= 8:  # built on the device: no copy to queue behind other transfers
             slot = torch.full((Nz,), -1, dtype=torch.int64, device=dev)
             for i, p in enumerate(planes):
-                slot[p] = i
+                slot[p:p + 1].fill_(i)  # a fill kernel (no host copy, so a graph capture takes it)
         else:
             s = np.full(Nz, -1, dtype=np.int64)
             for i, p in enumerate(planes):
@@ -639,6 +639,44 @@ def _far_field_streamed(ogrid, rgrid, zgrid, rho, source, distance, pre_table, n
                 out_planes[p][:, a:b] = v
     landed[-1].synchronize()  # every block is on the device: the host source is no longer read
     return ff, out_planes, plan
+
+
+class FarFieldPlan:
+    """The fast form of far_field for one set of inputs, recorded once as a CUDA graph and replayed:
+    the same kernels and the same result as far_field(..., form="fast"), without the host's work
+    per call (the plan, the uploads of the grids, some ten launches).  The source and the
+    pre-factor table stay on the device where they are; replay() recomputes from their current
+    contents, so a new source of the same shape is copied into `source` before a replay.  Up to
+    SERIES_PLANES requested planes (the entry and exit planes); more planes take far_field."""
+
+    def __init__(self, ogrid, rgrid, zgrid, rho, source, distance, pre_table=None, near_field=True, planes=(),
+                 tol=1e-9):
+        if not source.is_cuda:
+            raise ValueError("the source of a FarFieldPlan lives on the device")
+        if len(set(planes)) > SERIES_PLANES:
+            raise ValueError("a FarFieldPlan computes at most %d planes; far_field computes more" % SERIES_PLANES)
+        dev = source.device
+        self.source = source
+        host = [np.ascontiguousarray(_np(a), dtype=np.float64) for a in (ogrid, rgrid, zgrid, rho)]
+        self._grids = tuple(torch.as_tensor(a, device=dev) for a in host)  # kept: the graph reads them
+        self.pre = None if pre_table is None else _dev(pre_table, dev, torch.complex128)
+        kw = dict(pre_table=self.pre, near_field=near_field, planes=planes, form="fast", tol=tol,
+                  planes_via="direct", _grids=self._grids)
+        torch.cuda.synchronize(dev)
+        s = torch.cuda.Stream(device=dev)
+        s.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(s):  # one eager call first: the library's one-time state is made outside the capture
+            far_field(*host, source, distance, stream=s, **kw)
+        torch.cuda.current_stream(dev).wait_stream(s)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.ff, self.planes, self.plan = far_field(*host, source, distance, **kw)
+
+    def replay(self):
+        """Run the recorded far field on the current stream; returns (FF [Nrho, No], {plane: [Nrho, No]})."""
+        self.graph.replay()
+        return self.ff, self.planes
 
 
 def HankelTransform(ogrid, rgrid, FField, distance, rgrid_FF, integrator=trapezoidal_integrator,

@@ -247,3 +247,38 @@ def test_ring_bounded_waits_run_out(gpu_lib):
     good, _, _ = H.far_field(og, rg, zg, rho, S, 1.0, None, True, form="fast")
     torch.cuda.synchronize()
     assert torch.equal(good, ref)
+
+
+def test_far_field_plan_replays_the_call(gpu_lib):
+    """FarFieldPlan records the fast form once as a CUDA graph: a replay gives the far_field call's
+    far field and planes bit for bit, and after a new source is copied into the plan's source a
+    replay gives the call on that source."""
+    from mma_gb300 import hankel as H
+
+    omega0 = 0.057 / 2.4188843265857e-17
+    rg = np.linspace(0.0, 200e-6, 256)
+    zg = np.linspace(-5e-3, 5e-3, 17)
+    og = np.linspace(10 * omega0, 42 * omega0, 40)
+    rho = np.linspace(0.0, 5e-3, 32)
+    rng = np.random.default_rng(5)
+
+    def source():
+        S = np.exp(-(rg / 50e-6) ** 2)[None, None, :] * np.exp(1j * rng.uniform(0, 6.28, (len(zg), len(og))))[:, :, None]
+        return torch.tensor(S, dtype=torch.complex64, device="cuda")
+
+    pre = torch.tensor(np.exp(1j * np.linspace(0, 1, len(zg)))[:, None] * np.exp(-0.1j * np.arange(len(og)))[None, :],
+                       dtype=torch.complex128, device="cuda")
+    S = source()
+    plan = H.FarFieldPlan(og, rg, zg, rho, S, 1.0, pre, True, planes=(0, -1))
+    ff, pl = plan.replay()
+    ref, ref_pl, _ = H.far_field(og, rg, zg, rho, S, 1.0, pre, True, planes=(0, -1), form="fast")
+    torch.cuda.synchronize()
+    assert torch.equal(ff, ref)
+    for k in ref_pl:
+        assert torch.equal(pl[k], ref_pl[k])
+    S.copy_(source())
+    ff2, _ = plan.replay()
+    ref2, _, _ = H.far_field(og, rg, zg, rho, S, 1.0, pre, True, planes=(0, -1), form="fast")
+    torch.cuda.synchronize()
+    assert not torch.equal(ref2, ref)
+    assert torch.equal(ff2, ref2)
