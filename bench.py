@@ -980,9 +980,13 @@ def main():
             "frac_of_fp64_peak": achieved / r64["peak"] if r64.get("peak") else None,
             "flops_per_site_step": FLOPS_PER_SITE_STEP,
             "fp32_instructions_per_site_step": prof.get("thread_instructions_per_site_step"),
+            # the binding resource of the double-word arithmetic, from the committed ncu capture of
+            # the same kernel (small_df workload, profiles/tdse_df64_propagate_small.md)
+            "fp32_pipe_active_frac_ncu": (prof.get("fp32_pipe_active_pct") or 0.0) / 100.0 or None,
             "note": "achieved counts the 72 algorithmic FP64-equivalent flop per site-step; the kernel carries "
-                    "each in double-word FP32 arithmetic (about 10 FP32 instructions per operation), so the "
-                    "FP32 issue rate, not this fraction, is its ceiling"}
+                    "each in double-word FP32 arithmetic (about 10 FP32 instructions per operation), so its "
+                    "ceiling is the FP32 pipe (fp32_pipe_active_frac_ncu: the share of cycles the pipe was busy "
+                    "in the ncu capture), not this fraction"}
     a64 = FLOPS_PER_SITE_STEP * site_steps / (r64["kernel_ms"] * 1e-3)
     a_c64 = FLOPS_PER_SITE_STEP * site_steps / (r["kernel_ms"] * 1e-3)
     target = 1e-6
