@@ -798,23 +798,27 @@ def run_ours(args, rank, world, precision):
     host_series = torch.empty(plan.outputs.shape, dtype=torch.float64).pin_memory()
     host_F = torch.empty(res0["Fsourceterm"].shape, dtype=torch.complex128).pin_memory()
     host_M2 = torch.empty(res0["FsourcetermM2"].shape, dtype=torch.float64).pin_memory()
-    e2e_ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-    e_ms = []
+    # events: start, fields on the device, batch done, results on the host
+    e2e_ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    e_ms, e_parts = [], []
     clk_e2e = ClockSampler(dev.index)
     clk_e2e.__enter__()
     for it in range(1 + max(2, min(args.steps, 3))):  # the first pass is an untimed warm-up
         l2_flush(flush)
         e2e_ev[0].record(stream)
         plan.load_fields(host_fields)  # host -> device copy of this step's fields
+        e2e_ev[1].record(stream)
         plan.replay()
+        e2e_ev[2].record(stream)
         r_ = plan.result()
         host_series.copy_(plan.outputs, non_blocking=True)
         host_F.copy_(r_["Fsourceterm"], non_blocking=True)
         host_M2.copy_(r_["FsourcetermM2"], non_blocking=True)
-        e2e_ev[1].record(stream)
+        e2e_ev[3].record(stream)
         torch.cuda.synchronize()
         if it > 0:
-            e_ms.append(e2e_ev[0].elapsed_time(e2e_ev[1]))
+            e_ms.append(e2e_ev[0].elapsed_time(e2e_ev[3]))
+            e_parts.append([e2e_ev[i].elapsed_time(e2e_ev[i + 1]) for i in range(3)])
     clk_e2e.__exit__(None, None, None)
     e2e_ms = float(np.mean(e_ms))
     d2h = host_series.numel() * 8 + host_F.numel() * 16 + host_M2.numel() * 8
@@ -836,6 +840,7 @@ def run_ours(args, rank, world, precision):
                cta_threads=int(grids.c64_threads[0]), m32=int(grids.m32[0]), autotune=autotune.last_report(),
                dft=autotune.dft_choice(S),
                clocks=clk.summary(), e2e_ms=e2e_ms, e2e_ms_each=e_ms, e2e_clocks=clk_e2e.summary(),
+               e2e_parts_ms=[float(np.median([p[i] for p in e_parts])) for i in range(3)],
                h2d=host_fields.numel() * 8, d2h=d2h,
                t=t, fields=fields_np, spectrum=res["Fsourceterm"], omega=res["omegagrid"],
                sourceterm=res["sourceterm"])
@@ -1000,6 +1005,10 @@ def main():
                              "algorithmic_tflops": achieved / 1e12,
                              "e2e_site_steps_per_s": world * site_steps / (rdf["e2e_ms"] * 1e-3),
                              "e2e_ms_each": rdf["e2e_ms_each"], "e2e_clocks": rdf["e2e_clocks"],
+                             "e2e_parts_ms": {"fields_in": rdf["e2e_parts_ms"][0], "batch": rdf["e2e_parts_ms"][1],
+                                              "results_out": rdf["e2e_parts_ms"][2],
+                                              "d2h_gb_per_s": rdf["d2h"] / (rdf["e2e_parts_ms"][2] * 1e-3) / 1e9
+                                              if rdf["e2e_parts_ms"][2] > 0 else None},
                              "error_vs_fp64": err_df,
                              "meets_plateau_target": err_df["plateau_rel_err_max"] <= target},
         "tdse_chosen_c64": {"site_steps_per_s": r["value"], "ms_per_step": r["ms_per_step"],
