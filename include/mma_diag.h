@@ -4,6 +4,8 @@
 #ifndef MMA_DIAG_H
 #define MMA_DIAG_H
 
+#include "mma_hankel.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -33,6 +35,12 @@ int mma_s1tc_selftest(const float *A, const float *B, float *D, int *status, voi
  * returns, its far field is NaN and mma_hankel_fast_status reports MMA_ERR_TIMEOUT.  Process-wide;
  * for tests only. */
 int mma_hankel_test_ring_timeout(int on);
+
+/* The series cut-off behind the fast far field's choice of series length (host only, no device):
+ * the largest x = sigma y / 2 at which m terms still meet plan->trunc_bound, x^m / m! e^x <=
+ * trunc_bound; -1 for m < 2.  Stage 2 and the tensor-core generators take m = MM - 8 or MM - 4
+ * terms where a chunk's largest y is within it. */
+double mma_hankel_series_cut(const mma_hankel_fast_plan_t *plan, int m);
 
 #ifdef __cplusplus
 }

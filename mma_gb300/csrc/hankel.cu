@@ -932,6 +932,13 @@ extern "C" size_t mma_hankel_fast_scratch_bytes(const mma_hankel_problem* p, con
     return asel_off(p, plan) + up256(sizeof(float2) * 2 * (size_t)p->n_omega * (size_t)p->n_r);
 }
 
+// The series cut-off of m terms for a plan (host only): the largest x = sigma y / 2 at which m
+// terms meet the plan's truncation bound, -1 if m < 2.
+extern "C" double mma_hankel_series_cut(const mma_hankel_fast_plan_t* plan, int m)
+{
+    return plan ? (double)series_cut(plan, m) : -1.0;
+}
+
 extern "C" int mma_hankel_test_ring_timeout(int on)
 {
     g_ring_no_issue = on ? 1 : 0;

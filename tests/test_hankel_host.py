@@ -47,3 +47,38 @@ def test_library_far_field_switches_and_block_copy_arguments():
     assert lib.mma_hankel_copy_block(p, p, 0, 16, 16, None) != MMA_OK  # no planes
     assert lib.mma_hankel_copy_block(p, p, 2, 8, 16, None) != MMA_OK  # block wider than the plane pitch
     assert lib.mma_hankel_copy_block(p, p, 2, 16, 0, None) != MMA_OK  # empty block
+
+
+def test_series_cut_meets_the_plan_bound():
+    """The cut-offs behind the fast far field's series length (host only): at the cut-off x for m
+    terms, x^m / m! e^x stays within the plan's truncation bound, and 1e-5 above it exceeds it;
+    the cut-offs grow with m, and m = n_terms reaches the plan's own x_max."""
+    from math import exp, factorial
+
+    from mma_gb300 import hankel as H
+
+    lib = H._sig()
+    lib.mma_hankel_series_cut.argtypes = [ctypes.POINTER(H.FastPlan), ctypes.c_int]
+    lib.mma_hankel_series_cut.restype = ctypes.c_double
+    omega0 = 0.057 / 2.4188843265857e-17
+    z = np.ascontiguousarray(np.linspace(-5e-3, 5e-3, 256)[:-1])
+    plan = H.FastPlan()
+    assert lib.mma_hankel_fast_plan(z.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(z), 1.0, 42 * omega0,
+                                    200e-6, 5e-3, 1e-9, ctypes.byref(plan)) == MMA_OK
+    d = plan.as_dict()
+    M, tb = int(d["n_terms"]), float(d["trunc_bound"])
+    x_max = 0.5 * float(d["sigma"]) * float(d["y_max"])
+
+    def bound(x, m):
+        return x ** m / factorial(m) * exp(x)
+
+    cuts = {}
+    for m in (M - 8, M - 4):
+        x = lib.mma_hankel_series_cut(ctypes.byref(plan), m)
+        assert 0.0 < x < x_max
+        assert bound(x, m) <= tb * (1 + 1e-9)
+        assert bound(x * (1 + 1e-5), m) > tb
+        cuts[m] = x
+    assert cuts[M - 8] < cuts[M - 4]
+    assert abs(lib.mma_hankel_series_cut(ctypes.byref(plan), M) - x_max) <= 1e-6 * x_max
+    assert lib.mma_hankel_series_cut(ctypes.byref(plan), 1) == -1.0
